@@ -1,0 +1,321 @@
+"""Benchmark: attempted spin flips/ns of the GPU Metropolis hot path.
+
+Workload (N=1 line): plain 3D Ising Metropolis on an sc 256x256x256 lattice
+(16,777,216 spins, int8 payload, full PBC, J=1, h=0, random +-1 start from a
+seed) -- the single-lattice configuration the headline metric is quoted on.
+One step = 200 measured sweeps (per-sweep E and |M| reduced on the device,
+as the reference's instruments do after every sweep) at the next temperature
+of the 21-point ladder 5.5 -> 3.5 (CoolDown(5.5, 3.5, 0.1), replayed with the
+reference's FP loop).  Synthetic data: the lattice and its initial state are
+generated from a seed; no external dataset exists for this workload.
+
+Timing: CUDA events on the engine's stream around every step; L2 is flushed
+(a 256 MiB write) between steps outside the events; the lattice itself
+(16.8 MB) is L2-resident within a step.  `value` = total attempted flips /
+summed step time (device-resident state); `e2e` = the same metric through the
+C ABI with host buffers: host->device copy of the state from pinned memory,
+the sweeps, device->host copy of the per-sweep E/|M| and of the final state.
+
+--impl reference times the reference algorithm on the host cores (the C
+restatement in oracle/ -- Rust is absent, so the crate cannot be built):
+independent random-site Metropolis chains on the same lattice, one per core.
+
+Multi-GPU: the path does not need a collective; --gpus N runs N independent
+replicas (one per rank/GPU, torchrun) and reports the aggregate.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+for p in (os.path.join(REPO, "vegas-rs_gb300"), REPO):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+L = 256
+SWEEPS_PER_STEP = 200
+SEED = 20261203
+BYTES_PER_FLIP = 3.0  # int8 sc checkerboard: (C + 1) x 1 byte, C = 2 colour passes
+METRIC = "attempted spin flips/ns on 1 GB300 (batched vs plain GPU path), % HBM roofline"
+
+
+def ladder():
+    out, t = [], 5.5
+    while True:  # CoolDown::run (src/program.rs:202-211)
+        out.append(t)
+        t -= 0.1
+        if t < 3.5:
+            break
+    return out
+
+
+def peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def read_profile_traffic():
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary."""
+    path = os.path.join(REPO, "profiles", "ising_sc_pass_256cubed.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].strip())
+    except OSError:
+        pass
+    return None
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        load = [s for s in sm if s > 0.5 * max(sm)] if sm else []
+        return {"sm_mhz": statistics.median(load) if load else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_baseline_sample(threads=1, sweeps=2):
+    """ref_cpu (C restatement of the reference's Metropolis) on the same 256^3 lattice."""
+    import oracle as O
+
+    H = O.Hamiltonian(has_exchange=1, J=1.0, compound=0)
+    lat = O.lattice("sc", L, L, L)
+    flips, dt = O.ref_parallel(lat, 0, H, 4.5, sweeps, threads, seed=SEED, measure=True)
+    return flips / (dt * 1e9), dt
+
+
+def run_reference(args, rank):
+    """--impl reference: the reference algorithm on all host cores."""
+    if rank != 0:
+        return
+    import oracle as O
+
+    oracle_lib = O.lib()
+    del oracle_lib
+    threads = os.cpu_count() or 1
+    H = O.Hamiltonian(has_exchange=1, J=1.0, compound=0)
+    lat = O.lattice("sc", L, L, L)
+    # bounded sample: each step is one measured reference sweep of the
+    # 256^3 lattice on every host core (lattice setup included once per call)
+    steps = max(1, min(args.steps, 3))
+    flips, dt = O.ref_parallel(lat, 0, H, 4.5, steps, threads, seed=SEED, measure=True)
+    v = flips / (dt * 1e9)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "flips/ns", "n_gpus": args.gpus,
+        "steps": steps, "warmup": 0, "ms_per_step": dt * 1e3 / steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "ising-sc-256^3-pbc-J1-h0 (reference random-site Metropolis, CLI measurement)",
+                   "lattice": [L, L, L], "threads": threads},
+        "cpu_baseline": {"value": v, "unit": "flips/ns", "cores": threads, "kind": "port",
+                         "sample": f"{steps} measured sweeps per core, one 256^3 lattice per core"},
+        "e2e": {"value": v, "unit": "flips/ns", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "gpu_launches": 0,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--lattice", type=int, default=L)
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+
+    import numpy as np
+    import torch
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+
+    import vegas_gb300 as V
+
+    n_l = args.lattice
+    lat = V.Lattice.sc(n_l, n_l, n_l)
+    H = V.hamiltonian(V.Exchange(1.0))
+    eng = V.Engine(lat, H, spin=V.SPIN_ISING, seed=SEED, replica=rank, device=local_rank)
+    eng.init_random()
+    info = eng.info()
+    N = lat.n_sites
+    stream = torch.cuda.ExternalStream(eng.stream())
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    temps = ladder()
+
+    def flush_l2():
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+
+    def step(k):
+        eng.set_thermostat(temps[k % len(temps)])
+        eng.sweeps_async(SWEEPS_PER_STEP, measure=True)
+
+    for k in range(args.warmup):
+        step(k)
+    eng.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    stops = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    launches_per_step = SWEEPS_PER_STEP * info.n_colours + (SWEEPS_PER_STEP + 63) // 64
+    with Clocks(local_rank) as clk:
+        wall0 = time.perf_counter()
+        for k in range(args.steps):
+            flush_l2()
+            starts[k].record(stream)
+            step(args.warmup + k)
+            stops[k].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+    eng.read_sums(SWEEPS_PER_STEP)  # results of the last step reach the host
+    step_ms = [a.elapsed_time(b) for a, b in zip(starts, stops)]
+    dev_ms = sum(step_ms)
+    if dist:
+        t = torch.tensor([dev_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_ms = float(t.item())
+        dist.barrier()
+    flips_rank = float(N) * SWEEPS_PER_STEP * args.steps
+    value = flips_rank * world / (dev_ms * 1e6)
+
+    # dominant kernel: one colour pass, timed per launch with CUDA events
+    pass_ms, sweep_ms = eng.time_passes(50, measure=True)
+    alg_bytes_per_launch = 1.5 * N  # read both classes (N bytes), write one class (N/2)
+    achieved = alg_bytes_per_launch / (pass_ms * 1e-3) / 1e9
+    peak, peak_kind = peaks()
+    traffic = read_profile_traffic()
+
+    # end to end through the C ABI with host buffers
+    import ctypes as C
+
+    hbuf = C.c_void_p()
+    V._check(V.lib().vg_host_alloc(C.byref(hbuf), N))
+    obuf = C.c_void_p()
+    V._check(V.lib().vg_host_alloc(C.byref(obuf), 16 * SWEEPS_PER_STEP))
+    host_state = np.ctypeslib.as_array((C.c_int8 * N).from_address(hbuf.value))
+    host_state[:] = eng.get_state()
+    Eo = (C.c_double * SWEEPS_PER_STEP).from_address(obuf.value)
+    Mo = (C.c_double * SWEEPS_PER_STEP).from_address(obuf.value + 8 * SWEEPS_PER_STEP)
+    e2e_steps = max(3, min(args.steps, 10))
+    lib = V.lib()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(e2e_steps):
+        eng.set_thermostat(temps[k % len(temps)])
+        V._check(lib.vg_set_state(eng._h, hbuf, C.c_int64(N)), eng._h)
+        V._check(lib.vg_sweeps(eng._h, C.c_uint64(SWEEPS_PER_STEP), 1, Eo, Mo), eng._h)
+        V._check(lib.vg_get_state(eng._h, hbuf, C.c_int64(N)), eng._h)
+    e2e_s = time.perf_counter() - t0
+    e2e_value = float(N) * SWEEPS_PER_STEP * e2e_steps * world / (e2e_s * 1e9)
+    lib.vg_host_free(hbuf)
+    lib.vg_host_free(obuf)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, dt = cpu_baseline_sample(threads=1, sweeps=2)
+        cpu = {"value": v, "unit": "flips/ns", "cores": 1, "kind": "port",
+               "sample": f"2 measured reference sweeps of the 256^3 lattice on one core ({dt:.1f} s of sweeping)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "flips/ns", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int8", "data": "synthetic",
+            "config": {"workload": f"ising-sc-{n_l}^3-pbc-J1-h0 plain single lattice, checkerboard kernels",
+                       "lattice": [n_l, n_l, n_l], "spins": N, "sweeps_per_step": SWEEPS_PER_STEP,
+                       "temperatures": "CoolDown(5.5, 3.5, 0.1) ladder, one per step",
+                       "measurement": "per-sweep E and |M| on device",
+                       "l2": "flushed between steps (256 MiB write, outside the events); the 16.8 MB lattice is "
+                             "L2-resident within a step",
+                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                       "path": {1: "generic", 2: "structured"}.get(info.path, "?")},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "kernel": "ising_sc_kernel (one colour pass)", "pass_ms": pass_ms,
+                         "alg_bytes_per_launch": alg_bytes_per_launch, "peak_kind": peak_kind,
+                         "note": "frac > 1 means the lattice is served from L2"},
+            "e2e": {"value": e2e_value, "unit": "flips/ns", "h2d_bytes_per_step": N,
+                    "d2h_bytes_per_step": N + 16 * SWEEPS_PER_STEP},
+            "gpu_launches": launches_per_step * args.steps,
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "wall_s": wall,
+            "sweep_ms": sweep_ms,
+        }
+        print(json.dumps(line), flush=True)
+    eng.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

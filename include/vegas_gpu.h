@@ -1,0 +1,197 @@
+/*
+ * vegas_gpu.h -- C ABI of the GB300 (sm_103a) Metropolis engine for vegas.
+ *
+ * The engine replaces the hot path of the vegas crate:
+ *   Integrator<S>::step            src/integrator.rs:40-49  (trait)
+ *   MetropolisFlipIntegrator::step src/integrator.rs:113-137
+ *   MetropolisIntegrator::step     src/integrator.rs:66-92
+ *   Hamiltonian::energy/total      src/energy.rs:45-60, terms :62-257
+ *   State / Spin / Field           src/state.rs:28-318
+ *   Thermostat                     src/thermostat.rs:17-79
+ * and the per-sweep measurement done by the instruments
+ *   StatSensor::after_step         src/instrument.rs:133-141
+ *   ObservableSensor::after_step   src/instrument.rs:254-262.
+ *
+ * Conventions
+ *   - Every function returns an int status (VG_OK = 0).  The library never
+ *     aborts and never falls back to the CPU: without a usable GPU it returns
+ *     VG_ERR_NO_DEVICE / VG_ERR_CUDA.
+ *   - A context owns its device memory and one CUDA stream.  A context is not
+ *     thread-safe; distinct contexts are independent.
+ *   - Host buffers belong to the caller and are copied.  Spin buffers are in
+ *     the lattice's site order: site = ((cz*ny + cy)*nx + cx)*nbasis + b.
+ *     Ising spins are int8 +1 (Up) / -1 (Down); Heisenberg spins are three
+ *     doubles (x, y, z) per site.
+ *   - Sweep t of a context draws its random numbers from Philox4x32-10 keyed by
+ *     (seed, replica) with counters (site, t, stream tag); (seed, sweep index)
+ *     is the whole RNG state, so vg_set_sweep_index resumes a run exactly.
+ */
+#ifndef VEGAS_GPU_H
+#define VEGAS_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VG_ABI_VERSION 1
+
+typedef struct vg_ctx vg_ctx;
+
+enum vg_status {
+  VG_OK = 0,
+  VG_ERR_INVALID_ARG = 1,
+  VG_ERR_CUDA = 2,
+  VG_ERR_TIMEOUT = 3,
+  VG_ERR_OOM = 4,
+  VG_ERR_UNSUPPORTED = 5,
+  VG_ERR_NO_DEVICE = 6
+};
+
+enum vg_spin_kind { VG_SPIN_ISING = 0, VG_SPIN_HEISENBERG = 1 };
+enum vg_unit_cell { VG_CELL_SC = 0, VG_CELL_BCC = 1, VG_CELL_FCC = 2 };
+/* FLIP: MetropolisFlipIntegrator (src/integrator.rs:99-138).
+ * RANDOM: MetropolisIntegrator, proposal Spin::rand (src/integrator.rs:56-92). */
+enum vg_proposal { VG_PROPOSE_FLIP = 0, VG_PROPOSE_RANDOM = 1 };
+/* Kernel family.  AUTO picks STRUCTURED when the lattice allows it. */
+enum vg_path { VG_PATH_AUTO = 0, VG_PATH_GENERIC = 1, VG_PATH_STRUCTURED = 2 };
+enum vg_precision { VG_FP32 = 0, VG_FP64 = 1 };
+
+/* Lattice::sc/bcc/fcc(1.0).expand(nx, ny, nz) with drop_x/y/z on the open
+ * axes (src/input.rs:296-322). */
+typedef struct {
+  int32_t cell;           /* vg_unit_cell */
+  int32_t nx, ny, nz;     /* unit cells per axis, >= 1 */
+  int32_t pbc_x, pbc_y, pbc_z;
+} vg_lattice_desc;
+
+/* A Hamiltonian assembled from the reference's terms (src/energy.rs):
+ *   Exchange::from_lattice(J)  per site -J sum_j s_i.s_j          (:176-206)
+ *   UniaxialAnisotropy(e, K)   per site +K (s.e)^2                (:108-112)
+ *   Zeeman                     per site zeeman_sign |B| (s.b)     (:147-151)
+ *   Gauge(g)                   per site g                         (:75-80)
+ *   cubic (extension, no reference counterpart)  -Kc (sx^4+sy^4+sz^4)
+ * compound = 1 selects Compound's total (sum_i energy(i), :55-59, :248-257);
+ * compound = 0 requires exactly one term and uses that term's own
+ * total_energy (Exchange halves :208-213, UniaxialAnisotropy drops K
+ * :114-120, Zeeman negates :153-160, Gauge N g). */
+typedef struct {
+  int32_t has_exchange;   double exchange;
+  int32_t has_anisotropy; double anisotropy; double anisotropy_axis[3];
+  int32_t has_zeeman;     double zeeman_sign; /* +1 reproduces the reference */
+  int32_t has_gauge;      double gauge;
+  int32_t has_cubic;      double cubic;
+  int32_t compound;
+} vg_hamiltonian_desc;
+
+typedef struct {
+  int32_t spin_kind;          /* vg_spin_kind */
+  int32_t proposal;           /* vg_proposal */
+  int32_t path;               /* vg_path */
+  int32_t precision;          /* vg_precision (Heisenberg only) */
+  uint32_t replica;           /* replica id mixed into the RNG counters */
+  int32_t threads_per_block;  /* 0 = library default */
+  int32_t blocks_per_sm;      /* 0 = library default (grid-stride cap) */
+  int32_t device;             /* -1 = current device */
+} vg_options;
+
+/* Raw per-sweep lattice sums (FP64), from which every total the reference
+ * reports is formed.  bond counts each bond once (with multiplicity). */
+typedef struct {
+  double bond;        /* sum over bonds s_i . s_j */
+  double anisotropy;  /* sum_i (s_i . e)^2 */
+  double zeeman;      /* sum_i s_i . b */
+  double cubic;       /* sum_i sx^4 + sy^4 + sz^4 */
+  double mx, my, mz;  /* magnetisation vector */
+  double accepted;    /* accepted proposals in the sweep */
+} vg_sums;
+
+typedef struct {
+  int64_t n_sites;
+  int32_t n_colours;
+  int32_t coordination;
+  int32_t path;               /* the path actually used */
+  int32_t precision;
+  int32_t grid_blocks;
+  int32_t threads_per_block;
+  int32_t sm_count;
+  int64_t device_bytes;       /* device memory held by the context */
+  uint64_t sweep_index;
+} vg_info;
+
+/* ---------------------------------------------------------------- status */
+const char* vg_status_string(int status);
+int vg_abi_version(void);
+int vg_device_count(int32_t* count);
+
+/* ------------------------------------------------------------- lifecycle */
+/* Defaults: flip proposal for Ising, random proposal for Heisenberg (the
+ * integrators src/input.rs:347-364 picks), AUTO path, FP32. */
+int vg_options_default(int32_t spin_kind, vg_options* out);
+int vg_ctx_create(const vg_lattice_desc* lattice, const vg_hamiltonian_desc* hamiltonian,
+                  int32_t spin_kind, uint64_t seed, vg_ctx** out);
+int vg_ctx_create_ex(const vg_lattice_desc* lattice, const vg_hamiltonian_desc* hamiltonian,
+                     const vg_options* options, uint64_t seed, vg_ctx** out);
+int vg_ctx_destroy(vg_ctx* ctx);
+int vg_ctx_info(const vg_ctx* ctx, vg_info* out);
+const char* vg_last_error(const vg_ctx* ctx);
+/* Run the context's work on a caller-owned cudaStream_t (NULL restores the
+ * context's own stream). */
+int vg_set_stream(vg_ctx* ctx, void* cuda_stream);
+int vg_get_stream(const vg_ctx* ctx, void** cuda_stream);
+
+/* ------------------------------------------------------ state and bath */
+/* State::rand_with_size (src/state.rs:260-262) on the device. */
+int vg_init_random(vg_ctx* ctx);
+int vg_set_state(vg_ctx* ctx, const void* host_spins, int64_t n_sites);
+int vg_get_state(vg_ctx* ctx, void* host_spins, int64_t n_sites);
+/* Thermostat::new(T, Field::new(orientation, magnitude)); T is clamped to
+ * f64::EPSILON (src/thermostat.rs:29-39) and |magnitude| is used
+ * (Field::magnitude, src/state.rs:219-221). For Ising only the sign of
+ * b_hat[2] matters (Up / Down). */
+int vg_set_thermostat(vg_ctx* ctx, double temperature, const double b_hat[3], double magnitude);
+int vg_set_sweep_index(vg_ctx* ctx, uint64_t sweep);
+int vg_get_sweep_index(const vg_ctx* ctx, uint64_t* sweep);
+
+/* ---------------------------------------------------------------- sweeps */
+/* n Metropolis sweeps (each attempts one update per site).  If measure, the
+ * per-sweep total energy (with the desc's total semantics) and |M| are
+ * written to E_out[t] and M_out[t] (either may be NULL).  Synchronous. */
+int vg_sweeps(vg_ctx* ctx, uint64_t n, int32_t measure, double* E_out, double* M_out);
+/* Same, returning the raw per-sweep sums (out may be NULL). Synchronous. */
+int vg_sweeps_sums(vg_ctx* ctx, uint64_t n, vg_sums* out);
+/* Enqueue n sweeps on the context stream and return at once.  With measure,
+ * the per-sweep sums stay on the device; vg_read_sums fetches the last
+ * enqueued batch.  Used for device-resident timing. */
+int vg_sweeps_async(vg_ctx* ctx, uint64_t n, int32_t measure);
+int vg_read_sums(vg_ctx* ctx, uint64_t count, vg_sums* out);
+int vg_synchronize(vg_ctx* ctx);
+
+/* Run n sweeps with a CUDA event pair around every colour pass on the
+ * context stream; returns the mean pass duration and the mean sweep
+ * duration (ms).  The sweeps are real work (the sweep index advances). */
+int vg_time_passes(vg_ctx* ctx, uint64_t n, int32_t measure, double* mean_pass_ms, double* mean_sweep_ms);
+
+/* ---------------------------------------------------------- observables */
+int vg_current_sums(vg_ctx* ctx, vg_sums* out);
+int vg_total_energy(vg_ctx* ctx, double* energy);
+int vg_magnetization(vg_ctx* ctx, double m[3], double* magnitude);
+/* Total energy / |M| from raw sums with a context's Hamiltonian semantics. */
+int vg_energy_from_sums(const vg_ctx* ctx, const vg_sums* sums, double* energy, double* magnitude);
+
+/* ------------------------------------------------------- host utilities */
+/* Neighbour table of a lattice (nbr[i*zmax + k], -1 = absent) and its greedy
+ * colouring; pass NULL buffers to query n and zmax. */
+int vg_lattice_neighbours(const vg_lattice_desc* lattice, int32_t* nbr, int64_t capacity,
+                          int64_t* n_sites, int32_t* zmax);
+int vg_lattice_colouring(const vg_lattice_desc* lattice, int32_t* colour, int64_t capacity,
+                         int32_t* n_colours);
+/* Page-locked host buffers for fast host<->device copies. */
+int vg_host_alloc(void** ptr, uint64_t bytes);
+int vg_host_free(void* ptr);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

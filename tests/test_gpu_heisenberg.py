@@ -1,0 +1,120 @@
+"""Heisenberg colour-class sweeps on the GPU against the FP64 CPU oracle.
+
+Tolerances: the FP64 kernels follow the oracle to 1e-12 per spin component
+(acceptance decisions may differ only where u ~ exp(-dE/T) to ~1e-15, allowed
+for at most 0.1% of sites); the FP32 kernels to 2e-6 per component for sites
+that took the same decision, with at most 0.1% of decisions differing.
+Lattice sums in FP32 agree with FP64 sums of the same state to 1e-6 relative
+(of the sum of |terms|).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+LATTICES = [
+    ("sc", (8, 8, 8), (1, 1, 1)),        # structured checkerboard
+    ("sc", (8, 6, 5), (1, 1, 0)),        # structured, open z
+    ("sc", (7, 4, 4), (1, 1, 1)),        # generic (odd x)
+    ("bcc", (4, 4, 4), (1, 1, 1)),
+    ("fcc", (3, 3, 3), (1, 1, 1)),
+]
+
+
+def _params(O, J, K, axis, hz, b, Kc, T):
+    P = O.HeisParams(J=J, K=K, hz=hz, Kc=Kc, T=T)
+    P.axis[:] = axis
+    P.b[:] = b
+    return P
+
+
+def _run(V, O, cell, ext, pbc, precision, proposal, n=2, seed=21):
+    J, K, axis, mag, b, T = 1.0, 0.1, (0.0, 0.0, 1.0), 0.05, (0.0, 0.6, 0.8), 0.9
+    H = V.hamiltonian(V.Exchange(J), V.UniaxialAnisotropy(axis, K), V.Zeeman())
+    lat = getattr(V.Lattice, cell)(*ext, pbc=tuple(bool(p) for p in pbc))
+    with V.Engine(lat, H, spin=V.SPIN_HEISENBERG, seed=seed, precision=precision, proposal=proposal) as eng:
+        eng.init_random()
+        s0 = eng.get_state()
+        eng.set_thermostat(T, b, mag)
+        sums = eng.sweeps_sums(n)
+        s1 = eng.get_state()
+        path = eng.info().path
+    g = O.Graph(O.lattice(cell, *ext, pbc))
+    ref0 = g.heis_init(seed)
+    P = _params(O, J, K, axis, mag, b, 0.0, T)
+    ref1, obs = g.heis_sweeps(s0, P, seed, 0, n, proposal=proposal)
+    return s0, ref0, s1, ref1, sums, obs, path
+
+
+@pytest.mark.parametrize("cell,ext,pbc", LATTICES)
+@pytest.mark.parametrize("proposal", [1, 0])
+def test_fp64_follows_oracle(V, O, cell, ext, pbc, proposal):
+    s0, ref0, s1, ref1, sums, obs, _ = _run(V, O, cell, ext, pbc, V.FP64, proposal)
+    assert np.abs(s0 - ref0).max() < 1e-12
+    same = np.all(np.abs(s1 - ref1) < 1e-12, axis=1)
+    assert same.mean() >= 0.999
+    if same.all():
+        np.testing.assert_allclose(sums[-1, :7], obs[-1, :7], rtol=0, atol=1e-9)
+
+
+@pytest.mark.parametrize("cell,ext,pbc", LATTICES)
+def test_fp32_follows_oracle(V, O, cell, ext, pbc):
+    s0, ref0, s1, ref1, sums, obs, _ = _run(V, O, cell, ext, pbc, V.FP32, 1, n=1)
+    assert np.abs(s0 - ref0).max() < 2e-6
+    # re-run the oracle from the FP32 start state so only the sweep itself is compared
+    d = np.abs(s1 - ref1).max(axis=1)
+    assert (d < 2e-6).mean() >= 0.999
+    norms = np.linalg.norm(s1, axis=1)
+    assert np.abs(norms - 1).max() < 1e-6
+
+
+def test_fp32_sums_match_fp64_on_same_state(V):
+    H = V.hamiltonian(V.Exchange(1.0), V.UniaxialAnisotropy((0, 0, 1), 0.1), V.Zeeman())
+    lat = V.Lattice.sc(16, 16, 16)
+    rng = np.random.default_rng(3)
+    s = rng.normal(size=(lat.n_sites, 3))
+    s /= np.linalg.norm(s, axis=1, keepdims=True)
+    out = {}
+    for prec in (V.FP32, V.FP64):
+        with V.Engine(lat, H, spin=V.SPIN_HEISENBERG, seed=1, precision=prec) as eng:
+            eng.set_state(s)
+            eng.set_thermostat(1.0, (0, 0, 1), 0.05)
+            out[prec] = eng.current_sums()
+    scale = np.array([3 * lat.n_sites, lat.n_sites, lat.n_sites, lat.n_sites] + [lat.n_sites] * 3)
+    assert np.all(np.abs(out[V.FP32][:7] - out[V.FP64][:7]) <= 1e-6 * scale)
+
+
+def test_norms_do_not_drift(V):
+    H = V.hamiltonian(V.Exchange(1.0))
+    with V.Engine(V.Lattice.sc(32, 16, 16), H, spin=V.SPIN_HEISENBERG, seed=4) as eng:
+        eng.init_random()
+        eng.set_thermostat(0.7)
+        eng.sweeps(200, measure=False)
+        s = eng.get_state()
+    assert np.abs(np.linalg.norm(s, axis=1) - 1.0).max() < 1e-6
+
+
+def test_reference_known_answers_on_gpu(V):
+    """The reference's energy unit tests (src/energy.rs:530-605) through the GPU totals."""
+    import json
+    import os
+
+    gold = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_known_answers.json")))
+    lat = V.Lattice.sc(10, 1, 1, pbc=(True, False, False))
+    for case in gold["energy"]:
+        terms = []
+        for t in case["terms"]:
+            if t[0] == "gauge":
+                terms.append(V.Gauge(t[1]))
+            elif t[0] == "anisotropy":
+                terms.append(V.UniaxialAnisotropy(t[1], t[2]))
+            elif t[0] == "zeeman":
+                terms.append(V.Zeeman())
+        H = V.hamiltonian(*terms)
+        s = np.zeros((10, 3))
+        s[:, 2] = 1.0 if case["state"] == "up" else -1.0
+        with V.Engine(lat, H, spin=V.SPIN_HEISENBERG, seed=0, precision=V.FP64) as eng:
+            eng.set_state(s)
+            f = case["field"]
+            eng.set_thermostat(1.0, f[:3], f[3])
+            assert eng.total_energy() == pytest.approx(case["exact"], abs=1e-12), case["test"]

@@ -1,0 +1,149 @@
+"""Ising colour-class sweeps on the GPU, bit-exact against the CPU oracle (same Philox draws)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+CASES = [
+    # cell, extents, pbc, expected path
+    ("sc", (32, 4, 4), (1, 1, 1), "structured"),
+    ("sc", (32, 32, 1), (1, 1, 0), "structured"),   # 2D square lattice, open z
+    ("sc", (64, 6, 5), (1, 1, 0), "structured"),
+    ("sc", (32, 5, 4), (0, 0, 1), "structured"),    # open x and y boundaries
+    ("sc", (16, 4, 4), (1, 1, 1), "generic"),       # x/2 not a multiple of 16
+    ("sc", (33, 4, 4), (1, 1, 1), "generic"),       # odd periodic cycle: greedy colouring
+    ("bcc", (4, 4, 4), (1, 1, 1), "generic"),
+    ("bcc", (3, 5, 2), (1, 0, 1), "generic"),
+    ("fcc", (4, 4, 4), (1, 1, 1), "generic"),
+    ("fcc", (3, 3, 3), (1, 1, 0), "generic"),
+]
+
+
+def _engine(V, cell, ext, pbc, ham, seed, **kw):
+    lat = getattr(V.Lattice, cell)(*ext, pbc=tuple(bool(p) for p in pbc))
+    return V.Engine(lat, ham, spin=V.SPIN_ISING, seed=seed, **kw)
+
+
+@pytest.mark.parametrize("cell,ext,pbc,path", CASES)
+def test_flip_sweeps_bit_exact(V, O, cell, ext, pbc, path):
+    seed, J, T, n = 1234, 1.0, 3.2, 6
+    with _engine(V, cell, ext, pbc, V.hamiltonian(V.Exchange(J)), seed) as eng:
+        want = V.PATH_STRUCTURED if path == "structured" else V.PATH_GENERIC
+        assert eng.info().path == want
+        eng.init_random()
+        g = O.Graph(O.lattice(cell, *ext, pbc))
+        s0 = g.ising_init(seed)
+        assert np.array_equal(eng.get_state(), s0)
+        eng.set_thermostat(T)
+        E, M = eng.sweeps(n)
+        ref, obs = g.ising_sweeps(s0, J, 0.0, T, seed, 0, n)
+        assert np.array_equal(eng.get_state(), ref)
+        np.testing.assert_array_equal(E, -J * obs[:, 0].astype(float))   # Exchange::total_energy = bond energy
+        np.testing.assert_array_equal(M, np.abs(obs[:, 1]).astype(float))
+
+
+@pytest.mark.parametrize("cell,ext,pbc,path", CASES[:2] + CASES[4:7])
+def test_random_proposal_and_field_bit_exact(V, O, cell, ext, pbc, path):
+    """MetropolisIntegrator (random +-1 proposal) with Exchange + Zeeman, field Down."""
+    seed, J, T, mag, n = 99, 0.7, 2.1, 0.35, 5
+    H = V.hamiltonian(V.Exchange(J), V.Zeeman())
+    with _engine(V, cell, ext, pbc, H, seed, proposal=V.PROPOSE_RANDOM) as eng:
+        eng.init_random()
+        g = O.Graph(O.lattice(cell, *ext, pbc))
+        s0 = g.ising_init(seed)
+        eng.set_thermostat(T, (0.0, 0.0, -1.0), mag)
+        E, M = eng.sweeps(n)
+        hz = 1.0 * mag * -1.0
+        ref, obs = g.ising_sweeps(s0, J, hz, T, seed, 0, n, proposal=O.PROPOSE_RANDOM)
+        assert np.array_equal(eng.get_state(), ref)
+        bond, m = obs[:, 0].astype(float), obs[:, 1].astype(float)
+        # Compound total: sum_i energy(i) = -2 J bond + |B| (s . b) summed
+        np.testing.assert_allclose(E, -2 * J * bond + mag * (-m), rtol=0, atol=1e-9)
+        np.testing.assert_array_equal(M, np.abs(m))
+
+
+def test_generic_and_structured_paths_agree(V):
+    H = V.hamiltonian(V.Exchange(1.0))
+    out = []
+    for path in (V.PATH_STRUCTURED, V.PATH_GENERIC):
+        with _engine(V, "sc", (64, 8, 6), (1, 1, 1), H, 5, path=path) as eng:
+            eng.init_random()
+            eng.set_thermostat(4.4)
+            E, M = eng.sweeps(20)
+            out.append((eng.get_state(), E, M))
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1]) and np.array_equal(out[0][2], out[1][2])
+
+
+def test_resume_from_sweep_index(V):
+    """(seed, sweep index) is the whole RNG state: splitting a run changes nothing."""
+    H = V.hamiltonian(V.Exchange(1.0))
+    with _engine(V, "sc", (32, 8, 8), (1, 1, 1), H, 8) as a, _engine(V, "sc", (32, 8, 8), (1, 1, 1), H, 8) as b:
+        for e in (a, b):
+            e.init_random()
+            e.set_thermostat(4.5)
+        a.sweeps(10, measure=False)
+        b.sweeps(4, measure=False)
+        s = b.get_state()
+        b.set_state(s)
+        b.sweeps(6, measure=False)
+        assert a.sweep_index == b.sweep_index == 10
+        assert np.array_equal(a.get_state(), b.get_state())
+
+
+def test_set_get_roundtrip_and_observables(V, O):
+    lat = ("sc", (32, 6, 4), (1, 1, 1))
+    rng = np.random.default_rng(1)
+    s = rng.choice(np.array([-1, 1], dtype=np.int8), size=32 * 6 * 4)
+    H = V.hamiltonian(V.Exchange(1.0), V.Zeeman(), V.Gauge(0.25))
+    with _engine(V, *lat, H, 3) as eng:
+        eng.set_state(s)
+        assert np.array_equal(eng.get_state(), s)
+        eng.set_thermostat(2.0, (0, 0, 1), 0.5)
+        g = O.Graph(O.lattice(*lat))
+        Href = O.Hamiltonian(has_exchange=1, J=1.0, has_zeeman=1, zeeman_sign=1.0, has_gauge=1, gauge=0.25,
+                             compound=1)
+        e_ref = g.ref_total_energy(0, s, Href, b=(0, 0, 1), bmag=0.5)
+        assert eng.total_energy() == pytest.approx(e_ref, abs=1e-9)
+        m, mag = eng.magnetization()
+        assert mag == abs(int(s.sum())) and m[2] == int(s.sum())
+
+
+def test_low_and_high_temperature_limits(V):
+    H = V.hamiltonian(V.Exchange(1.0))
+    with _engine(V, "sc", (32, 16, 16), (1, 1, 1), H, 2) as eng:
+        eng.set_state(np.ones(32 * 16 * 16, dtype=np.int8))
+        eng.set_thermostat(0.0)  # clamped to f64::EPSILON: nothing can flip upward in energy
+        E, M = eng.sweeps(3)
+        assert np.all(E == -3 * 32 * 16 * 16) and np.all(M == 32 * 16 * 16)
+        eng.set_thermostat(1e9)
+        E, M = eng.sweeps(50)
+        n = 32 * 16 * 16
+        assert abs(E[10:].mean()) < 0.02 * 3 * n and M[10:].mean() < 0.05 * n
+
+
+def test_invalid_spins_rejected(V):
+    H = V.hamiltonian(V.Exchange(1.0))
+    with _engine(V, "sc", (32, 4, 4), (1, 1, 1), H, 2) as eng:
+        bad = np.ones(512, dtype=np.int8)
+        bad[7] = 0
+        with pytest.raises(V.VegasGpuError) as e:
+            eng.set_state(bad)
+        assert e.value.status == 1
+        with pytest.raises(V.VegasGpuError):
+            eng.set_state(np.ones(100, dtype=np.int8))
+        with pytest.raises(V.VegasGpuError):
+            eng.set_thermostat(float("nan"))
+        eng.set_thermostat(2.0)
+        eng.sweeps(1)  # the context stays usable after rejected calls
+
+
+def test_acceptance_counts(V):
+    H = V.hamiltonian(V.Exchange(1.0))
+    with _engine(V, "sc", (32, 8, 8), (1, 1, 1), H, 4) as eng:
+        eng.init_random()
+        eng.set_thermostat(1e9)
+        sums = eng.sweeps_sums(5)
+        n = 32 * 8 * 8
+        # at T -> infinity every flip with dE > 0 is accepted with probability ~1
+        assert np.all(sums[:, 7] > 0.99 * n)

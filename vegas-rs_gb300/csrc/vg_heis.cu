@@ -1,0 +1,274 @@
+// vg_heis.cu -- Heisenberg colour-class Metropolis passes (FP32 and FP64).
+//
+// Replaces MetropolisIntegrator::step (proposal Spin::rand, a uniform point
+// on S^2, src/integrator.rs:66-92, src/util.rs:21-34) and
+// MetropolisFlipIntegrator::step (proposal -s, :113-137) for HeisenbergSpin,
+// with the energy terms of src/energy.rs (Exchange, UniaxialAnisotropy,
+// Zeeman with the reference's per-site sign, Gauge) plus a cubic term.
+// Each site consumes one Philox block keyed (class entry j, sweep, tag,
+// colour): words 0/1 give the proposal (Archimedes map: z uniform in (-1,1),
+// azimuth uniform), word 2 the acceptance uniform.  dE is formed as a
+// difference of per-term changes (no cancellation of two O(z) energies),
+// accepted if dE <= 0 or u < exp(-dE/T).
+//
+// Per-sweep sums: each site adds its terms after its own update; the bond
+// sum takes, for each site, only neighbours of lower colour, which are final
+// for the sweep when that site's pass runs, so every bond is counted once.
+#include "vg_internal.cuh"
+
+namespace vg {
+
+__device__ __forceinline__ void sincospi_(float t, float* s, float* c) { sincospif(t, s, c); }
+__device__ __forceinline__ void sincospi_(double t, double* s, double* c) { sincospi(t, s, c); }
+__device__ __forceinline__ float sqrt_(float x) { return sqrtf(x); }
+__device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
+__device__ __forceinline__ float exp_(float x) { return expf(x); }
+__device__ __forceinline__ double exp_(double x) { return exp(x); }
+
+template <typename R>
+struct V3 {
+  R x, y, z;
+};
+
+template <typename R>
+__device__ __forceinline__ R quart(const V3<R>& s) {
+  const R a = s.x * s.x, b = s.y * s.y, c = s.z * s.z;
+  return a * a + b * b + c * c;
+}
+
+// Proposal and acceptance draw of one site; returns the new spin and whether
+// it was accepted.
+template <typename R, int PROP>
+__device__ __forceinline__ bool heis_update(const V3<R>& s, const V3<R>& h, const HeisParams<R>& P, const uint4& w,
+                                            V3<R>& out) {
+  V3<R> p;
+  if (PROP == VG_PROPOSE_RANDOM) {
+    // z = (2k + 1 - 2^24) / 2^24 is exact in FP32; azimuth pi * t, t in [0, 2)
+    const R z = (R)((int)((w.x >> 8) << 1) + 1 - (1 << 24)) * (R)(1.0 / 16777216.0);
+    const R t = (R)(w.y >> 8) * (R)(1.0 / 8388608.0);
+    R sn, cs;
+    sincospi_(t, &sn, &cs);
+    const R r = sqrt_(((R)1 - z) * ((R)1 + z));
+    p.x = r * cs;
+    p.y = r * sn;
+    p.z = z;
+  } else {
+    p.x = -s.x;
+    p.y = -s.y;
+    p.z = -s.z;
+  }
+  const R dx = p.x - s.x, dy = p.y - s.y, dz = p.z - s.z;
+  const R pe = p.x * P.ax + p.y * P.ay + p.z * P.az;
+  const R se = s.x * P.ax + s.y * P.ay + s.z * P.az;
+  R de = -P.J * (dx * h.x + dy * h.y + dz * h.z);
+  de += P.K * (pe * pe - se * se);
+  de += P.hz * (dx * P.bx + dy * P.by + dz * P.bz);
+  de -= P.Kc * (quart(p) - quart(s));
+  const R u = (R)(w.z >> 8) * (R)(1.0 / 16777216.0);
+  const bool acc = de <= (R)0 || u < exp_(-de * P.beta);
+  out = acc ? p : s;
+  return acc;
+}
+
+template <typename R>
+__device__ __forceinline__ void add_site_sums(R (&acc)[kNumSums], const V3<R>& s, const V3<R>& low,
+                                              const HeisParams<R>& P) {
+  const R se = s.x * P.ax + s.y * P.ay + s.z * P.az;
+  acc[0] += s.x * low.x + s.y * low.y + s.z * low.z;
+  acc[1] += se * se;
+  acc[2] += s.x * P.bx + s.y * P.by + s.z * P.bz;
+  acc[3] += quart(s);
+  acc[4] += s.x;
+  acc[5] += s.y;
+  acc[6] += s.z;
+}
+
+// Thread-level partials in R, block reduction in FP64.
+template <typename R>
+__device__ __forceinline__ void flush_sums(R (&acc)[kNumSums], double* part) {
+  double v[kNumSums];
+#pragma unroll
+  for (int i = 0; i < kNumSums; ++i) v[i] = (double)acc[i];
+  block_sum_store(v, part + (long long)blockIdx.x * kNumSums);
+}
+
+// ------------------------------------------------------------------ sc
+template <typename R, int C, bool ALLPER, bool MEASURE, bool UPDATE, int PROP>
+__global__ void __launch_bounds__(256) heis_sc_kernel(const HeisScArgs<R> a, const HeisParams<R> P, const RngKey key,
+                                                      double* __restrict__ part) {
+  R* __restrict__ ox = a.x[C];
+  R* __restrict__ oy = a.y[C];
+  R* __restrict__ oz = a.z[C];
+  const R* __restrict__ nx = a.x[C ^ 1];
+  const R* __restrict__ ny = a.y[C ^ 1];
+  const R* __restrict__ nz = a.z[C ^ 1];
+  R acc[kNumSums];
+#pragma unroll
+  for (int i = 0; i < kNumSums; ++i) acc[i] = (R)0;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < a.n_c; j += stride) {
+    const long long row = j / a.Hx;
+    const int h = (int)(j - row * a.Hx);
+    const int y = (int)(row % a.Ly), z = (int)(row / a.Ly);
+    const int p = (y + z + C) & 1;
+    const long long rb = row * a.Hx;
+    V3<R> hs = {(R)0, (R)0, (R)0};
+    auto add = [&](long long q) {
+      hs.x += __ldg(nx + q);
+      hs.y += __ldg(ny + q);
+      hs.z += __ldg(nz + q);
+    };
+    add(rb + h);
+    int hx = p ? h + 1 : h - 1;
+    bool hxok = true;
+    if (hx < 0) {
+      hx = a.Hx - 1;
+      hxok = ALLPER || a.pbx;
+    } else if (hx >= a.Hx) {
+      hx = 0;
+      hxok = ALLPER || a.pbx;
+    }
+    if (hxok) add(rb + hx);
+    if (y > 0) add(rb - a.Hx + h);
+    else if (ALLPER || a.pby) add(rb + (long long)(a.Ly - 1) * a.Hx + h);
+    if (y < a.Ly - 1) add(rb + a.Hx + h);
+    else if (ALLPER || a.pby) add(rb - (long long)(a.Ly - 1) * a.Hx + h);
+    const long long plane = (long long)a.Ly * a.Hx;
+    if (z > 0) add(rb - plane + h);
+    else if (ALLPER || a.pbz) add(rb + (long long)(a.Lz - 1) * plane + h);
+    if (z < a.Lz - 1) add(rb + plane + h);
+    else if (ALLPER || a.pbz) add(rb - (long long)(a.Lz - 1) * plane + h);
+
+    const long long q = rb + h;
+    V3<R> s = {ox[q], oy[q], oz[q]};
+    if (UPDATE) {
+      const uint4 w = philox(make_uint4((uint32_t)j, key.sweep, (kTagHeis << 24) | ((uint32_t)C << 8), key.replica),
+                             key.k0, key.k1);
+      V3<R> sn;
+      if (heis_update<R, PROP>(s, hs, P, w, sn)) {
+        ox[q] = sn.x;
+        oy[q] = sn.y;
+        oz[q] = sn.z;
+        s = sn;
+        acc[7] += (R)1;
+      }
+    }
+    if (MEASURE) {
+      const V3<R> low = C == 1 ? hs : V3<R>{(R)0, (R)0, (R)0};
+      add_site_sums(acc, s, low, P);
+    }
+  }
+  if (MEASURE) flush_sums(acc, part);
+}
+
+// ------------------------------------------------------------- generic
+template <typename R, int ZT, bool MEASURE, bool UPDATE, int PROP>
+__global__ void __launch_bounds__(256) heis_gen_kernel(const HeisGenArgs<R> a, const HeisParams<R> P, const RngKey key,
+                                                       const int colour, double* __restrict__ part) {
+  R acc[kNumSums];
+#pragma unroll
+  for (int i = 0; i < kNumSums; ++i) acc[i] = (R)0;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < a.n_c; j += stride) {
+    const int i = __ldg(a.sites + j);
+    const uint32_t lm = __ldg(a.lowmask + j);
+    V3<R> hs = {(R)0, (R)0, (R)0}, low = {(R)0, (R)0, (R)0};
+#pragma unroll
+    for (int k = 0; k < ZT; ++k) {
+      if (k < a.zc) {
+        const int t = __ldg(a.nbr + (long long)k * a.n_c + j);
+        if (t >= 0) {
+          const R vx = a.x[t], vy = a.y[t], vz = a.z[t];
+          hs.x += vx;
+          hs.y += vy;
+          hs.z += vz;
+          if ((lm >> k) & 1u) {
+            low.x += vx;
+            low.y += vy;
+            low.z += vz;
+          }
+        }
+      }
+    }
+    V3<R> s = {a.x[i], a.y[i], a.z[i]};
+    if (UPDATE) {
+      const uint4 w = philox(make_uint4((uint32_t)j, key.sweep, (kTagHeis << 24) | ((uint32_t)colour << 8), key.replica),
+                             key.k0, key.k1);
+      V3<R> sn;
+      if (heis_update<R, PROP>(s, hs, P, w, sn)) {
+        a.x[i] = sn.x;
+        a.y[i] = sn.y;
+        a.z[i] = sn.z;
+        s = sn;
+        acc[7] += (R)1;
+      }
+    }
+    if (MEASURE) add_site_sums(acc, s, low, P);
+  }
+  if (MEASURE) flush_sums(acc, part);
+}
+
+// ------------------------------------------------------------ dispatch
+template <typename R, int C, bool ALLPER>
+static void sc_go(const HeisScArgs<R>& a, const HeisParams<R>& p, RngKey key, int proposal, bool update, double* part,
+                  int grid, int tpb, cudaStream_t s) {
+  const bool m = part != nullptr;
+  if (!update) {
+    heis_sc_kernel<R, C, ALLPER, true, false, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, p, key, part);
+  } else if (proposal == VG_PROPOSE_RANDOM) {
+    if (m) heis_sc_kernel<R, C, ALLPER, true, true, VG_PROPOSE_RANDOM><<<grid, tpb, 0, s>>>(a, p, key, part);
+    else heis_sc_kernel<R, C, ALLPER, false, true, VG_PROPOSE_RANDOM><<<grid, tpb, 0, s>>>(a, p, key, part);
+  } else {
+    if (m) heis_sc_kernel<R, C, ALLPER, true, true, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, p, key, part);
+    else heis_sc_kernel<R, C, ALLPER, false, true, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, p, key, part);
+  }
+}
+
+template <typename R>
+cudaError_t launch_heis_sc(const HeisScArgs<R>& a, const HeisParams<R>& p, RngKey key, int colour, int proposal,
+                           bool update, double* part, int grid, int tpb, cudaStream_t s) {
+  const bool allper = a.pbx && a.pby && a.pbz;
+  if (colour == 0) {
+    if (allper) sc_go<R, 0, true>(a, p, key, proposal, update, part, grid, tpb, s);
+    else sc_go<R, 0, false>(a, p, key, proposal, update, part, grid, tpb, s);
+  } else {
+    if (allper) sc_go<R, 1, true>(a, p, key, proposal, update, part, grid, tpb, s);
+    else sc_go<R, 1, false>(a, p, key, proposal, update, part, grid, tpb, s);
+  }
+  return cudaGetLastError();
+}
+
+template <typename R, int ZT>
+static void gen_go(const HeisGenArgs<R>& a, const HeisParams<R>& p, RngKey key, int colour, int proposal, bool update,
+                   double* part, int grid, int tpb, cudaStream_t s) {
+  const bool m = part != nullptr;
+  if (!update) {
+    heis_gen_kernel<R, ZT, true, false, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, p, key, colour, part);
+  } else if (proposal == VG_PROPOSE_RANDOM) {
+    if (m) heis_gen_kernel<R, ZT, true, true, VG_PROPOSE_RANDOM><<<grid, tpb, 0, s>>>(a, p, key, colour, part);
+    else heis_gen_kernel<R, ZT, false, true, VG_PROPOSE_RANDOM><<<grid, tpb, 0, s>>>(a, p, key, colour, part);
+  } else {
+    if (m) heis_gen_kernel<R, ZT, true, true, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, p, key, colour, part);
+    else heis_gen_kernel<R, ZT, false, true, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, p, key, colour, part);
+  }
+}
+
+template <typename R>
+cudaError_t launch_heis_gen(const HeisGenArgs<R>& a, const HeisParams<R>& p, RngKey key, int colour, int proposal,
+                            bool update, double* part, int grid, int tpb, cudaStream_t s) {
+  if (a.zc <= 6) gen_go<R, 6>(a, p, key, colour, proposal, update, part, grid, tpb, s);
+  else if (a.zc <= 8) gen_go<R, 8>(a, p, key, colour, proposal, update, part, grid, tpb, s);
+  else gen_go<R, 12>(a, p, key, colour, proposal, update, part, grid, tpb, s);
+  return cudaGetLastError();
+}
+
+template cudaError_t launch_heis_sc<float>(const HeisScArgs<float>&, const HeisParams<float>&, RngKey, int, int, bool,
+                                           double*, int, int, cudaStream_t);
+template cudaError_t launch_heis_sc<double>(const HeisScArgs<double>&, const HeisParams<double>&, RngKey, int, int,
+                                            bool, double*, int, int, cudaStream_t);
+template cudaError_t launch_heis_gen<float>(const HeisGenArgs<float>&, const HeisParams<float>&, RngKey, int, int,
+                                            bool, double*, int, int, cudaStream_t);
+template cudaError_t launch_heis_gen<double>(const HeisGenArgs<double>&, const HeisParams<double>&, RngKey, int, int,
+                                             bool, double*, int, int, cudaStream_t);
+
+}  // namespace vg

@@ -1,0 +1,155 @@
+// vg_internal.cuh -- shared device helpers and kernel argument blocks of the
+// vegas GB300 engine.  Nothing here is part of the public C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "vegas_gpu.h"
+
+namespace vg {
+
+constexpr int kMaxZ = 12;          // fcc coordination
+constexpr int kMaxColours = 16;
+constexpr int kIsingGroup = 16;    // class entries sharing one Philox block
+constexpr int kNumSums = 8;        // members of vg_sums
+
+// Draw-stream tags (bits 24..31 of Philox counter word 2).
+enum : uint32_t {
+  kTagIsingAccept = 1,
+  kTagIsingPropose = 2,
+  kTagHeis = 3,
+  kTagInitIsing = 4,
+  kTagInitHeis = 5
+};
+
+// ------------------------------------------------------------ Philox4x32-10
+// Salmon et al., "Parallel random numbers: as easy as 1, 2, 3" (SC'11).
+__host__ __device__ __forceinline__ uint4 philox(uint4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    if (r) {
+      k0 += 0x9E3779B9u;
+      k1 += 0xBB67AE85u;
+    }
+#ifdef __CUDA_ARCH__
+    const uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+    const uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+#else
+    const uint64_t p0 = (uint64_t)0xD2511F53u * c.x, p1 = (uint64_t)0xCD9E8D57u * c.z;
+    const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+#endif
+    c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
+  }
+  return c;
+}
+
+__device__ __forceinline__ uint32_t blk_byte(const uint4& b, int k) {
+  const uint32_t w = (k >> 2) == 0 ? b.x : (k >> 2) == 1 ? b.y : (k >> 2) == 2 ? b.z : b.w;
+  return (w >> (8 * (k & 3))) & 0xFFu;
+}
+
+// Ising acceptance table: index s*(2z+1) + nsum + z, value = threshold on a
+// 32-bit uniform (accept iff U < thr); thr >= 2^32 means always.
+struct IsingTable {
+  unsigned long long thr[2 * (2 * kMaxZ + 1)];
+};
+
+struct RngKey {
+  uint32_t k0, k1, replica, sweep;
+};
+
+// ------------------------------------------------------------ kernel args
+struct IsingScArgs {          // sc checkerboard, class-separated uint8 0/1
+  uint8_t* cls[2];
+  long long groups;           // 16-site groups per class
+  int Hx, Ly, Lz, G;          // Hx = Lx/2, G = Hx/16
+  int pbx, pby, pbz;
+};
+
+struct IsingGenArgs {         // any lattice: natural order uint8 0/1 + ELL
+  uint8_t* spin;
+  const int32_t* sites;       // class entry -> site
+  const int32_t* nbr;         // [z][n_c] neighbour sites (-1 absent)
+  const uint32_t* lowmask;    // bit k: neighbour k has a lower colour
+  long long n_c;
+  int z;
+};
+
+template <typename R>
+struct HeisScArgs {           // sc checkerboard, class-separated SoA
+  R* x[2];
+  R* y[2];
+  R* z[2];
+  long long n_c;              // sites per class
+  int Hx, Ly, Lz;
+  int pbx, pby, pbz;
+};
+
+template <typename R>
+struct HeisGenArgs {          // any lattice: natural order SoA + ELL
+  R* x;
+  R* y;
+  R* z;
+  const int32_t* sites;
+  const int32_t* nbr;
+  const uint32_t* lowmask;
+  long long n_c;
+  int zc;
+};
+
+template <typename R>
+struct HeisParams {
+  R J, K, ax, ay, az, hz, bx, by, bz, Kc, beta;
+  R T;
+};
+
+// ------------------------------------------------------------ launchers
+// Each launcher enqueues one colour pass; part (may be null) receives one
+// row of kNumSums partials per block (int64 for Ising, double for
+// Heisenberg).  update = false only measures.
+cudaError_t launch_ising_sc(const IsingScArgs& a, const IsingTable& tab, RngKey key, int colour,
+                            int proposal, bool all_periodic, bool update, long long* part, int grid,
+                            int tpb, cudaStream_t s);
+cudaError_t launch_ising_gen(const IsingGenArgs& a, const IsingTable& tab, RngKey key, int colour,
+                             int proposal, bool update, long long* part, int grid, int tpb,
+                             cudaStream_t s);
+template <typename R>
+cudaError_t launch_heis_sc(const HeisScArgs<R>& a, const HeisParams<R>& p, RngKey key, int colour,
+                           int proposal, bool update, double* part, int grid, int tpb,
+                           cudaStream_t s);
+template <typename R>
+cudaError_t launch_heis_gen(const HeisGenArgs<R>& a, const HeisParams<R>& p, RngKey key, int colour,
+                            int proposal, bool update, double* part, int grid, int tpb,
+                            cudaStream_t s);
+
+// ------------------------------------------------------------ reductions
+// Block-wide sum of kNumSums values into row `out` (thread 0 writes).
+template <typename T>
+__device__ __forceinline__ void block_sum_store(T (&v)[kNumSums], T* out) {
+  __shared__ T red[32][kNumSums];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int i = 0; i < kNumSums; ++i) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[i] += __shfl_down_sync(0xffffffffu, v[i], o);
+  }
+  if (lane == 0) {
+#pragma unroll
+    for (int i = 0; i < kNumSums; ++i) red[warp][i] = v[i];
+  }
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int i = 0; i < kNumSums; ++i) {
+      T t = lane < nw ? red[lane][i] : T(0);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+      if (lane == 0) out[i] = t;
+    }
+  }
+}
+
+}  // namespace vg

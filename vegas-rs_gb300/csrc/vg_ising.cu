@@ -1,0 +1,319 @@
+// vg_ising.cu -- Ising colour-class Metropolis passes.
+//
+// Replaces MetropolisFlipIntegrator::step / MetropolisIntegrator::step for
+// IsingSpin (src/integrator.rs:66-137) with the reference's accept rule:
+// dE < 0 accepts; otherwise accept iff u < exp(-dE/T).  dE is an integer
+// function of (s, sum of neighbour spins), so the rule is a table of 32-bit
+// thresholds built on the host in FP64 (accept iff U < thr for the site's
+// 32-bit uniform U).  U is drawn byte-serially: byte (j & 15) of Philox
+// block d = 0..3 of the 16-site group j >> 4 is digit d (most significant
+// first), and a later block is generated only while some site of the group
+// still ties with its threshold -- usually one block per 16 sites.
+//
+// Two kernel families, identical results:
+//  * ising_sc_kernel: sc lattice in a checkerboard, class-separated layout
+//    (class c holds sites with (x+y+z)&1 == c, row-major [z][y][x/2]); one
+//    thread owns 16 consecutive sites of a row as one uint4 of 0/1 bytes and
+//    adds its six neighbour vectors with plain 32-bit adds (bytes <= 6).
+//  * ising_gen_kernel: any lattice via an ELL neighbour table per colour
+//    class of a greedy colouring (natural-order spins).
+#include "vg_internal.cuh"
+
+namespace vg {
+
+// Decide 16 candidate sites given their 64-bit thresholds; returns the
+// accepted mask.  Site k of group g uses byte k of the group's blocks.
+__device__ __forceinline__ uint32_t decide16(const unsigned long long (&t)[16], uint32_t cand,
+                                             const RngKey& key, uint32_t g, int colour) {
+  uint32_t thr32[16];
+  uint32_t acc = 0, und = 0;
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    thr32[k] = (uint32_t)t[k];
+    const bool c = (cand >> k) & 1u;
+    if (c && t[k] >= (1ull << 32)) acc |= 1u << k;
+    if (c && t[k] > 0ull && t[k] < (1ull << 32)) und |= 1u << k;
+  }
+#pragma unroll 1
+  for (int d = 0; d < 4 && und; ++d) {
+    const uint4 b = philox(make_uint4(g, key.sweep, (kTagIsingAccept << 24) | ((uint32_t)colour << 8) | (uint32_t)d,
+                                      key.replica),
+                           key.k0, key.k1);
+    const uint32_t w[4] = {b.x, b.y, b.z, b.w};
+    const int sh = 24 - 8 * d;
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      const uint32_t bit = 1u << k;
+      const uint32_t ub = (w[k >> 2] >> (8 * (k & 3))) & 0xFFu;
+      const uint32_t tb = (thr32[k] >> sh) & 0xFFu;
+      if (und & bit) {
+        if (ub < tb) {
+          acc |= bit;
+          und &= ~bit;
+        } else if (ub > tb) {
+          und &= ~bit;
+        }
+      }
+    }
+  }
+  return acc;
+}
+
+// 4 bits -> 4 bytes of 0/1 and back.
+__device__ __forceinline__ uint32_t spread4(uint32_t m) { return ((m & 0xFu) * 0x00204081u) & 0x01010101u; }
+__device__ __forceinline__ uint32_t gather4(uint32_t x) { return (((x & 0x01010101u) * 0x01020408u) >> 24) & 0xFu; }
+
+// Random +-1 proposal of IsingSpin::rand (src/state.rs:76-84): byte < 128
+// (u < 0.5) proposes Up.  Returns the mask of sites whose proposal differs.
+__device__ __forceinline__ uint32_t propose_random16(const uint32_t (&s)[4], const RngKey& key, uint32_t g,
+                                                     int colour) {
+  const uint4 b = philox(make_uint4(g, key.sweep, (kTagIsingPropose << 24) | ((uint32_t)colour << 8), key.replica),
+                         key.k0, key.k1);
+  const uint32_t w[4] = {b.x, b.y, b.z, b.w};
+  uint32_t diff = 0;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const uint32_t up = (~w[i] >> 7) & 0x01010101u;
+    diff |= gather4(up ^ s[i]) << (4 * i);
+  }
+  return diff;
+}
+
+// ------------------------------------------------------------------ sc
+template <int C, bool ALLPER, bool MEASURE, bool UPDATE, int PROP>
+__global__ void __launch_bounds__(256) ising_sc_kernel(const IsingScArgs a, const IsingTable tab, const RngKey key,
+                                                       long long* __restrict__ part) {
+  constexpr int Z = 6, W = 2 * Z + 1;
+  __shared__ unsigned long long s_thr[2 * W];
+  for (int i = threadIdx.x; i < 2 * W; i += blockDim.x) s_thr[i] = tab.thr[i];
+  __syncthreads();
+
+  uint8_t* __restrict__ own = a.cls[C];
+  const uint8_t* __restrict__ oth = a.cls[C ^ 1];
+  long long bond = 0, ups = 0, nacc = 0;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x; gid < a.groups; gid += stride) {
+    const long long row = gid / a.G;
+    const int h0 = (int)(gid - row * a.G) << 4;
+    const int y = (int)(row % a.Ly), z = (int)(row / a.Ly);
+    const int p = (y + z + C) & 1;  // x parity of this row's class-C sites
+    const long long rb = row * a.Hx;
+
+    const uint4 Sv = *reinterpret_cast<const uint4*>(own + rb + h0);
+    const uint4 X0 = __ldg(reinterpret_cast<const uint4*>(oth + rb + h0));
+    // x-neighbour not shared with X0: h0-1 (p = 0) or h0+16 (p = 1)
+    uint32_t e = 0;
+    bool xmiss = false;
+    if (p == 0) {
+      if (h0 > 0) e = __ldg(oth + rb + h0 - 1);
+      else if (ALLPER || a.pbx) e = __ldg(oth + rb + a.Hx - 1);
+      else xmiss = true;
+    } else {
+      if (h0 + 16 < a.Hx) e = __ldg(oth + rb + h0 + 16);
+      else if (ALLPER || a.pbx) e = __ldg(oth + rb);
+      else xmiss = true;
+    }
+    uint32_t X1[4];
+    if (p == 0) {
+      X1[0] = __byte_perm(e << 24, X0.x, 0x6543);
+      X1[1] = __byte_perm(X0.x, X0.y, 0x6543);
+      X1[2] = __byte_perm(X0.y, X0.z, 0x6543);
+      X1[3] = __byte_perm(X0.z, X0.w, 0x6543);
+    } else {
+      X1[0] = __byte_perm(X0.x, X0.y, 0x4321);
+      X1[1] = __byte_perm(X0.y, X0.z, 0x4321);
+      X1[2] = __byte_perm(X0.z, X0.w, 0x4321);
+      X1[3] = __byte_perm(X0.w, e, 0x4321);
+    }
+    long long rym, ryp, rzm, rzp;
+    rym = y > 0 ? row - 1 : ((ALLPER || a.pby) ? row + a.Ly - 1 : -1);
+    ryp = y < a.Ly - 1 ? row + 1 : ((ALLPER || a.pby) ? row - (a.Ly - 1) : -1);
+    rzm = z > 0 ? row - a.Ly : ((ALLPER || a.pbz) ? row + (long long)(a.Lz - 1) * a.Ly : -1);
+    rzp = z < a.Lz - 1 ? row + a.Ly : ((ALLPER || a.pbz) ? row - (long long)(a.Lz - 1) * a.Ly : -1);
+    const uint4 zero4 = make_uint4(0, 0, 0, 0);
+    const uint4 Ym = rym >= 0 ? __ldg(reinterpret_cast<const uint4*>(oth + rym * a.Hx + h0)) : zero4;
+    const uint4 Yp = ryp >= 0 ? __ldg(reinterpret_cast<const uint4*>(oth + ryp * a.Hx + h0)) : zero4;
+    const uint4 Zm = rzm >= 0 ? __ldg(reinterpret_cast<const uint4*>(oth + rzm * a.Hx + h0)) : zero4;
+    const uint4 Zp = rzp >= 0 ? __ldg(reinterpret_cast<const uint4*>(oth + rzp * a.Hx + h0)) : zero4;
+
+    const uint32_t S[4] = {Sv.x, Sv.y, Sv.z, Sv.w};
+    const uint32_t A[4] = {X0.x + X1[0] + Ym.x + Yp.x + Zm.x + Zp.x, X0.y + X1[1] + Ym.y + Yp.y + Zm.y + Zp.y,
+                           X0.z + X1[2] + Ym.z + Yp.z + Zm.z + Zp.z, X0.w + X1[3] + Ym.w + Yp.w + Zm.w + Zp.w};
+    // M = 2A + (Z - Zc) per byte, where Zc counts existing neighbours; the
+    // neighbour sum of site k is M_k - Z.
+    uint32_t M[4];
+    if (ALLPER) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) M[i] = 2u * A[i];
+    } else {
+      const uint32_t zmiss = (uint32_t)((rym < 0) + (ryp < 0) + (rzm < 0) + (rzp < 0));
+#pragma unroll
+      for (int i = 0; i < 4; ++i) M[i] = 2u * A[i] + zmiss * 0x01010101u;
+      if (xmiss) {
+        if (p == 0) M[0] += 1u;
+        else M[3] += 1u << 24;
+      }
+    }
+
+    uint32_t flip = 0;
+    if (UPDATE) {
+      const uint32_t cand = PROP == VG_PROPOSE_FLIP ? 0xFFFFu : propose_random16(S, key, (uint32_t)gid, C);
+      unsigned long long t[16];
+#pragma unroll
+      for (int k = 0; k < 16; ++k) {
+        const uint32_t idx = ((S[k >> 2] * (uint32_t)W + M[k >> 2]) >> (8 * (k & 3))) & 0xFFu;
+        t[k] = s_thr[idx];
+      }
+      flip = decide16(t, cand, key, (uint32_t)gid, C) & cand;
+    }
+    uint32_t Sn[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) Sn[i] = S[i] ^ spread4(flip >> (4 * i));
+    if (flip) *reinterpret_cast<uint4*>(own + rb + h0) = make_uint4(Sn[0], Sn[1], Sn[2], Sn[3]);
+
+    if (MEASURE) {
+      int u = 0;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) u += __popc(Sn[i]);
+      ups += u;
+      nacc += __popc(flip);
+      if (C == 1) {  // both neighbours' classes precede: every bond of class 1 is counted here
+        unsigned sm = 0, m = 0;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          sm = __dp4a(Sn[i], M[i], sm);
+          m = __dp4a(M[i], 0x01010101u, m);
+        }
+        bond += 2 * (int)sm - (int)m - Z * (2 * u - 16);
+      }
+    }
+  }
+  if (MEASURE) {
+    long long v[kNumSums] = {bond, 0, 0, 0, 0, 0, ups, nacc};
+    block_sum_store(v, part + (long long)blockIdx.x * kNumSums);
+  }
+}
+
+// ------------------------------------------------------------- generic
+template <int ZT, bool MEASURE, bool UPDATE, int PROP>
+__global__ void __launch_bounds__(256) ising_gen_kernel(const IsingGenArgs a, const IsingTable tab, const RngKey key,
+                                                        const int colour, long long* __restrict__ part) {
+  constexpr int W = 2 * ZT + 1;
+  __shared__ unsigned long long s_thr[2 * W];
+  const int z = a.z;
+  const int Wz = 2 * z + 1;
+  for (int i = threadIdx.x; i < 2 * Wz; i += blockDim.x) s_thr[i] = tab.thr[i];
+  __syncthreads();
+
+  long long bond = 0, ups = 0, nacc = 0;
+  const long long ngroups = (a.n_c + 15) >> 4;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < ngroups; g += stride) {
+    const long long j0 = g << 4;
+    int site[16], nsum[16], nlow[16];
+    uint32_t S[4] = {0, 0, 0, 0}, valid = 0;
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      const long long j = j0 + k;
+      site[k] = -1;
+      nsum[k] = 0;
+      nlow[k] = 0;
+      if (j < a.n_c) {
+        valid |= 1u << k;
+        const int i = __ldg(a.sites + j);
+        site[k] = i;
+        S[k >> 2] |= (uint32_t)a.spin[i] << (8 * (k & 3));
+        const uint32_t lm = __ldg(a.lowmask + j);
+#pragma unroll
+        for (int q = 0; q < ZT; ++q) {
+          if (q < z) {
+            const int t = __ldg(a.nbr + (long long)q * a.n_c + j);
+            if (t >= 0) {
+              const int v = 2 * (int)a.spin[t] - 1;
+              nsum[k] += v;
+              if ((lm >> q) & 1u) nlow[k] += v;
+            }
+          }
+        }
+      }
+    }
+    uint32_t flip = 0;
+    if (UPDATE) {
+      const uint32_t cand = (PROP == VG_PROPOSE_FLIP ? 0xFFFFu : propose_random16(S, key, (uint32_t)g, colour)) & valid;
+      unsigned long long t[16];
+#pragma unroll
+      for (int k = 0; k < 16; ++k) {
+        const int s = (S[k >> 2] >> (8 * (k & 3))) & 1;
+        t[k] = s_thr[s * Wz + nsum[k] + z];
+      }
+      flip = decide16(t, cand, key, (uint32_t)g, colour) & cand;
+    }
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      const int s = (S[k >> 2] >> (8 * (k & 3))) & 1;
+      const int sn = s ^ (int)((flip >> k) & 1u);
+      if ((flip >> k) & 1u) a.spin[site[k]] = (uint8_t)sn;
+      if (MEASURE && ((valid >> k) & 1u)) {
+        ups += sn;
+        bond += sn ? nlow[k] : -nlow[k];
+      }
+    }
+    if (MEASURE) nacc += __popc(flip);
+  }
+  if (MEASURE) {
+    long long v[kNumSums] = {bond, 0, 0, 0, 0, 0, ups, nacc};
+    block_sum_store(v, part + (long long)blockIdx.x * kNumSums);
+  }
+}
+
+// ------------------------------------------------------------ dispatch
+template <int C, bool ALLPER>
+static cudaError_t sc_dispatch(const IsingScArgs& a, const IsingTable& tab, RngKey key, int proposal, bool update,
+                               long long* part, int grid, int tpb, cudaStream_t s) {
+  const bool m = part != nullptr;
+  if (!update) {
+    ising_sc_kernel<C, ALLPER, true, false, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, tab, key, part);
+  } else if (proposal == VG_PROPOSE_FLIP) {
+    if (m) ising_sc_kernel<C, ALLPER, true, true, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, tab, key, part);
+    else ising_sc_kernel<C, ALLPER, false, true, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, tab, key, part);
+  } else {
+    if (m) ising_sc_kernel<C, ALLPER, true, true, VG_PROPOSE_RANDOM><<<grid, tpb, 0, s>>>(a, tab, key, part);
+    else ising_sc_kernel<C, ALLPER, false, true, VG_PROPOSE_RANDOM><<<grid, tpb, 0, s>>>(a, tab, key, part);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ising_sc(const IsingScArgs& a, const IsingTable& tab, RngKey key, int colour, int proposal,
+                            bool all_periodic, bool update, long long* part, int grid, int tpb, cudaStream_t s) {
+  if (colour == 0) {
+    return all_periodic ? sc_dispatch<0, true>(a, tab, key, proposal, update, part, grid, tpb, s)
+                        : sc_dispatch<0, false>(a, tab, key, proposal, update, part, grid, tpb, s);
+  }
+  return all_periodic ? sc_dispatch<1, true>(a, tab, key, proposal, update, part, grid, tpb, s)
+                      : sc_dispatch<1, false>(a, tab, key, proposal, update, part, grid, tpb, s);
+}
+
+template <int ZT>
+static cudaError_t gen_dispatch(const IsingGenArgs& a, const IsingTable& tab, RngKey key, int colour, int proposal,
+                                bool update, long long* part, int grid, int tpb, cudaStream_t s) {
+  const bool m = part != nullptr;
+  if (!update) {
+    ising_gen_kernel<ZT, true, false, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, tab, key, colour, part);
+  } else if (proposal == VG_PROPOSE_FLIP) {
+    if (m) ising_gen_kernel<ZT, true, true, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, tab, key, colour, part);
+    else ising_gen_kernel<ZT, false, true, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, tab, key, colour, part);
+  } else {
+    if (m) ising_gen_kernel<ZT, true, true, VG_PROPOSE_RANDOM><<<grid, tpb, 0, s>>>(a, tab, key, colour, part);
+    else ising_gen_kernel<ZT, false, true, VG_PROPOSE_RANDOM><<<grid, tpb, 0, s>>>(a, tab, key, colour, part);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ising_gen(const IsingGenArgs& a, const IsingTable& tab, RngKey key, int colour, int proposal,
+                             bool update, long long* part, int grid, int tpb, cudaStream_t s) {
+  if (a.z <= 6) return gen_dispatch<6>(a, tab, key, colour, proposal, update, part, grid, tpb, s);
+  if (a.z <= 8) return gen_dispatch<8>(a, tab, key, colour, proposal, update, part, grid, tpb, s);
+  return gen_dispatch<12>(a, tab, key, colour, proposal, update, part, grid, tpb, s);
+}
+
+}  // namespace vg

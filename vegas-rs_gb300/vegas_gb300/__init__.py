@@ -1,0 +1,319 @@
+"""Python binding of the vegas GB300 Metropolis engine (libvegas_gpu.so).
+
+Mirrors the pieces of the vegas API the engine replaces, with the same names
+and meaning:
+
+* ``Lattice.sc/bcc/fcc`` + ``expand`` + per-axis PBC (src/input.rs:296-322);
+* the energy terms ``Exchange``, ``UniaxialAnisotropy``, ``Zeeman``,
+  ``Gauge`` and the ``hamiltonian(...)`` builder, which nests terms into a
+  Compound exactly like the ``hamiltonian!`` macro (src/energy.rs:273-290);
+* ``Engine``: the device-resident state + Metropolis integrator
+  (MetropolisFlipIntegrator / MetropolisIntegrator, src/integrator.rs:56-138),
+  with ``set_thermostat`` (src/thermostat.rs) and per-sweep E / |M|.
+
+All compute runs in the CUDA library; this module only marshals arguments.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import Optional, Sequence, Tuple
+
+import numpy as np
+
+from . import _abi
+from ._abi import (CELL_BCC, CELL_FCC, CELL_SC, FP32, FP64, PATH_AUTO, PATH_GENERIC, PATH_STRUCTURED,
+                   PROPOSE_FLIP, PROPOSE_RANDOM, SPIN_HEISENBERG, SPIN_ISING, Sums, VegasGpuError)
+
+__all__ = [
+    "Lattice", "Exchange", "UniaxialAnisotropy", "Zeeman", "Gauge", "CubicAnisotropy", "hamiltonian",
+    "Engine", "Sums", "VegasGpuError", "lib", "SPIN_ISING", "SPIN_HEISENBERG", "PROPOSE_FLIP",
+    "PROPOSE_RANDOM", "PATH_AUTO", "PATH_GENERIC", "PATH_STRUCTURED", "FP32", "FP64",
+]
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """The loaded CUDA library (raises if it is not built)."""
+    global _lib
+    if _lib is None:
+        _lib = _abi.load()
+    return _lib
+
+
+def _check(rc: int, ctx=None):
+    if rc != _abi.VG_OK:
+        msg = lib().vg_last_error(ctx)
+        raise VegasGpuError(rc, (msg or b"").decode() or lib().vg_status_string(rc).decode())
+
+
+# ------------------------------------------------------------------ lattice
+@dataclass(frozen=True)
+class Lattice:
+    """``Lattice::<cell>(1.0).expand(nx, ny, nz)`` with drop_x/y/z on open axes."""
+
+    cell: int
+    nx: int
+    ny: int
+    nz: int
+    pbc: Tuple[bool, bool, bool] = (True, True, True)
+
+    @staticmethod
+    def sc(nx, ny=None, nz=None, pbc=(True, True, True)):
+        return Lattice(CELL_SC, nx, ny if ny is not None else nx, nz if nz is not None else nx, tuple(pbc))
+
+    @staticmethod
+    def bcc(nx, ny=None, nz=None, pbc=(True, True, True)):
+        return Lattice(CELL_BCC, nx, ny if ny is not None else nx, nz if nz is not None else nx, tuple(pbc))
+
+    @staticmethod
+    def fcc(nx, ny=None, nz=None, pbc=(True, True, True)):
+        return Lattice(CELL_FCC, nx, ny if ny is not None else nx, nz if nz is not None else nx, tuple(pbc))
+
+    def desc(self) -> _abi.LatticeDesc:
+        return _abi.LatticeDesc(self.cell, self.nx, self.ny, self.nz, int(self.pbc[0]), int(self.pbc[1]),
+                                int(self.pbc[2]))
+
+    @property
+    def basis(self) -> int:
+        return {CELL_SC: 1, CELL_BCC: 2, CELL_FCC: 4}[self.cell]
+
+    @property
+    def n_sites(self) -> int:
+        return self.nx * self.ny * self.nz * self.basis
+
+    def neighbours(self) -> np.ndarray:
+        d = self.desc()
+        n, z = C.c_int64(), C.c_int32()
+        _check(lib().vg_lattice_neighbours(C.byref(d), None, 0, C.byref(n), C.byref(z)))
+        out = np.empty(n.value * z.value, dtype=np.int32)
+        _check(lib().vg_lattice_neighbours(C.byref(d), out.ctypes.data_as(C.POINTER(C.c_int32)), out.size,
+                                           C.byref(n), C.byref(z)))
+        return out.reshape(n.value, z.value)
+
+    def colouring(self) -> Tuple[np.ndarray, int]:
+        d = self.desc()
+        out = np.empty(self.n_sites, dtype=np.int32)
+        nc = C.c_int32()
+        _check(lib().vg_lattice_colouring(C.byref(d), out.ctypes.data_as(C.POINTER(C.c_int32)), out.size,
+                                          C.byref(nc)))
+        return out, nc.value
+
+
+# ------------------------------------------------------------------ energies
+@dataclass
+class Exchange:
+    """Exchange::from_lattice(J, lattice): per site -J sum_j s_i.s_j."""
+    J: float = 1.0
+
+
+@dataclass
+class UniaxialAnisotropy:
+    """UniaxialAnisotropy::new(axis, K): per site +K (s.axis)^2."""
+    axis: Sequence[float] = (0.0, 0.0, 1.0)
+    K: float = 1.0
+
+
+@dataclass
+class Zeeman:
+    """Zeeman::new(): per site +|B| (s.b) with the thermostat's field."""
+    sign: float = 1.0
+
+
+@dataclass
+class Gauge:
+    """Gauge::new(g): per site g."""
+    value: float = 0.0
+
+
+@dataclass
+class CubicAnisotropy:
+    """Extension without a reference counterpart: per site -Kc (sx^4+sy^4+sz^4)."""
+    Kc: float = 0.0
+
+
+def hamiltonian(*terms) -> _abi.HamiltonianDesc:
+    """Flatten terms as the ``hamiltonian!`` macro nests them.
+
+    One term keeps that term's own ``total_energy``; two or more form a
+    Compound whose total is sum_i energy(i).  Repeated terms of one kind add
+    their per-site coefficients.
+    """
+    if not terms:
+        raise ValueError("hamiltonian needs at least one term")
+    h = _abi.HamiltonianDesc()
+    h.zeeman_sign = 0.0
+    for t in terms:
+        if isinstance(t, Exchange):
+            h.has_exchange = 1
+            h.exchange += t.J
+        elif isinstance(t, UniaxialAnisotropy):
+            if h.has_anisotropy and tuple(h.anisotropy_axis) != tuple(t.axis):
+                raise ValueError("two anisotropy terms with different axes are not supported")
+            h.has_anisotropy = 1
+            h.anisotropy += t.K
+            for i in range(3):
+                h.anisotropy_axis[i] = t.axis[i]
+        elif isinstance(t, Zeeman):
+            h.has_zeeman = 1
+            h.zeeman_sign += t.sign
+        elif isinstance(t, Gauge):
+            h.has_gauge = 1
+            h.gauge += t.value
+        elif isinstance(t, CubicAnisotropy):
+            h.has_cubic = 1
+            h.cubic += t.Kc
+        else:
+            raise TypeError(f"unknown energy term {t!r}")
+    h.compound = 1 if len(terms) >= 2 else 0
+    return h
+
+
+# ------------------------------------------------------------------ engine
+class Engine:
+    """A device-resident lattice state driven by the GPU Metropolis integrator."""
+
+    def __init__(self, lattice: Lattice, ham: _abi.HamiltonianDesc, spin: int = SPIN_ISING, seed: int = 0,
+                 proposal: Optional[int] = None, path: int = PATH_AUTO, precision: int = FP32, replica: int = 0,
+                 threads_per_block: int = 0, blocks_per_sm: int = 0, device: int = -1):
+        L = lib()
+        o = _abi.Options()
+        _check(L.vg_options_default(spin, C.byref(o)))
+        if proposal is not None:
+            o.proposal = proposal
+        o.path, o.precision, o.replica = path, precision, replica
+        o.threads_per_block, o.blocks_per_sm, o.device = threads_per_block, blocks_per_sm, device
+        self.lattice, self.ham, self.spin_kind = lattice, ham, spin
+        d = lattice.desc()
+        h = C.c_void_p()
+        _check(L.vg_ctx_create_ex(C.byref(d), C.byref(ham), C.byref(o), C.c_uint64(seed), C.byref(h)))
+        self._h = h
+        self.n = lattice.n_sites
+
+    # lifecycle
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().vg_ctx_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def info(self) -> _abi.Info:
+        i = _abi.Info()
+        _check(lib().vg_ctx_info(self._h, C.byref(i)), self._h)
+        return i
+
+    # state
+    def init_random(self):
+        _check(lib().vg_init_random(self._h), self._h)
+
+    def set_state(self, spins: np.ndarray):
+        if self.spin_kind == SPIN_ISING:
+            a = np.ascontiguousarray(spins, dtype=np.int8)
+        else:
+            a = np.ascontiguousarray(spins, dtype=np.float64)
+        _check(lib().vg_set_state(self._h, a.ctypes.data, C.c_int64(self.n)), self._h)
+
+    def get_state(self) -> np.ndarray:
+        if self.spin_kind == SPIN_ISING:
+            out = np.empty(self.n, dtype=np.int8)
+        else:
+            out = np.empty((self.n, 3), dtype=np.float64)
+        _check(lib().vg_get_state(self._h, out.ctypes.data, C.c_int64(self.n)), self._h)
+        return out
+
+    def set_thermostat(self, temperature: float, b=(0.0, 0.0, 1.0), magnitude: float = 0.0):
+        bb = (C.c_double * 3)(*b)
+        _check(lib().vg_set_thermostat(self._h, temperature, bb, magnitude), self._h)
+
+    @property
+    def sweep_index(self) -> int:
+        v = C.c_uint64()
+        _check(lib().vg_get_sweep_index(self._h, C.byref(v)), self._h)
+        return v.value
+
+    @sweep_index.setter
+    def sweep_index(self, v: int):
+        _check(lib().vg_set_sweep_index(self._h, C.c_uint64(v)), self._h)
+
+    # sweeps
+    def sweeps(self, n: int, measure: bool = True):
+        """Run n sweeps; returns (E, |M|) arrays per sweep when measuring."""
+        if not measure:
+            _check(lib().vg_sweeps(self._h, C.c_uint64(n), 0, None, None), self._h)
+            return None
+        E = np.empty(max(n, 1), dtype=np.float64)
+        M = np.empty(max(n, 1), dtype=np.float64)
+        dp = C.POINTER(C.c_double)
+        _check(lib().vg_sweeps(self._h, C.c_uint64(n), 1, E.ctypes.data_as(dp), M.ctypes.data_as(dp)), self._h)
+        return E[:n], M[:n]
+
+    def sweeps_sums(self, n: int) -> np.ndarray:
+        out = (Sums * max(n, 1))()
+        _check(lib().vg_sweeps_sums(self._h, C.c_uint64(n), out), self._h)
+        return np.frombuffer(out, dtype=np.float64).reshape(-1, 8)[:n].copy()
+
+    def sweeps_async(self, n: int, measure: bool = True):
+        _check(lib().vg_sweeps_async(self._h, C.c_uint64(n), int(measure)), self._h)
+
+    def read_sums(self, n: int) -> np.ndarray:
+        out = (Sums * max(n, 1))()
+        _check(lib().vg_read_sums(self._h, C.c_uint64(n), out), self._h)
+        return np.frombuffer(out, dtype=np.float64).reshape(-1, 8)[:n].copy()
+
+    def synchronize(self):
+        _check(lib().vg_synchronize(self._h), self._h)
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        _check(lib().vg_get_stream(self._h, C.byref(s)), self._h)
+        return s.value or 0
+
+    def set_stream(self, stream_ptr: int):
+        _check(lib().vg_set_stream(self._h, C.c_void_p(stream_ptr)), self._h)
+
+    def time_passes(self, n: int, measure: bool = True) -> Tuple[float, float]:
+        """Mean colour-pass and sweep durations (ms) over n real sweeps (CUDA events)."""
+        a, b = C.c_double(), C.c_double()
+        _check(lib().vg_time_passes(self._h, C.c_uint64(n), int(measure), C.byref(a), C.byref(b)), self._h)
+        return a.value, b.value
+
+    # observables
+    def current_sums(self) -> np.ndarray:
+        s = Sums()
+        _check(lib().vg_current_sums(self._h, C.byref(s)), self._h)
+        return np.frombuffer(s, dtype=np.float64).copy()
+
+    def total_energy(self) -> float:
+        e = C.c_double()
+        _check(lib().vg_total_energy(self._h, C.byref(e)), self._h)
+        return e.value
+
+    def magnetization(self):
+        m = (C.c_double * 3)()
+        mag = C.c_double()
+        _check(lib().vg_magnetization(self._h, m, C.byref(mag)), self._h)
+        return np.array(list(m)), mag.value
+
+    def energy_from_sums(self, sums_row) -> Tuple[float, float]:
+        s = Sums(*[float(v) for v in sums_row])
+        e, m = C.c_double(), C.c_double()
+        _check(lib().vg_energy_from_sums(self._h, C.byref(s), C.byref(e), C.byref(m)), self._h)
+        return e.value, m.value
+
+
+def device_count() -> int:
+    n = C.c_int32()
+    lib().vg_device_count(C.byref(n))
+    return n.value
