@@ -100,7 +100,7 @@ def test_set_get_roundtrip_and_observables(V, O):
         eng.set_state(s)
         assert np.array_equal(eng.get_state(), s)
         eng.set_thermostat(2.0, (0, 0, 1), 0.5)
-        g = O.Graph(O.lattice(*lat))
+        g = O.Graph(O.lattice(lat[0], *lat[1], lat[2]))
         Href = O.Hamiltonian(has_exchange=1, J=1.0, has_zeeman=1, zeeman_sign=1.0, has_gauge=1, gauge=0.25,
                              compound=1)
         e_ref = g.ref_total_energy(0, s, Href, b=(0, 0, 1), bmag=0.5)
@@ -116,10 +116,13 @@ def test_low_and_high_temperature_limits(V):
         eng.set_thermostat(0.0)  # clamped to f64::EPSILON: nothing can flip upward in energy
         E, M = eng.sweeps(3)
         assert np.all(E == -3 * 32 * 16 * 16) and np.all(M == 32 * 16 * 16)
-        eng.set_thermostat(1e9)
-        E, M = eng.sweeps(50)
+        # (at T -> infinity every proposal is accepted and checkerboard passes
+        # flip whole sublattices deterministically, as the oracle does too; a
+        # large finite T disorders the lattice)
+        eng.set_thermostat(50.0)
+        E, M = eng.sweeps(300)
         n = 32 * 16 * 16
-        assert abs(E[10:].mean()) < 0.02 * 3 * n and M[10:].mean() < 0.05 * n
+        assert abs(E[100:].mean()) < 0.1 * 3 * n and M[100:].mean() < 0.1 * n
 
 
 def test_invalid_spins_rejected(V):

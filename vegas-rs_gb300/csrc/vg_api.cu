@@ -192,14 +192,16 @@ int greedy_colouring(const Geometry& g, const std::vector<int32_t>& nbr, std::ve
 
 // ------------------------------------------------------------ device helpers
 struct ScMap {
-  long long Lx, Ly, Hx;
+  uint32_t Lx, Ly, Hx;
+  FastDiv fLx, fLy;
 };
 
 __device__ __forceinline__ void sc_locate(long long i, const ScMap& m, int& c, long long& j) {
-  const long long x = i % m.Lx, r = i / m.Lx;
-  const long long y = r % m.Ly, zz = r / m.Ly;
+  const uint32_t ii = (uint32_t)i;
+  const uint32_t r = fdiv(ii, m.fLx), x = ii - r * m.Lx;
+  const uint32_t zz = fdiv(r, m.fLy), y = r - zz * m.Ly;
   c = (int)((x + y + zz) & 1);
-  j = r * m.Hx + (x >> 1);
+  j = (long long)r * m.Hx + (x >> 1);
 }
 
 __global__ void ising_import(const int8_t* __restrict__ src, long long n, int structured, ScMap m, uint8_t* d0,
@@ -386,9 +388,11 @@ int dalloc(vg_ctx* c, void** p, size_t bytes) {
 
 ScMap sc_map(const vg_ctx* c) {
   ScMap m;
-  m.Lx = c->lat.nx;
-  m.Ly = c->lat.ny;
-  m.Hx = c->lat.nx / 2;
+  m.Lx = (uint32_t)c->lat.nx;
+  m.Ly = (uint32_t)c->lat.ny;
+  m.Hx = (uint32_t)(c->lat.nx / 2);
+  m.fLx = make_fastdiv(m.Lx);
+  m.fLy = make_fastdiv(m.Ly);
   return m;
 }
 
@@ -398,6 +402,7 @@ RngKey rng_key(const vg_ctx* c, uint64_t sweep) {
   k.k1 = (uint32_t)(c->seed >> 32);
   k.replica = c->opt.replica;
   k.sweep = (uint32_t)sweep;
+  k.ks = make_key_schedule(k.k0, k.k1);
   return k;
 }
 
@@ -440,6 +445,31 @@ IsingTable ising_table(const vg_ctx* c) {
       }
       t.thr[s01 * W + ns + z] = thr;
     }
+  // byte tables for lattices whose sites all have the same neighbour count
+  t.zeff = -1;
+  if (c->path == VG_PATH_STRUCTURED) {
+    const int ext[3] = {c->lat.nx, c->lat.ny, c->lat.nz};
+    const int per[3] = {c->lat.pbc_x, c->lat.pbc_y, c->lat.pbc_z};
+    int zeff = 0;
+    bool uniform = true;
+    for (int a = 0; a < 3; ++a) {
+      if (per[a]) zeff += 2;
+      else if (ext[a] > 1) uniform = false;
+    }
+    if (uniform) {
+      t.zeff = zeff;
+      uint8_t top[2][8] = {};
+      for (int s01 = 0; s01 < 2; ++s01)
+        for (int nu = 0; nu <= zeff; ++nu) {
+          const unsigned long long thr = t.thr[s01 * W + 2 * nu - zeff + z];
+          top[s01][nu] = thr >= (1ull << 32) ? 0xFF : (uint8_t)(thr >> 24);
+        }
+      for (int s01 = 0; s01 < 2; ++s01)
+        for (int h = 0; h < 2; ++h)
+          t.top[s01][h] = (uint32_t)top[s01][4 * h] | ((uint32_t)top[s01][4 * h + 1] << 8) |
+                          ((uint32_t)top[s01][4 * h + 2] << 16) | ((uint32_t)top[s01][4 * h + 3] << 24);
+    }
+  }
   return t;
 }
 
@@ -512,12 +542,13 @@ int launch_pass(vg_ctx* c, int colour, bool update, uint64_t sweep, void* part_r
       a.Ly = c->lat.ny;
       a.Lz = c->lat.nz;
       a.G = a.Hx / kIsingGroup;
-      a.groups = (long long)a.G * a.Ly * a.Lz;
+      a.groups = (uint32_t)a.G * (uint32_t)a.Ly * (uint32_t)a.Lz;
       a.pbx = c->lat.pbc_x != 0;
       a.pby = c->lat.pbc_y != 0;
       a.pbz = c->lat.pbc_z != 0;
-      e = launch_ising_sc(a, tab, key, colour, c->opt.proposal, c->all_periodic, update, part, c->grid, c->tpb,
-                          c->stream);
+      a.fG = make_fastdiv((uint32_t)a.G);
+      a.fLy = make_fastdiv((uint32_t)a.Ly);
+      e = launch_ising_sc(a, tab, key, colour, c->opt.proposal, update, part, c->grid, c->tpb, c->stream);
     } else {
       IsingGenArgs a;
       a.spin = (uint8_t*)c->spin[0][0];
@@ -543,10 +574,12 @@ int launch_pass(vg_ctx* c, int colour, bool update, uint64_t sweep, void* part_r
         a.Hx = c->lat.nx / 2;
         a.Ly = c->lat.ny;
         a.Lz = c->lat.nz;
-        a.n_c = (long long)a.Hx * a.Ly * a.Lz;
+        a.n_c = (uint32_t)a.Hx * (uint32_t)a.Ly * (uint32_t)a.Lz;
         a.pbx = c->lat.pbc_x != 0;
         a.pby = c->lat.pbc_y != 0;
         a.pbz = c->lat.pbc_z != 0;
+        a.fHx = make_fastdiv((uint32_t)a.Hx);
+        a.fLy = make_fastdiv((uint32_t)a.Ly);
         return launch_heis_sc<R>(a, P, key, colour, c->opt.proposal, update, part, c->grid, c->tpb, c->stream);
       }
       HeisGenArgs<R> a;

@@ -105,15 +105,16 @@ __global__ void __launch_bounds__(256) heis_sc_kernel(const HeisScArgs<R> a, con
   R acc[kNumSums];
 #pragma unroll
   for (int i = 0; i < kNumSums; ++i) acc[i] = (R)0;
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < a.n_c; j += stride) {
-    const long long row = j / a.Hx;
-    const int h = (int)(j - row * a.Hx);
-    const int y = (int)(row % a.Ly), z = (int)(row / a.Ly);
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < a.n_c; j += stride) {
+    const int row = (int)fdiv(j, a.fHx);
+    const int h = (int)(j - (uint32_t)row * a.Hx);
+    const int z = (int)fdiv((uint32_t)row, a.fLy);
+    const int y = row - z * a.Ly;
     const int p = (y + z + C) & 1;
-    const long long rb = row * a.Hx;
+    const int rb = row * a.Hx;
     V3<R> hs = {(R)0, (R)0, (R)0};
-    auto add = [&](long long q) {
+    auto add = [&](int q) {
       hs.x += __ldg(nx + q);
       hs.y += __ldg(ny + q);
       hs.z += __ldg(nz + q);
@@ -130,20 +131,19 @@ __global__ void __launch_bounds__(256) heis_sc_kernel(const HeisScArgs<R> a, con
     }
     if (hxok) add(rb + hx);
     if (y > 0) add(rb - a.Hx + h);
-    else if (ALLPER || a.pby) add(rb + (long long)(a.Ly - 1) * a.Hx + h);
+    else if (ALLPER || a.pby) add(rb + (a.Ly - 1) * a.Hx + h);
     if (y < a.Ly - 1) add(rb + a.Hx + h);
-    else if (ALLPER || a.pby) add(rb - (long long)(a.Ly - 1) * a.Hx + h);
-    const long long plane = (long long)a.Ly * a.Hx;
+    else if (ALLPER || a.pby) add(rb - (a.Ly - 1) * a.Hx + h);
+    const int plane = a.Ly * a.Hx;
     if (z > 0) add(rb - plane + h);
-    else if (ALLPER || a.pbz) add(rb + (long long)(a.Lz - 1) * plane + h);
+    else if (ALLPER || a.pbz) add(rb + (a.Lz - 1) * plane + h);
     if (z < a.Lz - 1) add(rb + plane + h);
-    else if (ALLPER || a.pbz) add(rb - (long long)(a.Lz - 1) * plane + h);
+    else if (ALLPER || a.pbz) add(rb - (a.Lz - 1) * plane + h);
 
-    const long long q = rb + h;
+    const int q = rb + h;
     V3<R> s = {ox[q], oy[q], oz[q]};
     if (UPDATE) {
-      const uint4 w = philox(make_uint4((uint32_t)j, key.sweep, (kTagHeis << 24) | ((uint32_t)C << 8), key.replica),
-                             key.k0, key.k1);
+      const uint4 w = philox_ks(make_uint4(j, key.sweep, (kTagHeis << 24) | ((uint32_t)C << 8), key.replica), key.ks);
       V3<R> sn;
       if (heis_update<R, PROP>(s, hs, P, w, sn)) {
         ox[q] = sn.x;
@@ -192,8 +192,8 @@ __global__ void __launch_bounds__(256) heis_gen_kernel(const HeisGenArgs<R> a, c
     }
     V3<R> s = {a.x[i], a.y[i], a.z[i]};
     if (UPDATE) {
-      const uint4 w = philox(make_uint4((uint32_t)j, key.sweep, (kTagHeis << 24) | ((uint32_t)colour << 8), key.replica),
-                             key.k0, key.k1);
+      const uint4 w =
+          philox_ks(make_uint4((uint32_t)j, key.sweep, (kTagHeis << 24) | ((uint32_t)colour << 8), key.replica), key.ks);
       V3<R> sn;
       if (heis_update<R, PROP>(s, hs, P, w, sn)) {
         a.x[i] = sn.x;

@@ -25,6 +25,8 @@ enum : uint32_t {
 
 // ------------------------------------------------------------ Philox4x32-10
 // Salmon et al., "Parallel random numbers: as easy as 1, 2, 3" (SC'11).
+// Each round: two 32x32->64 multiplies (one wide multiply each) and two
+// three-input XORs with the round key.
 __host__ __device__ __forceinline__ uint4 philox(uint4 c, uint32_t k0, uint32_t k1) {
 #pragma unroll
   for (int r = 0; r < 10; ++r) {
@@ -32,15 +34,35 @@ __host__ __device__ __forceinline__ uint4 philox(uint4 c, uint32_t k0, uint32_t 
       k0 += 0x9E3779B9u;
       k1 += 0xBB67AE85u;
     }
-#ifdef __CUDA_ARCH__
-    const uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
-    const uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
-#else
-    const uint64_t p0 = (uint64_t)0xD2511F53u * c.x, p1 = (uint64_t)0xCD9E8D57u * c.z;
-    const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
-    const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
-#endif
-    c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
+    const unsigned long long p0 = (unsigned long long)0xD2511F53u * c.x;
+    const unsigned long long p1 = (unsigned long long)0xCD9E8D57u * c.z;
+    c = make_uint4((uint32_t)(p1 >> 32) ^ c.y ^ k0, (uint32_t)p1, (uint32_t)(p0 >> 32) ^ c.w ^ k1, (uint32_t)p0);
+  }
+  return c;
+}
+
+// Round keys precomputed on the host; passed as kernel parameters they are
+// read straight from the constant bank by the XORs.
+struct KeySchedule {
+  uint32_t k0[10], k1[10];
+};
+
+inline KeySchedule make_key_schedule(uint32_t k0, uint32_t k1) {
+  KeySchedule s;
+  for (int r = 0; r < 10; ++r) {
+    s.k0[r] = k0 + (uint32_t)r * 0x9E3779B9u;
+    s.k1[r] = k1 + (uint32_t)r * 0xBB67AE85u;
+  }
+  return s;
+}
+
+__device__ __forceinline__ uint4 philox_ks(uint4 c, const KeySchedule& ks) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const unsigned long long p0 = (unsigned long long)0xD2511F53u * c.x;
+    const unsigned long long p1 = (unsigned long long)0xCD9E8D57u * c.z;
+    c = make_uint4((uint32_t)(p1 >> 32) ^ c.y ^ ks.k0[r], (uint32_t)p1, (uint32_t)(p0 >> 32) ^ c.w ^ ks.k1[r],
+                   (uint32_t)p0);
   }
   return c;
 }
@@ -50,22 +72,48 @@ __device__ __forceinline__ uint32_t blk_byte(const uint4& b, int k) {
   return (w >> (8 * (k & 3))) & 0xFFu;
 }
 
+// Division by a runtime constant d for dividends n < 2^31: one multiply-high,
+// one add, one shift (q = (umulhi(n, m) + n) >> s with s = ceil(log2 d),
+// m = floor(2^32 (2^s - d) / d) + 1).
+struct FastDiv {
+  uint32_t d, m, s;
+};
+
+inline FastDiv make_fastdiv(uint32_t d) {
+  FastDiv f;
+  f.d = d;
+  f.s = 0;
+  while ((1ull << f.s) < d) ++f.s;
+  f.m = (uint32_t)((((1ull << 32) * ((1ull << f.s) - d)) / d) + 1);
+  return f;
+}
+
+__device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv& f) { return (__umulhi(n, f.m) + n) >> f.s; }
+
 // Ising acceptance table: index s*(2z+1) + nsum + z, value = threshold on a
 // 32-bit uniform (accept iff U < thr); thr >= 2^32 means always.
+// For lattices where every site has zeff existing neighbours (zeff < 0
+// otherwise), byte tables indexed by the up-neighbour count n_up in
+// [0, zeff]: top[s][.] holds the most significant byte of thr(s, n_up)
+// (0xFF where the move always accepts); [0] = entries 0..3, [1] = 4..7.
 struct IsingTable {
   unsigned long long thr[2 * (2 * kMaxZ + 1)];
+  uint32_t top[2][2];
+  int zeff;
 };
 
 struct RngKey {
   uint32_t k0, k1, replica, sweep;
+  KeySchedule ks;
 };
 
 // ------------------------------------------------------------ kernel args
 struct IsingScArgs {          // sc checkerboard, class-separated uint8 0/1
   uint8_t* cls[2];
-  long long groups;           // 16-site groups per class
+  uint32_t groups;            // 16-site groups per class
   int Hx, Ly, Lz, G;          // Hx = Lx/2, G = Hx/16
   int pbx, pby, pbz;
+  FastDiv fG, fLy;
 };
 
 struct IsingGenArgs {         // any lattice: natural order uint8 0/1 + ELL
@@ -82,9 +130,10 @@ struct HeisScArgs {           // sc checkerboard, class-separated SoA
   R* x[2];
   R* y[2];
   R* z[2];
-  long long n_c;              // sites per class
+  uint32_t n_c;               // sites per class
   int Hx, Ly, Lz;
   int pbx, pby, pbz;
+  FastDiv fHx, fLy;
 };
 
 template <typename R>
@@ -110,8 +159,7 @@ struct HeisParams {
 // row of kNumSums partials per block (int64 for Ising, double for
 // Heisenberg).  update = false only measures.
 cudaError_t launch_ising_sc(const IsingScArgs& a, const IsingTable& tab, RngKey key, int colour,
-                            int proposal, bool all_periodic, bool update, long long* part, int grid,
-                            int tpb, cudaStream_t s);
+                            int proposal, bool update, long long* part, int grid, int tpb, cudaStream_t s);
 cudaError_t launch_ising_gen(const IsingGenArgs& a, const IsingTable& tab, RngKey key, int colour,
                              int proposal, bool update, long long* part, int grid, int tpb,
                              cudaStream_t s);

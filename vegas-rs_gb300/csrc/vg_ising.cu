@@ -36,9 +36,9 @@ __device__ __forceinline__ uint32_t decide16(const unsigned long long (&t)[16], 
   }
 #pragma unroll 1
   for (int d = 0; d < 4 && und; ++d) {
-    const uint4 b = philox(make_uint4(g, key.sweep, (kTagIsingAccept << 24) | ((uint32_t)colour << 8) | (uint32_t)d,
-                                      key.replica),
-                           key.k0, key.k1);
+    const uint4 b = philox_ks(make_uint4(g, key.sweep, (kTagIsingAccept << 24) | ((uint32_t)colour << 8) | (uint32_t)d,
+                                         key.replica),
+                              key.ks);
     const uint32_t w[4] = {b.x, b.y, b.z, b.w};
     const int sh = 24 - 8 * d;
 #pragma unroll
@@ -67,8 +67,8 @@ __device__ __forceinline__ uint32_t gather4(uint32_t x) { return (((x & 0x010101
 // (u < 0.5) proposes Up.  Returns the mask of sites whose proposal differs.
 __device__ __forceinline__ uint32_t propose_random16(const uint32_t (&s)[4], const RngKey& key, uint32_t g,
                                                      int colour) {
-  const uint4 b = philox(make_uint4(g, key.sweep, (kTagIsingPropose << 24) | ((uint32_t)colour << 8), key.replica),
-                         key.k0, key.k1);
+  const uint4 b = philox_ks(make_uint4(g, key.sweep, (kTagIsingPropose << 24) | ((uint32_t)colour << 8), key.replica),
+                            key.ks);
   const uint32_t w[4] = {b.x, b.y, b.z, b.w};
   uint32_t diff = 0;
 #pragma unroll
@@ -80,9 +80,71 @@ __device__ __forceinline__ uint32_t propose_random16(const uint32_t (&s)[4], con
 }
 
 // ------------------------------------------------------------------ sc
-template <int C, bool ALLPER, bool MEASURE, bool UPDATE, int PROP>
-__global__ void __launch_bounds__(256) ising_sc_kernel(const IsingScArgs a, const IsingTable tab, const RngKey key,
-                                                       long long* __restrict__ part) {
+// Byte-parallel helpers: a 32-bit word carries 4 sites, one byte each.
+// PRMT selector from 4 bytes in [0, 7].
+__device__ __forceinline__ uint32_t nibble_selector(uint32_t a) {
+  const uint32_t y = (a | (a >> 4)) & 0x00770077u;
+  return (y | (y >> 8)) & 0x7777u;
+}
+// 0x01 in each byte where r >= t (unsigned): two 16-bit lanes per word, the
+// borrow of 0x100 + r - t never crosses a lane.
+__device__ __forceinline__ uint32_t bytes_ge(uint32_t r, uint32_t t) {
+  const uint32_t e = ((r & 0x00FF00FFu) | 0x01000100u) - (t & 0x00FF00FFu);
+  const uint32_t o = (((r >> 8) & 0x00FF00FFu) | 0x01000100u) - ((t >> 8) & 0x00FF00FFu);
+  return ((e >> 8) & 0x00010001u) | (o & 0x01000100u);
+}
+// 0x01 in each byte of x that is zero
+__device__ __forceinline__ uint32_t bytes_zero(uint32_t x) {
+  const uint32_t t = (x & 0x7F7F7F7Fu) + 0x7F7F7F7Fu;
+  return (~(t | x) >> 7) & 0x01010101u;
+}
+__device__ __forceinline__ uint32_t byte_at(uint32_t w0, uint32_t w1, uint32_t w2, uint32_t w3, int k) {
+  const uint32_t lo = (k & 4) ? w1 : w0, hi = (k & 4) ? w3 : w2;
+  return (((k & 8) ? hi : lo) >> (8 * (k & 3))) & 0xFFu;
+}
+
+// Block sum of the three live Ising partials (bond, up spins, accepted) into
+// one kNumSums row.
+__device__ __forceinline__ void block_sum3_store(int a, int b, int c, long long* out) {
+  __shared__ int red[3][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, o);
+    b += __shfl_down_sync(0xffffffffu, b, o);
+    c += __shfl_down_sync(0xffffffffu, c, o);
+  }
+  if (lane == 0) {
+    red[0][warp] = a;
+    red[1][warp] = b;
+    red[2][warp] = c;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    long long sa = 0, sb = 0, sc = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      sa += red[0][w];
+      sb += red[1][w];
+      sc += red[2][w];
+    }
+    out[0] = sa;
+    out[1] = out[2] = out[3] = out[4] = out[5] = 0;
+    out[6] = sb;
+    out[7] = sc;
+  }
+}
+
+// UNIFORM: every site has the same number zeff of existing neighbours (each
+// axis periodic, or open with extent 1), so the up-neighbour count n_up in
+// [0, zeff] indexes 8-entry byte tables and four sites are decided per
+// word: the top threshold byte and the always-accept flag come from PRMT
+// lookups, the first random digit is compared byte-parallel, and only sites
+// whose digit ties with the threshold digit (probability 1/256) continue
+// digit by digit.  Otherwise the scalar decide16 path runs.  Both give the
+// same decisions as "accept iff U < thr".
+template <int C, bool UNIFORM, bool MEASURE, bool UPDATE, int PROP>
+__global__ void __launch_bounds__(256, UNIFORM ? 4 : 2) ising_sc_kernel(const IsingScArgs a, const IsingTable tab, const RngKey key,
+                                                          long long* __restrict__ part) {
   constexpr int Z = 6, W = 2 * Z + 1;
   __shared__ unsigned long long s_thr[2 * W];
   for (int i = threadIdx.x; i < 2 * W; i += blockDim.x) s_thr[i] = tab.thr[i];
@@ -90,14 +152,16 @@ __global__ void __launch_bounds__(256) ising_sc_kernel(const IsingScArgs a, cons
 
   uint8_t* __restrict__ own = a.cls[C];
   const uint8_t* __restrict__ oth = a.cls[C ^ 1];
-  long long bond = 0, ups = 0, nacc = 0;
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x; gid < a.groups; gid += stride) {
-    const long long row = gid / a.G;
-    const int h0 = (int)(gid - row * a.G) << 4;
-    const int y = (int)(row % a.Ly), z = (int)(row / a.Ly);
+  const int zoff = Z - tab.zeff;
+  int bond = 0, ups = 0, nacc = 0;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x; gid < a.groups; gid += stride) {
+    const int row = (int)fdiv(gid, a.fG);
+    const int h0 = (int)(gid - (uint32_t)row * a.G) << 4;
+    const int z = (int)fdiv((uint32_t)row, a.fLy);
+    const int y = row - z * a.Ly;
     const int p = (y + z + C) & 1;  // x parity of this row's class-C sites
-    const long long rb = row * a.Hx;
+    const int rb = row * a.Hx;
 
     const uint4 Sv = *reinterpret_cast<const uint4*>(own + rb + h0);
     const uint4 X0 = __ldg(reinterpret_cast<const uint4*>(oth + rb + h0));
@@ -106,11 +170,11 @@ __global__ void __launch_bounds__(256) ising_sc_kernel(const IsingScArgs a, cons
     bool xmiss = false;
     if (p == 0) {
       if (h0 > 0) e = __ldg(oth + rb + h0 - 1);
-      else if (ALLPER || a.pbx) e = __ldg(oth + rb + a.Hx - 1);
+      else if (a.pbx) e = __ldg(oth + rb + a.Hx - 1);
       else xmiss = true;
     } else {
       if (h0 + 16 < a.Hx) e = __ldg(oth + rb + h0 + 16);
-      else if (ALLPER || a.pbx) e = __ldg(oth + rb);
+      else if (a.pbx) e = __ldg(oth + rb);
       else xmiss = true;
     }
     uint32_t X1[4];
@@ -125,16 +189,15 @@ __global__ void __launch_bounds__(256) ising_sc_kernel(const IsingScArgs a, cons
       X1[2] = __byte_perm(X0.z, X0.w, 0x4321);
       X1[3] = __byte_perm(X0.w, e, 0x4321);
     }
-    long long rym, ryp, rzm, rzp;
-    rym = y > 0 ? row - 1 : ((ALLPER || a.pby) ? row + a.Ly - 1 : -1);
-    ryp = y < a.Ly - 1 ? row + 1 : ((ALLPER || a.pby) ? row - (a.Ly - 1) : -1);
-    rzm = z > 0 ? row - a.Ly : ((ALLPER || a.pbz) ? row + (long long)(a.Lz - 1) * a.Ly : -1);
-    rzp = z < a.Lz - 1 ? row + a.Ly : ((ALLPER || a.pbz) ? row - (long long)(a.Lz - 1) * a.Ly : -1);
+    const int rym = y > 0 ? row - 1 : (a.pby ? row + a.Ly - 1 : -1);
+    const int ryp = y < a.Ly - 1 ? row + 1 : (a.pby ? row - (a.Ly - 1) : -1);
+    const int rzm = z > 0 ? row - a.Ly : (a.pbz ? row + (a.Lz - 1) * a.Ly : -1);
+    const int rzp = z < a.Lz - 1 ? row + a.Ly : (a.pbz ? row - (a.Lz - 1) * a.Ly : -1);
     const uint4 zero4 = make_uint4(0, 0, 0, 0);
-    const uint4 Ym = rym >= 0 ? __ldg(reinterpret_cast<const uint4*>(oth + rym * a.Hx + h0)) : zero4;
-    const uint4 Yp = ryp >= 0 ? __ldg(reinterpret_cast<const uint4*>(oth + ryp * a.Hx + h0)) : zero4;
-    const uint4 Zm = rzm >= 0 ? __ldg(reinterpret_cast<const uint4*>(oth + rzm * a.Hx + h0)) : zero4;
-    const uint4 Zp = rzp >= 0 ? __ldg(reinterpret_cast<const uint4*>(oth + rzp * a.Hx + h0)) : zero4;
+    const uint4 Ym = rym >= 0 ? __ldg(reinterpret_cast<const uint4*>(oth + (size_t)rym * a.Hx + h0)) : zero4;
+    const uint4 Yp = ryp >= 0 ? __ldg(reinterpret_cast<const uint4*>(oth + (size_t)ryp * a.Hx + h0)) : zero4;
+    const uint4 Zm = rzm >= 0 ? __ldg(reinterpret_cast<const uint4*>(oth + (size_t)rzm * a.Hx + h0)) : zero4;
+    const uint4 Zp = rzp >= 0 ? __ldg(reinterpret_cast<const uint4*>(oth + (size_t)rzp * a.Hx + h0)) : zero4;
 
     const uint32_t S[4] = {Sv.x, Sv.y, Sv.z, Sv.w};
     const uint32_t A[4] = {X0.x + X1[0] + Ym.x + Yp.x + Zm.x + Zp.x, X0.y + X1[1] + Ym.y + Yp.y + Zm.y + Zp.y,
@@ -142,9 +205,9 @@ __global__ void __launch_bounds__(256) ising_sc_kernel(const IsingScArgs a, cons
     // M = 2A + (Z - Zc) per byte, where Zc counts existing neighbours; the
     // neighbour sum of site k is M_k - Z.
     uint32_t M[4];
-    if (ALLPER) {
+    if (UNIFORM) {
 #pragma unroll
-      for (int i = 0; i < 4; ++i) M[i] = 2u * A[i];
+      for (int i = 0; i < 4; ++i) M[i] = 2u * A[i] + (uint32_t)zoff * 0x01010101u;
     } else {
       const uint32_t zmiss = (uint32_t)((rym < 0) + (ryp < 0) + (rzm < 0) + (rzp < 0));
 #pragma unroll
@@ -155,29 +218,97 @@ __global__ void __launch_bounds__(256) ising_sc_kernel(const IsingScArgs a, cons
       }
     }
 
-    uint32_t flip = 0;
+    uint32_t F[4] = {0, 0, 0, 0};  // 0x01 bytes: sites that flip
     if (UPDATE) {
-      const uint32_t cand = PROP == VG_PROPOSE_FLIP ? 0xFFFFu : propose_random16(S, key, (uint32_t)gid, C);
-      unsigned long long t[16];
+      uint32_t cand[4] = {0x01010101u, 0x01010101u, 0x01010101u, 0x01010101u};
+      if (PROP == VG_PROPOSE_RANDOM) {
+        const uint4 b = philox_ks(make_uint4(gid, key.sweep, (kTagIsingPropose << 24) | ((uint32_t)C << 8), key.replica),
+                                  key.ks);
+        const uint32_t w[4] = {b.x, b.y, b.z, b.w};
 #pragma unroll
-      for (int k = 0; k < 16; ++k) {
-        const uint32_t idx = ((S[k >> 2] * (uint32_t)W + M[k >> 2]) >> (8 * (k & 3))) & 0xFFu;
-        t[k] = s_thr[idx];
+        for (int i = 0; i < 4; ++i) cand[i] = ((~w[i] >> 7) & 0x01010101u) ^ S[i];
       }
-      flip = decide16(t, cand, key, (uint32_t)gid, C) & cand;
+      if (UNIFORM) {
+        // first digit of every site's uniform against its threshold's top byte
+        // (0xFF for always-accept moves, whose ties resolve to accept below)
+        const uint4 b = philox_ks(make_uint4(gid, key.sweep, (kTagIsingAccept << 24) | ((uint32_t)C << 8), key.replica),
+                                  key.ks);
+        const uint32_t R[4] = {b.x, b.y, b.z, b.w};
+        uint32_t thr[4], anytie = 0;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const uint32_t sel = nibble_selector(A[i]);
+          const uint32_t sm = S[i] * 0xFFu;
+          thr[i] = (__byte_perm(tab.top[1][0], tab.top[1][1], sel) & sm) |
+                   (__byte_perm(tab.top[0][0], tab.top[0][1], sel) & ~sm);
+          F[i] = (bytes_ge(R[i], thr[i]) ^ 0x01010101u) & cand[i];
+          const uint32_t x = R[i] ^ thr[i];
+          anytie |= (x - 0x01010101u) & ~x & 0x80808080u;  // nonzero iff some byte of x is zero
+        }
+        if (anytie) {
+          uint32_t tm = 0;
+#pragma unroll
+          for (int i = 0; i < 4; ++i) tm |= gather4(bytes_zero(R[i] ^ thr[i]) & cand[i]) << (4 * i);
+          uint32_t accm = 0;
+#pragma unroll 1
+          for (int d = 1; d < 4 && tm; ++d) {
+            const uint4 bd = philox_ks(
+                make_uint4(gid, key.sweep, (kTagIsingAccept << 24) | ((uint32_t)C << 8) | (uint32_t)d, key.replica),
+                key.ks);
+            uint32_t t = tm;
+            while (t) {
+              const int k = __ffs(t) - 1;
+              t &= t - 1;
+              const uint32_t sk = byte_at(S[0], S[1], S[2], S[3], k);
+              const uint32_t nk = byte_at(A[0], A[1], A[2], A[3], k);
+              const unsigned long long th = s_thr[sk * W + 2 * nk - tab.zeff + Z];
+              if (th >= (1ull << 32)) {  // always accepts
+                tm &= ~(1u << k);
+                accm |= 1u << k;
+                continue;
+              }
+              const uint32_t ub = byte_at(bd.x, bd.y, bd.z, bd.w, k);
+              const uint32_t tb = ((uint32_t)th >> (24 - 8 * d)) & 0xFFu;
+              if (ub != tb) {
+                tm &= ~(1u << k);
+                if (ub < tb) accm |= 1u << k;
+              }
+            }
+          }
+#pragma unroll
+          for (int i = 0; i < 4; ++i) F[i] |= spread4(accm >> (4 * i));
+        }
+      } else {
+        uint32_t cm = 0;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) cm |= gather4(cand[i]) << (4 * i);
+        unsigned long long t[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+          const uint32_t idx = ((S[k >> 2] * (uint32_t)W + M[k >> 2]) >> (8 * (k & 3))) & 0xFFu;
+          t[k] = s_thr[idx];
+        }
+        const uint32_t flip = decide16(t, cm, key, gid, C) & cm;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) F[i] = spread4(flip >> (4 * i));
+      }
     }
     uint32_t Sn[4];
 #pragma unroll
-    for (int i = 0; i < 4; ++i) Sn[i] = S[i] ^ spread4(flip >> (4 * i));
-    if (flip) *reinterpret_cast<uint4*>(own + rb + h0) = make_uint4(Sn[0], Sn[1], Sn[2], Sn[3]);
+    for (int i = 0; i < 4; ++i) Sn[i] = S[i] ^ F[i];
+    if ((F[0] | F[1] | F[2] | F[3]) != 0u)
+      *reinterpret_cast<uint4*>(own + rb + h0) = make_uint4(Sn[0], Sn[1], Sn[2], Sn[3]);
 
     if (MEASURE) {
-      int u = 0;
+      int u = 0, f = 0;
 #pragma unroll
-      for (int i = 0; i < 4; ++i) u += __popc(Sn[i]);
+      for (int i = 0; i < 4; ++i) {
+        u += __popc(Sn[i]);
+        f += __popc(F[i]);
+      }
       ups += u;
-      nacc += __popc(flip);
-      if (C == 1) {  // both neighbours' classes precede: every bond of class 1 is counted here
+      nacc += f;
+      if (C == 1) {  // every neighbour of class 1 has the lower colour: all bonds counted here
         unsigned sm = 0, m = 0;
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
@@ -188,10 +319,7 @@ __global__ void __launch_bounds__(256) ising_sc_kernel(const IsingScArgs a, cons
       }
     }
   }
-  if (MEASURE) {
-    long long v[kNumSums] = {bond, 0, 0, 0, 0, 0, ups, nacc};
-    block_sum_store(v, part + (long long)blockIdx.x * kNumSums);
-  }
+  if (MEASURE) block_sum3_store(bond, ups, nacc, part + (size_t)blockIdx.x * kNumSums);
 }
 
 // ------------------------------------------------------------- generic
@@ -284,13 +412,14 @@ static cudaError_t sc_dispatch(const IsingScArgs& a, const IsingTable& tab, RngK
 }
 
 cudaError_t launch_ising_sc(const IsingScArgs& a, const IsingTable& tab, RngKey key, int colour, int proposal,
-                            bool all_periodic, bool update, long long* part, int grid, int tpb, cudaStream_t s) {
+                            bool update, long long* part, int grid, int tpb, cudaStream_t s) {
+  const bool uniform = tab.zeff >= 0;
   if (colour == 0) {
-    return all_periodic ? sc_dispatch<0, true>(a, tab, key, proposal, update, part, grid, tpb, s)
-                        : sc_dispatch<0, false>(a, tab, key, proposal, update, part, grid, tpb, s);
+    return uniform ? sc_dispatch<0, true>(a, tab, key, proposal, update, part, grid, tpb, s)
+                   : sc_dispatch<0, false>(a, tab, key, proposal, update, part, grid, tpb, s);
   }
-  return all_periodic ? sc_dispatch<1, true>(a, tab, key, proposal, update, part, grid, tpb, s)
-                      : sc_dispatch<1, false>(a, tab, key, proposal, update, part, grid, tpb, s);
+  return uniform ? sc_dispatch<1, true>(a, tab, key, proposal, update, part, grid, tpb, s)
+                 : sc_dispatch<1, false>(a, tab, key, proposal, update, part, grid, tpb, s);
 }
 
 template <int ZT>
