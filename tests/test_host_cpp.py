@@ -1,0 +1,60 @@
+"""The C++ host mirror (Machine, programs, instruments, TOML input, CLI) over the C ABI."""
+import os
+import subprocess
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+BIN = os.path.join(REPO, "vegas-rs_gb300", "_build", "bin")
+
+
+def _bin(name):
+    path = os.path.join(BIN, name)
+    if not os.path.exists(path):
+        import build_ext
+
+        build_ext.build()
+    return path
+
+
+def test_host_selftest_cpu():
+    r = subprocess.run([_bin("host_selftest"), "--cpu"], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    assert "checks passed" in r.stdout
+
+
+def test_cli_prints_default_input_and_fails_loudly_without_args():
+    r = subprocess.run([_bin("vegas_gpu_cli"), "input"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and "[[stages]]" in r.stdout and 'program = "CoolDown"' in r.stdout
+    r = subprocess.run([_bin("vegas_gpu_cli"), "run", "/nonexistent.toml"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1 and r.stderr.startswith("Error:")
+
+
+@pytest.mark.gpu
+def test_host_selftest_gpu(tmp_path):
+    r = subprocess.run([_bin("host_selftest"), "--gpu"], capture_output=True, text=True, timeout=600, cwd=tmp_path)
+    assert r.returncode == 0, r.stdout + r.stderr
+
+
+@pytest.mark.gpu
+def test_cli_run_and_bench(tmp_path):
+    toml = tmp_path / "in.toml"
+    toml.write_text(
+        'model = "Ising"\nalgorithm = "Metropolis"\n[sample.unitcell]\nname = "sc"\n'
+        "[sample.size]\nx = 32\ny = 32\nz = 1\n[sample.pbc]\nx = true\ny = true\nz = false\n"
+        '[[stages]]\nprogram = "Relax"\nsteps = 100\ntemperature = 4.0\n'
+        '[[stages]]\nprogram = "CoolDown"\nmax_temperature = 4.0\nmin_temperature = 0.1\ncool_rate = 0.1\n'
+        "relax = 20\nsteps = 100\n"
+        f'[output]\nobservables = "{tmp_path}/obs.csv"\n')
+    r = subprocess.run([_bin("vegas_gpu_cli"), "run", str(toml), "-s", "1"], capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stderr
+    lines = r.stdout.strip().splitlines()
+    assert len(lines) == 39  # CoolDown(4.0, 0.1, 0.1) visits 39 temperatures
+    cols = [list(map(float, ln.split())) for ln in lines]
+    assert all(len(c) == 7 for c in cols)
+    # energy per spin at the lowest temperature is near the ground state -2 (bond) x 2 (Compound total)
+    assert cols[-1][2] / 1024 < -3.9
+    assert (tmp_path / "obs.csv").exists() and not (tmp_path / "obs.csv.tmp").exists()
+    r = subprocess.run([_bin("vegas_gpu_cli"), "bench", "potts", "8"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1 and "unknown model" in r.stderr

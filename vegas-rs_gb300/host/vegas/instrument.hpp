@@ -1,0 +1,189 @@
+// instrument.hpp -- instruments hooked into the machine (src/instrument.rs).
+//
+// The hooks are the reference's (on_relax_start/end, on_measure_start/end,
+// after_step).  after_step receives a StepView: the sweep's total energy and
+// |M| computed on the device with the Hamiltonian's total-energy semantics
+// (what the reference's instruments compute from the state themselves,
+// src/instrument.rs:133-141, :254-262) and a callback that copies the state
+// back when an instrument needs the spins (StateSensor).
+//
+// Output files: the reference writes parquet (src/output.rs); this host writes
+// the same columns as CSV, through a ".tmp" file renamed on close as the
+// reference does (src/output.rs:101-112, :189-200).
+#pragma once
+
+#include <cstdio>
+#include <functional>
+#include <memory>
+#include <string>
+
+#include "accumulator.hpp"
+#include "error.hpp"
+#include "state.hpp"
+#include "thermostat.hpp"
+
+namespace vegas {
+
+template <typename S>
+struct StepView {
+  double energy;
+  double magnetization;
+  size_t n;
+  std::function<State<S>()> state;  // device -> host copy on demand
+};
+
+template <typename S>
+class Instrument {
+ public:
+  virtual ~Instrument() = default;
+  virtual void on_relax_start(const Thermostat<S>&, size_t /*n*/) {}
+  virtual void on_relax_end() {}
+  virtual void on_measure_start(const Thermostat<S>&, size_t /*n*/) {}
+  virtual void on_measure_end() {}
+  virtual void after_step(const StepView<S>&) {}
+  // True if after_step needs E / |M| for this sweep (lets the machine skip
+  // the per-sweep reduction when no instrument listens).
+  virtual bool wants_observables() const { return false; }
+  // Sweeps (within the current relax/measure run) at which the state is read.
+  virtual size_t state_frequency() const { return 0; }
+};
+
+// StatSensor (src/instrument.rs:98-141): one line per measure run with
+// T |B| <E> Var(E)/(N T^2) <|M|> Var(|M|)/(N T) U4, 16 decimals.
+template <typename S>
+class StatSensor : public Instrument<S> {
+ public:
+  explicit StatSensor(FILE* out) : out_(out) {}
+  void on_measure_start(const Thermostat<S>& t, size_t n) override {
+    thermostat_ = std::make_unique<Thermostat<S>>(t);
+    n_ = n;
+  }
+  void on_measure_end() override {
+    if (thermostat_) {
+      const double T = thermostat_->temperature();
+      std::fprintf(out_, "%.16f %.16f %.16f %.16f %.16f %.16f %.16f\n", T, thermostat_->field().magnitude(),
+                   energy_.mean(), energy_.variance() / ((double)n_ * T * T), magnetization_.mean(),
+                   magnetization_.variance() / ((double)n_ * T), magnetization_.binder_cumulant());
+      std::fflush(out_);
+    }
+    thermostat_.reset();
+    n_ = 0;
+    energy_ = Accumulator();
+    magnetization_ = Accumulator();
+  }
+  void after_step(const StepView<S>& v) override {
+    if (!thermostat_) return;
+    energy_.collect(v.energy);
+    magnetization_.collect(v.magnetization);
+  }
+  bool wants_observables() const override { return thermostat_ != nullptr; }
+
+ private:
+  FILE* out_;
+  std::unique_ptr<Thermostat<S>> thermostat_;
+  size_t n_ = 0;
+  Accumulator energy_, magnetization_;
+};
+
+// Atomic CSV file: writes path + ".tmp", renames to path on close.
+class CsvOutput {
+ public:
+  CsvOutput(const std::string& path, const char* header) : path_(path), tmp_(path + ".tmp") {
+    f_ = std::fopen(tmp_.c_str(), "w");
+    if (!f_) throw IoError("std io error: cannot create " + tmp_);
+    std::fprintf(f_, "%s\n", header);
+  }
+  ~CsvOutput() { close(); }
+  FILE* file() { return f_; }
+  void close() {
+    if (!f_) return;
+    std::fclose(f_);
+    f_ = nullptr;
+    if (std::rename(tmp_.c_str(), path_.c_str()) != 0) std::fprintf(stderr, "Failed to rename %s\n", tmp_.c_str());
+  }
+
+ private:
+  std::string path_, tmp_;
+  FILE* f_ = nullptr;
+};
+
+// ObservableSensor (src/instrument.rs:144-263): per-sweep rows during relax
+// and measure runs; schema of src/output.rs:37-46.
+template <typename S>
+class ObservableSensor : public Instrument<S> {
+ public:
+  explicit ObservableSensor(const std::string& path)
+      : io_(path, "relax,stage,step,n,temperature,field,energy,magnetization") {}
+  void on_relax_start(const Thermostat<S>& t, size_t n) override { start(t, n, true); }
+  void on_relax_end() override { finish(); }
+  void on_measure_start(const Thermostat<S>& t, size_t n) override { start(t, n, false); }
+  void on_measure_end() override { finish(); }
+  void after_step(const StepView<S>& v) override {
+    if (!thermostat_) return;
+    std::fprintf(io_.file(), "%s,%zu,%zu,%zu,%.17g,%.17g,%.17g,%.17g\n", relax_ ? "true" : "false", stage_, step_++,
+                 n_, thermostat_->temperature(), thermostat_->field().magnitude(), v.energy, v.magnetization);
+  }
+  bool wants_observables() const override { return thermostat_ != nullptr; }
+
+ private:
+  void start(const Thermostat<S>& t, size_t n, bool relax) {
+    thermostat_ = std::make_unique<Thermostat<S>>(t);
+    n_ = n;
+    relax_ = relax;
+    step_ = 0;
+  }
+  void finish() {
+    ++stage_;
+    thermostat_.reset();
+  }
+  CsvOutput io_;
+  std::unique_ptr<Thermostat<S>> thermostat_;
+  size_t n_ = 0, stage_ = 0, step_ = 0;
+  bool relax_ = false;
+};
+
+// StateSensor (src/instrument.rs:265-351): the whole state every `frequency`
+// sweeps; schema of src/output.rs:126-136.
+template <typename S>
+class StateSensor : public Instrument<S> {
+ public:
+  StateSensor(const std::string& path, size_t frequency)
+      : io_(path, "relax,stage,step,temperature,field,id,sx,sy,sz"), frequency_(frequency ? frequency : 1) {}
+  void on_relax_start(const Thermostat<S>& t, size_t) override {
+    relax_ = 1;
+    thermostat_ = std::make_unique<Thermostat<S>>(t);
+  }
+  void on_relax_end() override { end(); }
+  void on_measure_start(const Thermostat<S>& t, size_t) override {
+    relax_ = 0;
+    thermostat_ = std::make_unique<Thermostat<S>>(t);
+  }
+  void on_measure_end() override { end(); }
+  void after_step(const StepView<S>& v) override {
+    if (step_ % frequency_ == 0 && relax_ >= 0 && thermostat_) {
+      const State<S> st = v.state();
+      for (size_t i = 0; i < st.len(); ++i) {
+        const S& s = st.at(i);
+        std::fprintf(io_.file(), "%s,%zu,%zu,%.17g,%.17g,%zu,%.17g,%.17g,%.17g\n", relax_ ? "true" : "false", stage_,
+                     step_, thermostat_->temperature(), thermostat_->field().magnitude(), i, s.sx(), s.sy(), s.sz());
+      }
+    }
+    ++step_;
+  }
+  size_t state_frequency() const override { return frequency_; }
+
+ private:
+  void end() {
+    relax_ = -1;
+    step_ = 0;
+    ++stage_;
+    thermostat_.reset();
+  }
+  CsvOutput io_;
+  size_t frequency_;
+  int relax_ = -1;
+  size_t step_ = 0, stage_ = 0;
+  std::unique_ptr<Thermostat<S>> thermostat_;
+};
+
+}  // namespace vegas
