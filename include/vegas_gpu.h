@@ -180,6 +180,29 @@ int vg_magnetization(vg_ctx* ctx, double m[3], double* magnitude);
 /* Total energy / |M| from raw sums with a context's Hamiltonian semantics. */
 int vg_energy_from_sums(const vg_ctx* ctx, const vg_sums* sums, double* energy, double* magnitude);
 
+/* ------------------------------------------------------ no-alloc sweeps */
+/* No counterpart in the reference.  n Ising flip-proposal sweeps of an sc
+ * lattice (x a multiple of 32, even extents on periodic axes) that allocate
+ * no memory, for callers that cannot call cudaMalloc: plugins whose host
+ * framework owns all device memory through its own pool, code enqueueing
+ * work while another party captures the stream into a CUDA graph, real-time
+ * loops where an allocation could synchronise the device.  The caller owns
+ * every buffer: class0 / class1 are the two checkerboard classes on the
+ * device (uint8 0 = Down / 1 = Up, sites with (x+y+z)&1 == c, row-major
+ * [z][y][x/2]) and sums_out (may be NULL) receives n_sweeps vg_sums rows
+ * (field along +z).  zeeman is the per-site Zeeman coefficient (sign * |B| *
+ * orientation).  Work is enqueued on cuda_stream (NULL = default stream);
+ * results are valid once that stream has been synchronised.  Draws and
+ * results equal vg_sweeps on a context with the same seed and replica at
+ * sweep index sweep0.  The per-block partial sums live in a 2 MiB array
+ * inside the library (at most 2048 thread blocks per colour pass; larger
+ * launches are rejected with VG_ERR_UNSUPPORTED); every call shares it, so
+ * calls that overlap on the GPU race.  The first call on a device looks up
+ * the array's address: make it before any stream capture. */
+int vg_ising_sc_sweeps_noalloc(const vg_lattice_desc* lattice, double exchange, double zeeman, double temperature,
+                               uint64_t seed, uint32_t replica, uint64_t sweep0, uint64_t n_sweeps,
+                               uint8_t* class0, uint8_t* class1, double* sums_out, void* cuda_stream);
+
 /* ------------------------------------------------------- host utilities */
 /* Neighbour table of a lattice (nbr[i*zmax + k], -1 = absent) and its greedy
  * colouring; pass NULL buffers to query n and zmax. */

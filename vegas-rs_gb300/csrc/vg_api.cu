@@ -1325,6 +1325,9 @@ int vg_host_alloc(void** p, uint64_t bytes) {
   return VG_OK;
 }
 
+// Lets other translation units record the thread's last error message.
+void vg_internal_set_last_error(const char* msg) { g_err = msg ? msg : ""; }
+
 int vg_host_free(void* p) {
   if (!p) return VG_OK;
   cudaError_t e = cudaFreeHost(p);
