@@ -938,6 +938,12 @@ int vg_ctx_create_ex(const vg_lattice_desc* lat, const vg_hamiltonian_desc* ham,
     items = std::max(items, is_ising(c) ? (nc + 15) / 16 : nc);
   }
   c->grid = launch_grid(c, items);
+  if (is_ising(c) && c->path == VG_PATH_STRUCTURED && opt->blocks_per_sm <= 0) {
+    // one wave of resident blocks, each thread walking several 16-site groups
+    const bool uniform = ising_table(c).zeff >= 0;
+    const long long cap = (long long)c->sm_count * ising_sc_blocks_per_sm(uniform, c->tpb);
+    c->grid = (int)std::max(1LL, std::min((items + c->tpb - 1) / c->tpb, cap));
+  }
   if ((rc = dalloc(c, (void**)&c->d_flag, sizeof(int)))) {
     destroy(c);
     return rc;

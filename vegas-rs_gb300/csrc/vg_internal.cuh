@@ -160,6 +160,7 @@ struct HeisParams {
 // Heisenberg).  update = false only measures.
 cudaError_t launch_ising_sc(const IsingScArgs& a, const IsingTable& tab, RngKey key, int colour,
                             int proposal, bool update, long long* part, int grid, int tpb, cudaStream_t s);
+int ising_sc_blocks_per_sm(bool uniform, int tpb);
 cudaError_t launch_ising_gen(const IsingGenArgs& a, const IsingTable& tab, RngKey key, int colour,
                              int proposal, bool update, long long* part, int grid, int tpb,
                              cudaStream_t s);

@@ -17,6 +17,8 @@
 //    adds its six neighbour vectors with plain 32-bit adds (bytes <= 6).
 //  * ising_gen_kernel: any lattice via an ELL neighbour table per colour
 //    class of a greedy colouring (natural-order spins).
+#include <utility>
+
 #include "vg_internal.cuh"
 
 namespace vg {
@@ -134,191 +136,248 @@ __device__ __forceinline__ void block_sum3_store(int a, int b, int c, long long*
   }
 }
 
+// Programmatic dependent launch: let the next colour pass launch while this
+// one drains, and make every pass wait for its predecessor's writes before
+// touching spins.  Both are no-ops for kernels launched without the PDL
+// attribute.
+__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+// Resolution of ties deferred to whole warps: a queued site (group gid,
+// site k, spin s, up-neighbour count nu) tied with its threshold on digit 0;
+// digits 1..3 decide it exactly as the in-line rule would.  Returns whether
+// the move is accepted.
+__device__ __forceinline__ bool resolve_tie(uint32_t gid, int k, uint32_t s01, uint32_t nu, int zeff, int colour,
+                                            const unsigned long long* s_thr, const RngKey& key) {
+  constexpr int Z = 6, W = 2 * Z + 1;
+  const unsigned long long th = s_thr[s01 * W + 2 * nu - zeff + Z];
+  if (th >= (1ull << 32)) return true;
+  for (int d = 1; d < 4; ++d) {
+    const uint4 bd = philox_ks(
+        make_uint4(gid, key.sweep, (kTagIsingAccept << 24) | ((uint32_t)colour << 8) | (uint32_t)d, key.replica),
+        key.ks);
+    const uint32_t ub = byte_at(bd.x, bd.y, bd.z, bd.w, k);
+    const uint32_t tb = ((uint32_t)th >> (24 - 8 * d)) & 0xFFu;
+    if (ub != tb) return ub < tb;
+  }
+  return false;  // U == thr: not below the threshold
+}
+
 // UNIFORM: every site has the same number zeff of existing neighbours (each
 // axis periodic, or open with extent 1), so the up-neighbour count n_up in
 // [0, zeff] indexes 8-entry byte tables and four sites are decided per
-// word: the top threshold byte and the always-accept flag come from PRMT
-// lookups, the first random digit is compared byte-parallel, and only sites
-// whose digit ties with the threshold digit (probability 1/256) continue
-// digit by digit.  Otherwise the scalar decide16 path runs.  Both give the
-// same decisions as "accept iff U < thr".
+// word: the threshold's top byte comes from a PRMT lookup (0xFF for moves
+// that always accept), the first random digit is compared byte-parallel, and
+// sites whose digit ties with the threshold digit (probability 1/256) are
+// queued per warp and resolved 32 at a time.  Otherwise the scalar
+// decide16 path runs in line.  Both give the decisions of "accept iff U < thr".
 template <int C, bool UNIFORM, bool MEASURE, bool UPDATE, int PROP>
 __global__ void __launch_bounds__(256, UNIFORM ? 4 : 2) ising_sc_kernel(const IsingScArgs a, const IsingTable tab, const RngKey key,
                                                           long long* __restrict__ part) {
   constexpr int Z = 6, W = 2 * Z + 1;
+  constexpr int kQ = 64;  // per-warp tie queue
   __shared__ unsigned long long s_thr[2 * W];
+  __shared__ uint2 s_q[8][kQ];
+  pdl_launch_dependents();
   for (int i = threadIdx.x; i < 2 * W; i += blockDim.x) s_thr[i] = tab.thr[i];
   __syncthreads();
+  pdl_wait();
 
   uint8_t* __restrict__ own = a.cls[C];
   const uint8_t* __restrict__ oth = a.cls[C ^ 1];
   const int zoff = Z - tab.zeff;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int bond = 0, ups = 0, nacc = 0;
+  int qn = 0;  // warp-uniform queue length
+
+  // apply the first n queued ties (one per lane), then drop them
+  auto drain = [&](int n) {
+    __syncwarp();
+    if (lane < n) {
+      const uint2 e = s_q[warp][lane];
+      const int k = (int)(e.y & 15u);
+      const uint32_t s01 = (e.y >> 4) & 1u, nu = e.y >> 5;
+      if (resolve_tie(e.x, k, s01, nu, tab.zeff, C, s_thr, key)) {
+        own[(size_t)e.x * 16 + k] = (uint8_t)(s01 ^ 1u);
+        ups += 1 - 2 * (int)s01;
+        nacc += 1;
+        if (C == 1) bond -= 2 * (2 * (int)s01 - 1) * (2 * (int)nu - tab.zeff);
+      }
+    }
+    __syncwarp();
+    const int rest = qn - n;
+    uint2 mv = make_uint2(0, 0);
+    if (lane < rest) mv = s_q[warp][n + lane];
+    __syncwarp();
+    if (lane < rest) s_q[warp][lane] = mv;
+    __syncwarp();
+    qn = rest;
+  };
+
   const uint32_t stride = gridDim.x * blockDim.x;
-  for (uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x; gid < a.groups; gid += stride) {
-    const int row = (int)fdiv(gid, a.fG);
-    const int h0 = (int)(gid - (uint32_t)row * a.G) << 4;
-    const int z = (int)fdiv((uint32_t)row, a.fLy);
-    const int y = row - z * a.Ly;
-    const int p = (y + z + C) & 1;  // x parity of this row's class-C sites
-    const int rb = row * a.Hx;
+  for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < a.groups; base += stride) {
+    const uint32_t gid = base + lane;
+    const bool active = gid < a.groups;
+    uint32_t tm = 0;  // sites of this group whose first digit tied
+    uint32_t S[4] = {0, 0, 0, 0}, A[4] = {0, 0, 0, 0};
+    if (active) {
+      const int row = (int)fdiv(gid, a.fG);
+      const int h0 = (int)(gid - (uint32_t)row * a.G) << 4;
+      const int z = (int)fdiv((uint32_t)row, a.fLy);
+      const int y = row - z * a.Ly;
+      const int p = (y + z + C) & 1;  // x parity of this row's class-C sites
+      const int rb = row * a.Hx;
 
-    const uint4 Sv = *reinterpret_cast<const uint4*>(own + rb + h0);
-    const uint4 X0 = __ldg(reinterpret_cast<const uint4*>(oth + rb + h0));
-    // x-neighbour not shared with X0: h0-1 (p = 0) or h0+16 (p = 1)
-    uint32_t e = 0;
-    bool xmiss = false;
-    if (p == 0) {
-      if (h0 > 0) e = __ldg(oth + rb + h0 - 1);
-      else if (a.pbx) e = __ldg(oth + rb + a.Hx - 1);
-      else xmiss = true;
-    } else {
-      if (h0 + 16 < a.Hx) e = __ldg(oth + rb + h0 + 16);
-      else if (a.pbx) e = __ldg(oth + rb);
-      else xmiss = true;
-    }
-    uint32_t X1[4];
-    if (p == 0) {
-      X1[0] = __byte_perm(e << 24, X0.x, 0x6543);
-      X1[1] = __byte_perm(X0.x, X0.y, 0x6543);
-      X1[2] = __byte_perm(X0.y, X0.z, 0x6543);
-      X1[3] = __byte_perm(X0.z, X0.w, 0x6543);
-    } else {
-      X1[0] = __byte_perm(X0.x, X0.y, 0x4321);
-      X1[1] = __byte_perm(X0.y, X0.z, 0x4321);
-      X1[2] = __byte_perm(X0.z, X0.w, 0x4321);
-      X1[3] = __byte_perm(X0.w, e, 0x4321);
-    }
-    const int rym = y > 0 ? row - 1 : (a.pby ? row + a.Ly - 1 : -1);
-    const int ryp = y < a.Ly - 1 ? row + 1 : (a.pby ? row - (a.Ly - 1) : -1);
-    const int rzm = z > 0 ? row - a.Ly : (a.pbz ? row + (a.Lz - 1) * a.Ly : -1);
-    const int rzp = z < a.Lz - 1 ? row + a.Ly : (a.pbz ? row - (a.Lz - 1) * a.Ly : -1);
-    const uint4 zero4 = make_uint4(0, 0, 0, 0);
-    const uint4 Ym = rym >= 0 ? __ldg(reinterpret_cast<const uint4*>(oth + (size_t)rym * a.Hx + h0)) : zero4;
-    const uint4 Yp = ryp >= 0 ? __ldg(reinterpret_cast<const uint4*>(oth + (size_t)ryp * a.Hx + h0)) : zero4;
-    const uint4 Zm = rzm >= 0 ? __ldg(reinterpret_cast<const uint4*>(oth + (size_t)rzm * a.Hx + h0)) : zero4;
-    const uint4 Zp = rzp >= 0 ? __ldg(reinterpret_cast<const uint4*>(oth + (size_t)rzp * a.Hx + h0)) : zero4;
-
-    const uint32_t S[4] = {Sv.x, Sv.y, Sv.z, Sv.w};
-    const uint32_t A[4] = {X0.x + X1[0] + Ym.x + Yp.x + Zm.x + Zp.x, X0.y + X1[1] + Ym.y + Yp.y + Zm.y + Zp.y,
-                           X0.z + X1[2] + Ym.z + Yp.z + Zm.z + Zp.z, X0.w + X1[3] + Ym.w + Yp.w + Zm.w + Zp.w};
-    // M = 2A + (Z - Zc) per byte, where Zc counts existing neighbours; the
-    // neighbour sum of site k is M_k - Z.
-    uint32_t M[4];
-    if (UNIFORM) {
-#pragma unroll
-      for (int i = 0; i < 4; ++i) M[i] = 2u * A[i] + (uint32_t)zoff * 0x01010101u;
-    } else {
-      const uint32_t zmiss = (uint32_t)((rym < 0) + (ryp < 0) + (rzm < 0) + (rzp < 0));
-#pragma unroll
-      for (int i = 0; i < 4; ++i) M[i] = 2u * A[i] + zmiss * 0x01010101u;
-      if (xmiss) {
-        if (p == 0) M[0] += 1u;
-        else M[3] += 1u << 24;
-      }
-    }
-
-    uint32_t F[4] = {0, 0, 0, 0};  // 0x01 bytes: sites that flip
-    if (UPDATE) {
-      uint32_t cand[4] = {0x01010101u, 0x01010101u, 0x01010101u, 0x01010101u};
-      if (PROP == VG_PROPOSE_RANDOM) {
-        const uint4 b = philox_ks(make_uint4(gid, key.sweep, (kTagIsingPropose << 24) | ((uint32_t)C << 8), key.replica),
-                                  key.ks);
-        const uint32_t w[4] = {b.x, b.y, b.z, b.w};
-#pragma unroll
-        for (int i = 0; i < 4; ++i) cand[i] = ((~w[i] >> 7) & 0x01010101u) ^ S[i];
-      }
-      if (UNIFORM) {
-        // first digit of every site's uniform against its threshold's top byte
-        // (0xFF for always-accept moves, whose ties resolve to accept below)
-        const uint4 b = philox_ks(make_uint4(gid, key.sweep, (kTagIsingAccept << 24) | ((uint32_t)C << 8), key.replica),
-                                  key.ks);
-        const uint32_t R[4] = {b.x, b.y, b.z, b.w};
-        uint32_t thr[4], anytie = 0;
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          const uint32_t sel = nibble_selector(A[i]);
-          const uint32_t sm = S[i] * 0xFFu;
-          thr[i] = (__byte_perm(tab.top[1][0], tab.top[1][1], sel) & sm) |
-                   (__byte_perm(tab.top[0][0], tab.top[0][1], sel) & ~sm);
-          F[i] = (bytes_ge(R[i], thr[i]) ^ 0x01010101u) & cand[i];
-          const uint32_t x = R[i] ^ thr[i];
-          anytie |= (x - 0x01010101u) & ~x & 0x80808080u;  // nonzero iff some byte of x is zero
-        }
-        if (anytie) {
-          uint32_t tm = 0;
-#pragma unroll
-          for (int i = 0; i < 4; ++i) tm |= gather4(bytes_zero(R[i] ^ thr[i]) & cand[i]) << (4 * i);
-          uint32_t accm = 0;
-#pragma unroll 1
-          for (int d = 1; d < 4 && tm; ++d) {
-            const uint4 bd = philox_ks(
-                make_uint4(gid, key.sweep, (kTagIsingAccept << 24) | ((uint32_t)C << 8) | (uint32_t)d, key.replica),
-                key.ks);
-            uint32_t t = tm;
-            while (t) {
-              const int k = __ffs(t) - 1;
-              t &= t - 1;
-              const uint32_t sk = byte_at(S[0], S[1], S[2], S[3], k);
-              const uint32_t nk = byte_at(A[0], A[1], A[2], A[3], k);
-              const unsigned long long th = s_thr[sk * W + 2 * nk - tab.zeff + Z];
-              if (th >= (1ull << 32)) {  // always accepts
-                tm &= ~(1u << k);
-                accm |= 1u << k;
-                continue;
-              }
-              const uint32_t ub = byte_at(bd.x, bd.y, bd.z, bd.w, k);
-              const uint32_t tb = ((uint32_t)th >> (24 - 8 * d)) & 0xFFu;
-              if (ub != tb) {
-                tm &= ~(1u << k);
-                if (ub < tb) accm |= 1u << k;
-              }
-            }
-          }
-#pragma unroll
-          for (int i = 0; i < 4; ++i) F[i] |= spread4(accm >> (4 * i));
-        }
+      const uint4 Sv = *reinterpret_cast<const uint4*>(own + rb + h0);
+      const uint4 X0 = __ldg(reinterpret_cast<const uint4*>(oth + rb + h0));
+      // x-neighbour not shared with X0: h0-1 (p = 0) or h0+16 (p = 1)
+      uint32_t e = 0;
+      bool xmiss = false;
+      if (p == 0) {
+        if (h0 > 0) e = __ldg(oth + rb + h0 - 1);
+        else if (a.pbx) e = __ldg(oth + rb + a.Hx - 1);
+        else xmiss = true;
       } else {
-        uint32_t cm = 0;
-#pragma unroll
-        for (int i = 0; i < 4; ++i) cm |= gather4(cand[i]) << (4 * i);
-        unsigned long long t[16];
-#pragma unroll
-        for (int k = 0; k < 16; ++k) {
-          const uint32_t idx = ((S[k >> 2] * (uint32_t)W + M[k >> 2]) >> (8 * (k & 3))) & 0xFFu;
-          t[k] = s_thr[idx];
-        }
-        const uint32_t flip = decide16(t, cm, key, gid, C) & cm;
-#pragma unroll
-        for (int i = 0; i < 4; ++i) F[i] = spread4(flip >> (4 * i));
+        if (h0 + 16 < a.Hx) e = __ldg(oth + rb + h0 + 16);
+        else if (a.pbx) e = __ldg(oth + rb);
+        else xmiss = true;
       }
-    }
-    uint32_t Sn[4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) Sn[i] = S[i] ^ F[i];
-    if ((F[0] | F[1] | F[2] | F[3]) != 0u)
-      *reinterpret_cast<uint4*>(own + rb + h0) = make_uint4(Sn[0], Sn[1], Sn[2], Sn[3]);
+      uint32_t X1[4];
+      if (p == 0) {
+        X1[0] = __byte_perm(e << 24, X0.x, 0x6543);
+        X1[1] = __byte_perm(X0.x, X0.y, 0x6543);
+        X1[2] = __byte_perm(X0.y, X0.z, 0x6543);
+        X1[3] = __byte_perm(X0.z, X0.w, 0x6543);
+      } else {
+        X1[0] = __byte_perm(X0.x, X0.y, 0x4321);
+        X1[1] = __byte_perm(X0.y, X0.z, 0x4321);
+        X1[2] = __byte_perm(X0.z, X0.w, 0x4321);
+        X1[3] = __byte_perm(X0.w, e, 0x4321);
+      }
+      const int rym = y > 0 ? row - 1 : (a.pby ? row + a.Ly - 1 : -1);
+      const int ryp = y < a.Ly - 1 ? row + 1 : (a.pby ? row - (a.Ly - 1) : -1);
+      const int rzm = z > 0 ? row - a.Ly : (a.pbz ? row + (a.Lz - 1) * a.Ly : -1);
+      const int rzp = z < a.Lz - 1 ? row + a.Ly : (a.pbz ? row - (a.Lz - 1) * a.Ly : -1);
+      const uint4 zero4 = make_uint4(0, 0, 0, 0);
+      const uint4 Ym = rym >= 0 ? __ldg(reinterpret_cast<const uint4*>(oth + (size_t)rym * a.Hx + h0)) : zero4;
+      const uint4 Yp = ryp >= 0 ? __ldg(reinterpret_cast<const uint4*>(oth + (size_t)ryp * a.Hx + h0)) : zero4;
+      const uint4 Zm = rzm >= 0 ? __ldg(reinterpret_cast<const uint4*>(oth + (size_t)rzm * a.Hx + h0)) : zero4;
+      const uint4 Zp = rzp >= 0 ? __ldg(reinterpret_cast<const uint4*>(oth + (size_t)rzp * a.Hx + h0)) : zero4;
 
-    if (MEASURE) {
-      int u = 0, f = 0;
+      S[0] = Sv.x;
+      S[1] = Sv.y;
+      S[2] = Sv.z;
+      S[3] = Sv.w;
+      A[0] = X0.x + X1[0] + Ym.x + Yp.x + Zm.x + Zp.x;
+      A[1] = X0.y + X1[1] + Ym.y + Yp.y + Zm.y + Zp.y;
+      A[2] = X0.z + X1[2] + Ym.z + Yp.z + Zm.z + Zp.z;
+      A[3] = X0.w + X1[3] + Ym.w + Yp.w + Zm.w + Zp.w;
+      // M = 2A + (Z - Zc) per byte, where Zc counts existing neighbours; the
+      // neighbour sum of site k is M_k - Z.
+      uint32_t M[4];
+      if (UNIFORM) {
 #pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        u += __popc(Sn[i]);
-        f += __popc(F[i]);
+        for (int i = 0; i < 4; ++i) M[i] = 2u * A[i] + (uint32_t)zoff * 0x01010101u;
+      } else {
+        const uint32_t zmiss = (uint32_t)((rym < 0) + (ryp < 0) + (rzm < 0) + (rzp < 0));
+#pragma unroll
+        for (int i = 0; i < 4; ++i) M[i] = 2u * A[i] + zmiss * 0x01010101u;
+        if (xmiss) {
+          if (p == 0) M[0] += 1u;
+          else M[3] += 1u << 24;
+        }
       }
-      ups += u;
-      nacc += f;
-      if (C == 1) {  // every neighbour of class 1 has the lower colour: all bonds counted here
-        unsigned sm = 0, m = 0;
+
+      uint32_t F[4] = {0, 0, 0, 0};  // 0x01 bytes: sites that flip
+      if (UPDATE) {
+        uint32_t cand[4] = {0x01010101u, 0x01010101u, 0x01010101u, 0x01010101u};
+        if (PROP == VG_PROPOSE_RANDOM) {
+          const uint4 b = philox_ks(make_uint4(gid, key.sweep, (kTagIsingPropose << 24) | ((uint32_t)C << 8), key.replica),
+                                    key.ks);
+          const uint32_t w[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+          for (int i = 0; i < 4; ++i) cand[i] = ((~w[i] >> 7) & 0x01010101u) ^ S[i];
+        }
+        if (UNIFORM) {
+          const uint4 b = philox_ks(make_uint4(gid, key.sweep, (kTagIsingAccept << 24) | ((uint32_t)C << 8), key.replica),
+                                    key.ks);
+          const uint32_t R[4] = {b.x, b.y, b.z, b.w};
+          uint32_t thr[4], anytie = 0;
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            const uint32_t sel = nibble_selector(A[i]);
+            const uint32_t sm = S[i] * 0xFFu;
+            thr[i] = (__byte_perm(tab.top[1][0], tab.top[1][1], sel) & sm) |
+                     (__byte_perm(tab.top[0][0], tab.top[0][1], sel) & ~sm);
+            F[i] = (bytes_ge(R[i], thr[i]) ^ 0x01010101u) & cand[i];
+            const uint32_t x = R[i] ^ thr[i];
+            anytie |= (x - 0x01010101u) & ~x & 0x80808080u;  // nonzero iff some byte of x is zero
+          }
+          if (anytie) {
+#pragma unroll
+            for (int i = 0; i < 4; ++i) tm |= gather4(bytes_zero(R[i] ^ thr[i]) & cand[i]) << (4 * i);
+          }
+        } else {
+          uint32_t cm = 0;
+#pragma unroll
+          for (int i = 0; i < 4; ++i) cm |= gather4(cand[i]) << (4 * i);
+          unsigned long long t[16];
+#pragma unroll
+          for (int k = 0; k < 16; ++k) {
+            const uint32_t idx = ((S[k >> 2] * (uint32_t)W + M[k >> 2]) >> (8 * (k & 3))) & 0xFFu;
+            t[k] = s_thr[idx];
+          }
+          const uint32_t flip = decide16(t, cm, key, gid, C) & cm;
+#pragma unroll
+          for (int i = 0; i < 4; ++i) F[i] = spread4(flip >> (4 * i));
+        }
+      }
+      uint32_t Sn[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) Sn[i] = S[i] ^ F[i];
+      if ((F[0] | F[1] | F[2] | F[3]) != 0u)
+        *reinterpret_cast<uint4*>(own + rb + h0) = make_uint4(Sn[0], Sn[1], Sn[2], Sn[3]);
+
+      if (MEASURE) {
+        int u = 0, f = 0;
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-          sm = __dp4a(Sn[i], M[i], sm);
-          m = __dp4a(M[i], 0x01010101u, m);
+          u += __popc(Sn[i]);
+          f += __popc(F[i]);
         }
-        bond += 2 * (int)sm - (int)m - Z * (2 * u - 16);
+        ups += u;
+        nacc += f;
+        if (C == 1) {  // every neighbour of class 1 has the lower colour: all bonds counted here
+          unsigned sm = 0, m = 0;
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            sm = __dp4a(Sn[i], M[i], sm);
+            m = __dp4a(M[i], 0x01010101u, m);
+          }
+          bond += 2 * (int)sm - (int)m - Z * (2 * u - 16);
+        }
+      }
+    }
+    if (UNIFORM && UPDATE) {
+      // queue this iteration's ties, one site per lane per round
+      unsigned lanes = __ballot_sync(0xffffffffu, tm != 0u);
+      while (lanes) {
+        if (qn + 32 > kQ) drain(32 < qn ? 32 : qn);
+        const int pos = qn + __popc(lanes & ((1u << lane) - 1u));
+        if (tm) {
+          const int k = __ffs(tm) - 1;
+          tm &= tm - 1u;
+          const uint32_t sk = byte_at(S[0], S[1], S[2], S[3], k);
+          const uint32_t nk = byte_at(A[0], A[1], A[2], A[3], k);
+          s_q[warp][pos] = make_uint2(gid, (uint32_t)k | (sk << 4) | (nk << 5));
+        }
+        qn += __popc(lanes);
+        if (qn >= 32) drain(32);
+        lanes = __ballot_sync(0xffffffffu, tm != 0u);
       }
     }
   }
+  if (UNIFORM && UPDATE && qn > 0) drain(qn);
   if (MEASURE) block_sum3_store(bond, ups, nacc, part + (size_t)blockIdx.x * kNumSums);
 }
 
@@ -395,20 +454,43 @@ __global__ void __launch_bounds__(256) ising_gen_kernel(const IsingGenArgs a, co
 }
 
 // ------------------------------------------------------------ dispatch
-template <int C, bool ALLPER>
+// Launch with programmatic stream serialization: the kernel may start while
+// its predecessor on the stream drains and waits (griddepcontrol.wait) for
+// that predecessor's completion before reading spins.
+template <typename... P, typename... A>
+static cudaError_t launch_pdl(void (*kern)(P...), int grid, int tpb, cudaStream_t s, A&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(tpb);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, std::forward<A>(args)...);
+}
+
+template <int C, bool UNIFORM>
 static cudaError_t sc_dispatch(const IsingScArgs& a, const IsingTable& tab, RngKey key, int proposal, bool update,
                                long long* part, int grid, int tpb, cudaStream_t s) {
   const bool m = part != nullptr;
-  if (!update) {
-    ising_sc_kernel<C, ALLPER, true, false, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, tab, key, part);
-  } else if (proposal == VG_PROPOSE_FLIP) {
-    if (m) ising_sc_kernel<C, ALLPER, true, true, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, tab, key, part);
-    else ising_sc_kernel<C, ALLPER, false, true, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, tab, key, part);
-  } else {
-    if (m) ising_sc_kernel<C, ALLPER, true, true, VG_PROPOSE_RANDOM><<<grid, tpb, 0, s>>>(a, tab, key, part);
-    else ising_sc_kernel<C, ALLPER, false, true, VG_PROPOSE_RANDOM><<<grid, tpb, 0, s>>>(a, tab, key, part);
+  if (!update) return launch_pdl(ising_sc_kernel<C, UNIFORM, true, false, VG_PROPOSE_FLIP>, grid, tpb, s, a, tab, key, part);
+  if (proposal == VG_PROPOSE_FLIP) {
+    if (m) return launch_pdl(ising_sc_kernel<C, UNIFORM, true, true, VG_PROPOSE_FLIP>, grid, tpb, s, a, tab, key, part);
+    return launch_pdl(ising_sc_kernel<C, UNIFORM, false, true, VG_PROPOSE_FLIP>, grid, tpb, s, a, tab, key, part);
   }
-  return cudaGetLastError();
+  if (m) return launch_pdl(ising_sc_kernel<C, UNIFORM, true, true, VG_PROPOSE_RANDOM>, grid, tpb, s, a, tab, key, part);
+  return launch_pdl(ising_sc_kernel<C, UNIFORM, false, true, VG_PROPOSE_RANDOM>, grid, tpb, s, a, tab, key, part);
+}
+
+// Resident blocks per SM of the sc kernel (for grid sizing).
+int ising_sc_blocks_per_sm(bool uniform, int tpb) {
+  int n = 0;
+  if (uniform) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ising_sc_kernel<1, true, true, true, VG_PROPOSE_FLIP>, tpb, 0);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ising_sc_kernel<1, false, true, true, VG_PROPOSE_FLIP>, tpb, 0);
+  return n > 0 ? n : 1;
 }
 
 cudaError_t launch_ising_sc(const IsingScArgs& a, const IsingTable& tab, RngKey key, int colour, int proposal,
