@@ -180,6 +180,63 @@ int vg_magnetization(vg_ctx* ctx, double m[3], double* magnitude);
 /* Total energy / |M| from raw sums with a context's Hamiltonian semantics. */
 int vg_energy_from_sums(const vg_ctx* ctx, const vg_sums* sums, double* energy, double* magnitude);
 
+/* ------------------------------------------------------ batched replicas */
+/* Many independent Ising replicas (MetropolisFlipIntegrator,
+ * src/integrator.rs:99-138, with Exchange only, h = 0) run at once: 32
+ * replicas of one lattice share each 32-bit word (multi-spin coding; bit l
+ * is replica 32w + l, 1 = Up).  A group is n_replicas (a multiple of 32, at
+ * most 1024) replicas of one sc lattice with even extents, periodic on every
+ * axis or 2D (nz = 1, open z), and a temperature ladder: replica r starts at
+ * ladder entry r.  Work proceeds in rounds of sweeps_per_round sweeps; after
+ * each round the engine records, per replica, the number of anti-aligned
+ * bonds and of up spins, and (if replica_exchange) swaps the temperatures of
+ * adjacent ladder entries i, i+1 (i even in even rounds, odd in odd rounds)
+ * with probability min(1, exp((1/T_i - 1/T_j)(E_i - E_j))).  A round is
+ * replayed as one CUDA graph.  Every replica's updates are bit-exact against
+ * an independent single-replica oracle of the same draws. */
+typedef struct {
+  vg_lattice_desc lattice;
+  int32_t n_replicas;
+  const double* temperatures;  /* n_replicas ladder entries (copied) */
+} vg_replica_group;
+
+typedef struct vg_batch vg_batch;
+
+typedef struct {
+  int32_t n_groups;
+  int32_t total_replicas;
+  int32_t replica_words;
+  int32_t sweeps_per_round;
+  int64_t replica_sites;       /* sum over replicas of lattice sites: flips per sweep */
+  uint64_t sweep_index;
+  uint32_t round_index;
+  int32_t graph;               /* 1 if a round is replayed as a CUDA graph */
+} vg_batch_info;
+
+int vg_batch_create(const vg_replica_group* groups, int32_t n_groups, double exchange, uint64_t seed,
+                    int32_t sweeps_per_round, int32_t replica_exchange, vg_batch** out);
+int vg_batch_destroy(vg_batch* batch);
+const char* vg_batch_last_error(const vg_batch* batch);
+int vg_batch_get_info(const vg_batch* batch, vg_batch_info* out);
+int vg_batch_get_stream(const vg_batch* batch, void** cuda_stream);
+/* Every replica random (bit l of Philox(site, 0, tag, word)), ladder reset. */
+int vg_batch_init_random(vg_batch* batch);
+/* rounds x sweeps_per_round sweeps (synchronous / enqueue only). */
+int vg_batch_run(vg_batch* batch, uint64_t rounds);
+int vg_batch_run_async(vg_batch* batch, uint64_t rounds);
+int vg_batch_synchronize(vg_batch* batch);
+/* Round `round` (0-based) of the last run: counts[2 r] = anti-aligned bonds,
+ * counts[2 r + 1] = up spins of replica r (global index), tau[r] = its
+ * ladder entry during that round.  E_r = -J (z N / 2 - 2 anti), M_r = 2 up - N. */
+int vg_batch_observables(vg_batch* batch, uint64_t round, int64_t* counts, int32_t* tau);
+/* Current ladder entry of every replica of a group. */
+int vg_batch_ladder(vg_batch* batch, int32_t group, int32_t* tau);
+/* Accepted / attempted swaps of ladder pairs (i, i+1), per i. */
+int vg_batch_swap_stats(vg_batch* batch, int32_t group, int64_t* accepted, int64_t* attempted);
+/* One replica's spins (int8 +1/-1, site order). */
+int vg_batch_get_replica(vg_batch* batch, int32_t group, int32_t replica, int8_t* spins);
+int vg_batch_set_replica(vg_batch* batch, int32_t group, int32_t replica, const int8_t* spins);
+
 /* ------------------------------------------------------ no-alloc sweeps */
 /* No counterpart in the reference.  n Ising flip-proposal sweeps of an sc
  * lattice (x a multiple of 32, even extents on periodic axes) that allocate

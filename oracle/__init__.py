@@ -54,6 +54,11 @@ class Hamiltonian(C.Structure):
                 ("compound", C.c_int32)]
 
 
+class MscGroup(C.Structure):
+    _fields_ = [("lat", Lattice), ("n_rep", C.c_int32), ("temperatures", C.POINTER(C.c_double)),
+                ("seg_base", C.c_uint32), ("spins", C.POINTER(C.c_int8)), ("tau", C.POINTER(C.c_int32))]
+
+
 class Pcg64(C.Structure):
     _fields_ = [("state_hi", C.c_uint64), ("state_lo", C.c_uint64),
                 ("inc_hi", C.c_uint64), ("inc_lo", C.c_uint64)]
@@ -109,6 +114,9 @@ def lib():
         L.vo_hysteresis_fields.argtypes = [C.c_double, C.c_double, P(C.c_double), C.c_int32]
         L.vo_hysteresis_fields.restype = C.c_int32
         L.vo_accumulate.argtypes = [P(C.c_double), C.c_int64, P(C.c_double)]
+        L.vo_msc_init.argtypes = [P(MscGroup), C.c_uint64]
+        L.vo_msc_run.argtypes = [P(MscGroup), C.c_int32, C.c_double, C.c_uint64, C.c_uint32, C.c_uint32, C.c_int32,
+                                 C.c_int32, C.c_int32, P(C.c_int64), P(C.c_int64)]
         _lib = L
     return _lib
 
@@ -205,6 +213,45 @@ class Graph:
             sf = np.ascontiguousarray(spin, dtype=np.float64)
         return lib().vo_ref_total_energy(self.n, self.zmax, _p(self.nbr, C.c_int32), kind, _p(si, C.c_int8),
                                          _p(sf, C.c_double), C.byref(H), bb, bmag)
+
+
+class MscBatch:
+    """Replica groups for the batched multi-spin-coded oracle (one int8 lattice per replica)."""
+
+    def __init__(self, groups):
+        # groups: list of (Lattice, temperatures array); word ids are assigned in order
+        self.groups = []
+        base = 0
+        for lat, temps in groups:
+            temps = np.ascontiguousarray(temps, dtype=np.float64)
+            n_rep = temps.size
+            assert n_rep % 32 == 0
+            n = int(lib().vo_num_sites(C.byref(lat)))
+            spins = np.zeros((n_rep, n), dtype=np.int8)
+            tau = np.arange(n_rep, dtype=np.int32)
+            self.groups.append(dict(lat=lat, temps=temps, spins=spins, tau=tau, base=base, n=n))
+            base += n_rep // 32
+        self.total = sum(g["temps"].size for g in self.groups)
+
+    def _structs(self):
+        arr = (MscGroup * len(self.groups))()
+        for k, g in enumerate(self.groups):
+            arr[k] = MscGroup(g["lat"], g["temps"].size, _p(g["temps"], C.c_double), g["base"],
+                              _p(g["spins"], C.c_int8), _p(g["tau"], C.c_int32))
+        return arr
+
+    def init(self, seed):
+        arr = self._structs()
+        for k in range(len(self.groups)):
+            lib().vo_msc_init(C.byref(arr[k]), seed)
+
+    def run(self, J, seed, sweep0, round0, every, rounds, exchange=True):
+        arr = self._structs()
+        obs = np.zeros((max(rounds, 1), self.total, 2), dtype=np.int64)
+        acc = np.zeros(self.total, dtype=np.int64)
+        lib().vo_msc_run(arr, len(self.groups), J, seed, sweep0, round0, every, rounds, int(exchange),
+                         _p(obs, C.c_int64), _p(acc, C.c_int64))
+        return obs[:rounds], acc
 
 
 def pcg64(seed: int) -> Pcg64:

@@ -704,6 +704,134 @@ int64_t vo_ref_parallel(const vo_lattice* lat, int32_t kind, int32_t proposal, c
   return total;
 }
 
+/* ======================================== batched multi-spin-coded oracle */
+/* The GPU packs 32 replicas per 32-bit word; here every replica is its own
+ * int8 lattice, updated with the draws the packed kernel uses:
+ *   plane p (0 = most significant) of class entry j in sweep t, colour c, is
+ *   word (p & 3) of Philox(j, t, TAG_MSC<<24 | c<<8 | p>>2, word id);
+ *   replica lane l's 32-bit uniform takes bit l of plane p as its bit 31-p.
+ * A move with dE = 2 J (z - 2 n_anti) <= 0 always accepts; otherwise accept
+ * iff U < thr(T, n_anti) (the Ising threshold rule above). */
+static int msc_z(const vo_lattice* L) { return L->nz == 1 && !L->pbc_z ? 4 : 6; }
+
+void vo_msc_init(vo_msc_group* g, uint64_t seed) {
+  int64_t n = vo_num_sites(&g->lat);
+  for (int32_t r = 0; r < g->n_rep; ++r) {
+    uint32_t word = g->seg_base + (uint32_t)(r / 32), lane = (uint32_t)(r % 32);
+    for (int64_t i = 0; i < n; ++i) {
+      uint32_t w[4];
+      draw(seed, (uint32_t)i, 0, (uint32_t)VO_TAG_MSC_INIT << 24, word, w);
+      g->spins[(int64_t)r * n + i] = (w[0] >> lane) & 1u ? 1 : -1;
+    }
+    g->tau[r] = r;
+  }
+}
+
+static uint32_t msc_uniform(uint64_t seed, uint32_t word, uint32_t sweep, int colour, int64_t j, uint32_t lane) {
+  uint32_t u = 0;
+  for (int p = 0; p < 32; ++p) {
+    uint32_t w[4];
+    draw(seed, (uint32_t)j, sweep, ((uint32_t)VO_TAG_MSC << 24) | ((uint32_t)colour << 8) | (uint32_t)(p >> 2), word, w);
+    u |= ((w[p & 3] >> lane) & 1u) << (31 - p);
+  }
+  return u;
+}
+
+int vo_msc_run(vo_msc_group* G, int32_t ng, double J, uint64_t seed, uint32_t sweep0, uint32_t round0, int32_t every,
+               int32_t rounds, int32_t exchange, int64_t* obs, int64_t* accepted) {
+  int64_t total_rep = 0;
+  for (int32_t gi = 0; gi < ng; ++gi) total_rep += G[gi].n_rep;
+  int64_t rep_off = 0;
+  for (int32_t gi = 0; gi < ng; ++gi) {
+    vo_msc_group* g = &G[gi];
+    const int64_t n = vo_num_sites(&g->lat);
+    const int z = msc_z(&g->lat);
+    int32_t* nbr = (int32_t*)malloc(sizeof(int32_t) * (size_t)(n * 6));
+    vo_build_neighbours(&g->lat, nbr);
+    int32_t* colour = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
+    const int ncol = vo_greedy_colouring(n, 6, nbr, colour);
+    int64_t* rank = class_ranks(n, colour, ncol);
+    uint64_t* thr = (uint64_t*)malloc(sizeof(uint64_t) * (size_t)g->n_rep * (size_t)(z + 1));
+    for (int32_t i = 0; i < g->n_rep; ++i) {
+      const double T = g->temperatures[i] < 2.220446049250313e-16 ? 2.220446049250313e-16 : g->temperatures[i];
+      for (int na = 0; na <= z; ++na) thr[(size_t)i * (z + 1) + na] = vo_ising_threshold(J, 0.0, T, 1, z - 2 * na);
+    }
+    int32_t* rep_at = (int32_t*)malloc(sizeof(int32_t) * (size_t)g->n_rep);
+    double* E = (double*)malloc(sizeof(double) * (size_t)g->n_rep);
+    for (int32_t r = 0; r < g->n_rep; ++r) rep_at[g->tau[r]] = r;
+    for (int32_t rd = 0; rd < rounds; ++rd) {
+      for (int32_t t = 0; t < every; ++t) {
+        const uint32_t sweep = sweep0 + (uint32_t)(rd * every + t);
+        for (int c = 0; c < 2; ++c)
+          for (int64_t i = 0; i < n; ++i) {
+            if (colour[i] != c) continue;
+            for (int32_t r = 0; r < g->n_rep; ++r) {
+              int8_t* sp = g->spins + (int64_t)r * n;
+              int na = 0;
+              for (int k = 0; k < 6; ++k) {
+                const int32_t q = nbr[i * 6 + k];
+                if (q >= 0 && sp[q] != sp[i]) ++na;
+              }
+              const uint64_t th = thr[(size_t)g->tau[r] * (z + 1) + na];
+              const int acc = th >= (1ull << 32)
+                                  ? 1
+                                  : msc_uniform(seed, g->seg_base + (uint32_t)(r / 32), sweep, c, rank[i],
+                                                (uint32_t)(r % 32)) < th;
+              if (acc) sp[i] = (int8_t)(-sp[i]);
+            }
+          }
+      }
+      /* measurement: anti-aligned bonds and up spins of every replica */
+      for (int32_t r = 0; r < g->n_rep; ++r) {
+        const int8_t* sp = g->spins + (int64_t)r * n;
+        int64_t anti2 = 0, ups = 0, nb2 = 0;
+        for (int64_t i = 0; i < n; ++i) {
+          ups += sp[i] > 0;
+          for (int k = 0; k < 6; ++k) {
+            const int32_t q = nbr[i * 6 + k];
+            if (q >= 0) {
+              ++nb2;
+              anti2 += sp[q] != sp[i];
+            }
+          }
+        }
+        E[r] = -J * (double)(nb2 / 2 - 2 * (anti2 / 2));
+        if (obs) {
+          int64_t* o = obs + ((int64_t)rd * total_rep + rep_off + r) * 2;
+          o[0] = anti2 / 2;
+          o[1] = ups;
+        }
+      }
+      /* replica exchange between adjacent ladder entries (i, i+1) */
+      if (exchange) {
+        const uint32_t round = round0 + (uint32_t)rd;
+        for (int32_t i = (int32_t)(round & 1u); i + 1 < g->n_rep; i += 2) {
+          const int32_t r1 = rep_at[i], r2 = rep_at[i + 1];
+          const double x = (1.0 / g->temperatures[i] - 1.0 / g->temperatures[i + 1]) * (E[r1] - E[r2]);
+          uint32_t w[4];
+          draw(seed, (uint32_t)i, round, ((uint32_t)VO_TAG_EXCHANGE << 24) | (uint32_t)gi, 0, w);
+          const double u = (double)w[0] * (1.0 / 4294967296.0);
+          if (x >= 0.0 || u < exp(x)) {
+            rep_at[i] = r2;
+            rep_at[i + 1] = r1;
+            g->tau[r1] = i + 1;
+            g->tau[r2] = i;
+            if (accepted) accepted[rep_off + i] += 1;
+          }
+        }
+      }
+    }
+    free(E);
+    free(rep_at);
+    free(thr);
+    free(rank);
+    free(colour);
+    free(nbr);
+    rep_off += g->n_rep;
+  }
+  return 0;
+}
+
 /* ================================================ programs and statistics */
 int32_t vo_cooldown_temperatures(double tmax, double tmin, double rate, double* out, int32_t cap) {
   int32_t n = 0;

@@ -149,6 +149,31 @@ int64_t vo_ref_parallel(const vo_lattice* lat, int32_t spin_kind, int32_t propos
                         const vo_hamiltonian* H, double T, int32_t nsweeps, int32_t measure,
                         int32_t nthreads, uint64_t seed, double* seconds);
 
+/* --------------------------------- (a) colour_cpu: batched multi-spin coding */
+/* A replica group: n_rep replicas (a multiple of 32) of one sc lattice that
+ * is periodic on every axis, or 2D (nz = 1, open z).  Replica r = 32 w + l is
+ * lane l of replica word w; its random numbers come from the Philox stream of
+ * word id (seg_base + w).  temperatures[i] is ladder entry i; replica r starts
+ * at ladder entry r.  spins: n_rep x N int8 (+1/-1), site order. */
+typedef struct {
+  vo_lattice lat;
+  int32_t n_rep;
+  const double* temperatures;
+  uint32_t seg_base;
+  int8_t* spins;
+  int32_t* tau;        /* ladder entry of each replica (in/out) */
+} vo_msc_group;
+
+enum { VO_TAG_MSC = 6, VO_TAG_MSC_INIT = 7, VO_TAG_EXCHANGE = 8 };
+
+void vo_msc_init(vo_msc_group* g, uint64_t seed);
+/* rounds x every sweeps; after each round the per-replica anti-aligned bond
+ * and up-spin counts are recorded (obs[round][rep][2], may be NULL) and, if
+ * exchange, adjacent ladder entries swap with probability
+ * min(1, exp((b_i - b_j)(E_i - E_j))).  accepted[i] counts swaps of (i, i+1). */
+int vo_msc_run(vo_msc_group* groups, int32_t n_groups, double J, uint64_t seed, uint32_t sweep0, uint32_t round0,
+               int32_t every, int32_t rounds, int32_t exchange, int64_t* obs, int64_t* accepted);
+
 /* ------------------------------------------------ programs and statistics */
 /* CoolDown temperatures (src/program.rs:202-211).  Returns count (<= cap). */
 int32_t vo_cooldown_temperatures(double tmax, double tmin, double rate, double* out, int32_t cap);

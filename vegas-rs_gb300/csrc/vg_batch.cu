@@ -1,0 +1,936 @@
+// vg_batch.cu -- batched, multi-spin-coded Ising Metropolis with on-device
+// replica exchange (the vg_batch_* ABI).
+//
+// Many independent replicas of MetropolisFlipIntegrator (src/integrator.rs:
+// 99-138) with J > 0 or < 0 and no field run at once.  A replica group is a
+// set of n replicas (a multiple of 32) of one sc lattice; every lattice site
+// holds one 32-bit word per 32 replicas (bit l = replica lane l, 1 = Up), in
+// the checkerboard class layout [z][y][x/2] of the single-lattice path.
+//
+// One colour pass updates a word (32 replicas) at once:
+//   * anti-aligned neighbour count per lane, bit-sliced with full adders
+//     (three-input XOR / majority), 3 bit planes;
+//   * dE = 2 J (z - 2 n_anti); moves with dE <= 0 always accept;
+//   * the rest compare their 32-bit uniform U with their threshold
+//     thr(T_lane, n_anti) most significant bit first: plane k is a Philox
+//     word whose bit l is bit 31-k of lane l's U; the thresholds are stored
+//     transposed (bit l of tab[q][k] = bit 31-k of lane l's threshold for the
+//     q-th drawing category).  A lane is decided at its first plane where the
+//     bits differ, so a word usually needs 6-11 planes (2-3 Philox blocks)
+//     for its 32 flips, and the outcome is exactly "U < thr".
+// Every `sweeps_per_round` sweeps a measurement kernel counts anti-aligned
+// bonds and up spins per replica (warp ballots over bit-sliced counts) and an
+// exchange kernel swaps the temperatures of adjacent ladder entries with
+// probability min(1, exp((b_i - b_j)(E_i - E_j))), then re-transposes the
+// threshold tables.  A round (passes, measurement, exchange, counter advance)
+// is captured once into a CUDA graph and replayed.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "vg_internal.cuh"
+
+using namespace vg;
+
+namespace {
+
+constexpr uint32_t kTagMsc = 6, kTagMscInit = 7, kTagExchange = 8;
+constexpr int kTabWords = 4 * 33;  // 4 drawing categories x (32 planes + always-lanes word)
+
+struct MscSeg {          // one replica word of one group
+  uint32_t* cls[2];
+  uint32_t n_c;          // words per class
+  int Hx, Ly, Lz;
+  int dim3;              // 1: z bonds (3D, periodic); 0: 2D (nz = 1, open z)
+  FastDiv fHx, fLy, fLx;
+  uint32_t word_id;      // Philox counter word 3
+  int group;
+  int nd;                // drawing categories (dE > 0)
+  int dn[4];             // their anti-aligned counts
+  int rep0;              // global index of lane 0
+};
+
+struct MscGroupDev {
+  int n_rep, rep_off, seg0, z;
+  double J, nbonds;
+  const double* beta;                 // 1/T per ladder entry
+  const unsigned long long* thr;      // [ladder][z + 1]
+  int* tau;                           // ladder entry of each replica
+  int* rep_at;                        // replica at each ladder entry
+  unsigned long long* accepted;       // swaps accepted per pair (i, i+1)
+  unsigned long long* attempted;
+};
+
+struct MscDev {
+  uint32_t sweep0;
+  uint32_t round;
+  uint32_t round_base;   // first round of the current run (ring slot 0)
+  uint32_t pad;
+};
+
+__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+// (b2 b1 b0) = number of set lanes among the inputs, per lane
+__device__ __forceinline__ void count6(uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t a4, uint32_t a5,
+                                       uint32_t& b0, uint32_t& b1, uint32_t& b2) {
+  const uint32_t sa = a0 ^ a1 ^ a2, ca = (a0 & a1) | (a0 & a2) | (a1 & a2);
+  const uint32_t sb = a3 ^ a4 ^ a5, cb = (a3 & a4) | (a3 & a5) | (a4 & a5);
+  b0 = sa ^ sb;
+  const uint32_t cab = sa & sb;
+  b1 = ca ^ cb ^ cab;
+  b2 = (ca & cb) | (ca & cab) | (cb & cab);
+}
+__device__ __forceinline__ void count4(uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t& b0,
+                                       uint32_t& b1, uint32_t& b2) {
+  const uint32_t sa = a0 ^ a1 ^ a2, ca = (a0 & a1) | (a0 & a2) | (a1 & a2);
+  b0 = sa ^ a3;
+  const uint32_t cx = sa & a3;
+  b1 = ca ^ cx;
+  b2 = ca & cx;
+}
+__device__ __forceinline__ uint32_t lanes_equal(uint32_t b0, uint32_t b1, uint32_t b2, int v) {
+  return ((v & 1) ? b0 : ~b0) & ((v & 2) ? b1 : ~b1) & ((v & 4) ? b2 : ~b2);
+}
+
+// Neighbour words of class entry j in the other class, xor'ed with s.
+__device__ __forceinline__ void msc_anti(const MscSeg& sg, int C, uint32_t j, uint32_t s, const uint32_t* oth,
+                                         uint32_t (&a)[6]) {
+  const int row = (int)fdiv(j, sg.fHx);
+  const int h = (int)(j - (uint32_t)row * sg.Hx);
+  const int z = (int)fdiv((uint32_t)row, sg.fLy);
+  const int y = row - z * sg.Ly;
+  const int p = (y + z + C) & 1;
+  const int rb = row * sg.Hx;
+  const int hx = p ? (h + 1 == sg.Hx ? 0 : h + 1) : (h == 0 ? sg.Hx - 1 : h - 1);
+  const int ym = y == 0 ? row + sg.Ly - 1 : row - 1;
+  const int yp = y == sg.Ly - 1 ? row - (sg.Ly - 1) : row + 1;
+  a[0] = s ^ __ldg(oth + rb + h);
+  a[1] = s ^ __ldg(oth + rb + hx);
+  a[2] = s ^ __ldg(oth + (size_t)ym * sg.Hx + h);
+  a[3] = s ^ __ldg(oth + (size_t)yp * sg.Hx + h);
+  if (sg.dim3) {
+    const int zm = z == 0 ? row + (sg.Lz - 1) * sg.Ly : row - sg.Ly;
+    const int zp = z == sg.Lz - 1 ? row - (sg.Lz - 1) * sg.Ly : row + sg.Ly;
+    a[4] = s ^ __ldg(oth + (size_t)zm * sg.Hx + h);
+    a[5] = s ^ __ldg(oth + (size_t)zp * sg.Hx + h);
+  } else {
+    a[4] = a[5] = 0u;
+  }
+}
+
+// Bit-plane decision state of one word (32 replicas at one site).
+template <int ND>
+struct WordState {
+  uint32_t m[ND];   // lanes in each drawing category
+  uint32_t und;     // lanes still undecided
+  uint32_t acc;     // lanes accepted so far
+};
+
+// Planes 4*blkno .. 4*blkno+3 of word j.
+template <int C, int ND>
+__device__ __forceinline__ void msc_block(WordState<ND>& w, uint32_t j, uint32_t sweep, uint32_t word_id,
+                                          int blkno, const uint32_t* s_tab, const KeySchedule& ks) {
+  const uint4 bk = philox_ks(make_uint4(j, sweep, (kTagMsc << 24) | ((uint32_t)C << 8) | (uint32_t)blkno, word_id), ks);
+  const uint32_t R[4] = {bk.x, bk.y, bk.z, bk.w};
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int k = 4 * blkno + i;
+    uint32_t T = 0;
+#pragma unroll
+    for (int q = 0; q < ND; ++q) T |= w.m[q] & s_tab[q * 33 + k];
+    w.acc |= w.und & ~R[i] & T;
+    w.und &= ~(R[i] ^ T);
+  }
+}
+
+// Categories of word j and its first 8 planes.  ZZ is the coordination (4 or
+// 6); the drawing categories are the anti-aligned counts with dE > 0:
+// n < ZZ/2 for J > 0, n > ZZ/2 for J < 0 (none for J = 0).
+template <int C, int ZZ>
+__device__ __forceinline__ WordState<ZZ / 2> msc_word_start(const MscSeg& sg, uint32_t j, uint32_t s,
+                                                            const uint32_t* oth, const uint32_t* s_tab,
+                                                            uint32_t sweep, const KeySchedule& ks, int jsign) {
+  constexpr int ND = ZZ / 2;
+  WordState<ND> w;
+  uint32_t a[6];
+  msc_anti(sg, C, j, s, oth, a);
+  uint32_t b0, b1, b2;
+  if (ZZ == 6) count6(a[0], a[1], a[2], a[3], a[4], a[5], b0, b1, b2);
+  else count4(a[0], a[1], a[2], a[3], b0, b1, b2);
+  uint32_t draw = 0, alw = 0;
+#pragma unroll
+  for (int q = 0; q < ND; ++q) {
+    const int n = jsign > 0 ? q : ZZ / 2 + 1 + q;
+    w.m[q] = jsign == 0 ? 0u : lanes_equal(b0, b1, b2, n);
+    draw |= w.m[q];
+    alw |= w.m[q] & s_tab[q * 33 + 32];
+  }
+  w.acc = ~draw | alw;
+  w.und = draw & ~alw;
+  msc_block<C, ND>(w, j, sweep, sg.word_id, 0, s_tab, ks);
+  msc_block<C, ND>(w, j, sweep, sg.word_id, 1, s_tab, ks);
+  return w;
+}
+
+constexpr int kWordsPerThread = 4;  // block covers 256 x 4 consecutive words of one segment
+
+// Words still undecided after 8 planes are queued per warp and finished 32
+// at a time, so the rare long comparisons run with full warps.
+constexpr int kQueue = 64;          // per-warp queue entries
+constexpr int kQueueWords = 4 + 3;  // j, s, und, acc, m[<= 3]
+
+template <int C, int ZZ>
+__device__ __forceinline__ void msc_pass_body(const MscSeg& sg, uint32_t j0, uint32_t* own, const uint32_t* oth,
+                                              const uint32_t* s_tab, uint32_t sweep, const KeySchedule& ks,
+                                              int jsign, uint32_t (*s_q)[kQueue][kQueueWords]) {
+  constexpr int ND = ZZ / 2;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int qn = 0;
+  auto finish = [&](int n) {  // complete the first n queued words, one per lane
+    __syncwarp();
+    if (lane < n) {
+      const uint32_t* e = s_q[warp][lane];
+      WordState<ND> w;
+      const uint32_t j = e[0], s = e[1];
+      w.und = e[2];
+      w.acc = e[3];
+#pragma unroll
+      for (int q = 0; q < ND; ++q) w.m[q] = e[4 + q];
+#pragma unroll 1
+      for (int blkno = 2; w.und != 0u && blkno < 8; ++blkno) msc_block<C, ND>(w, j, sweep, sg.word_id, blkno, s_tab, ks);
+      if (w.acc) own[j] = s ^ w.acc;
+    }
+    __syncwarp();
+    const int rest = qn - n;
+    uint32_t tmp[ND + 4];
+    if (lane < rest)
+#pragma unroll
+      for (int i = 0; i < ND + 4; ++i) tmp[i] = s_q[warp][n + lane][i];
+    __syncwarp();
+    if (lane < rest)
+#pragma unroll
+      for (int i = 0; i < ND + 4; ++i) s_q[warp][lane][i] = tmp[i];
+    __syncwarp();
+    qn = rest;
+  };
+#pragma unroll 1
+  for (int u = 0; u < kWordsPerThread; ++u) {
+    const uint32_t j = j0 + (uint32_t)(u * 256) + threadIdx.x;
+    const bool live = j < sg.n_c;
+    bool pend = false;
+    WordState<ND> w;
+    uint32_t s = 0;
+    if (live) {
+      s = own[j];
+      w = msc_word_start<C, ZZ>(sg, j, s, oth, s_tab, sweep, ks, jsign);
+      pend = w.und != 0u;
+      if (!pend && w.acc) own[j] = s ^ w.acc;
+    }
+    const unsigned pmask = __ballot_sync(0xffffffffu, pend);
+    if (pmask) {
+      if (pend) {
+        uint32_t* e = s_q[warp][qn + __popc(pmask & ((1u << lane) - 1u))];
+        e[0] = j;
+        e[1] = s;
+        e[2] = w.und;
+        e[3] = w.acc;
+#pragma unroll
+        for (int q = 0; q < ND; ++q) e[4 + q] = w.m[q];
+      }
+      qn += __popc(pmask);
+      if (qn >= 32) finish(32);
+    }
+  }
+  if (qn > 0) finish(qn);
+}
+
+template <int C>
+__global__ void __launch_bounds__(256) msc_pass(const MscSeg* __restrict__ segs, const int2* __restrict__ blocks,
+                                                const uint32_t* __restrict__ tabs, const MscDev* __restrict__ dev,
+                                                uint32_t t_off, KeySchedule ks, int jsign) {
+  __shared__ uint32_t s_tab[kTabWords];
+  __shared__ uint32_t s_q[8][kQueue][kQueueWords];
+  pdl_launch_dependents();
+  const int2 bl = blocks[blockIdx.x];
+  const MscSeg sg = segs[bl.x];
+  // Tables and counters change only in the exchange / advance kernels, which
+  // complete before any pass of the next round starts; spins are read after
+  // the wait for the previous pass.
+  for (int i = threadIdx.x; i < kTabWords; i += blockDim.x) s_tab[i] = tabs[(size_t)bl.x * kTabWords + i];
+  const uint32_t sweep = dev->sweep0 + t_off;
+  __syncthreads();
+  pdl_wait();
+  uint32_t* own = sg.cls[C];
+  const uint32_t* oth = sg.cls[C ^ 1];
+  if (sg.dim3) msc_pass_body<C, 6>(sg, (uint32_t)bl.y, own, oth, s_tab, sweep, ks, jsign, s_q);
+  else msc_pass_body<C, 4>(sg, (uint32_t)bl.y, own, oth, s_tab, sweep, ks, jsign, s_q);
+}
+
+// Per replica: anti-aligned bonds (over class-1 sites, whose neighbours are
+// all class 0) and up spins, added into obs[slot][replica][2].
+__global__ void __launch_bounds__(256) msc_measure(const MscSeg* __restrict__ segs, const int2* __restrict__ blocks,
+                                                   const MscDev* __restrict__ dev, int total_rep,
+                                                   unsigned long long* __restrict__ obs) {
+  __shared__ unsigned int s_cnt[2][32];
+  const int2 bl = blocks[blockIdx.x];
+  const MscSeg& sg = segs[bl.x];
+  if (threadIdx.x < 32) {
+    s_cnt[0][threadIdx.x] = 0;
+    s_cnt[1][threadIdx.x] = 0;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  unsigned int ca = 0, cu = 0;
+  for (int w = 0; w < kWordsPerThread; ++w) {
+    const uint32_t j = (uint32_t)bl.y + (uint32_t)(w * 256) + threadIdx.x;
+    uint32_t b0 = 0, b1 = 0, b2 = 0, u0 = 0, u1 = 0;
+    if (j < sg.n_c) {
+      const uint32_t s1 = sg.cls[1][j], s0 = sg.cls[0][j];
+      uint32_t a[6];
+      msc_anti(sg, 1, j, s1, sg.cls[0], a);
+      if (sg.dim3) count6(a[0], a[1], a[2], a[3], a[4], a[5], b0, b1, b2);
+      else count4(a[0], a[1], a[2], a[3], b0, b1, b2);
+      u0 = s0 ^ s1;
+      u1 = s0 & s1;
+    }
+    for (int l = 0; l < 32; ++l) {
+      const unsigned int na = __popc(__ballot_sync(0xffffffffu, (b0 >> l) & 1u)) +
+                              2u * __popc(__ballot_sync(0xffffffffu, (b1 >> l) & 1u)) +
+                              4u * __popc(__ballot_sync(0xffffffffu, (b2 >> l) & 1u));
+      const unsigned int nu = __popc(__ballot_sync(0xffffffffu, (u0 >> l) & 1u)) +
+                              2u * __popc(__ballot_sync(0xffffffffu, (u1 >> l) & 1u));
+      if (lane == l) {
+        ca += na;
+        cu += nu;
+      }
+    }
+  }
+  atomicAdd(&s_cnt[0][lane], ca);
+  atomicAdd(&s_cnt[1][lane], cu);
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const uint32_t slot = dev->round - dev->round_base;
+    unsigned long long* o = obs + ((size_t)slot * total_rep + sg.rep0 + threadIdx.x) * 2;
+    atomicAdd(o, (unsigned long long)s_cnt[0][threadIdx.x]);
+    atomicAdd(o + 1, (unsigned long long)s_cnt[1][threadIdx.x]);
+  }
+}
+
+// Threshold planes of every replica word of group g from the current
+// temperature assignment.
+__device__ void msc_build_tabs(const MscGroupDev& G, const MscSeg* segs, uint32_t* tabs) {
+  const int nw = G.n_rep / 32;
+  const MscSeg& s0 = segs[G.seg0];
+  for (int e = threadIdx.x; e < nw * kTabWords; e += blockDim.x) {
+    const int w = e / kTabWords, r = e % kTabWords, q = r / 33, k = r % 33;
+    uint32_t v = 0;
+    if (q < s0.nd) {
+      for (int l = 0; l < 32; ++l) {
+        const unsigned long long th = G.thr[(size_t)G.tau[w * 32 + l] * (G.z + 1) + s0.dn[q]];
+        uint32_t bit;
+        if (k == 32) bit = th >= (1ull << 32) ? 1u : 0u;
+        else bit = th >= (1ull << 32) ? 0u : (uint32_t)((th >> (31 - k)) & 1ull);
+        v |= bit << l;
+      }
+    }
+    tabs[(size_t)(G.seg0 + w) * kTabWords + r] = v;
+  }
+}
+
+__global__ void msc_tabs_kernel(const MscGroupDev* __restrict__ groups, const MscSeg* __restrict__ segs,
+                                uint32_t* __restrict__ tabs) {
+  msc_build_tabs(groups[blockIdx.x], segs, tabs);
+}
+
+// One block per group: energies, ladder swaps, threshold tables.
+__global__ void msc_exchange(const MscGroupDev* __restrict__ groups, const MscSeg* __restrict__ segs,
+                             uint32_t* __restrict__ tabs, const MscDev* __restrict__ dev, int total_rep,
+                             const unsigned long long* __restrict__ obs, int* __restrict__ tau_ring, int do_exchange,
+                             KeySchedule ks) {
+  extern __shared__ double s_E[];
+  const MscGroupDev G = groups[blockIdx.x];
+  const uint32_t round = dev->round;
+  const uint32_t slot = round - dev->round_base;
+  for (int r = threadIdx.x; r < G.n_rep; r += blockDim.x) {
+    const unsigned long long anti = obs[((size_t)slot * total_rep + G.rep_off + r) * 2];
+    s_E[r] = -G.J * (G.nbonds - 2.0 * (double)anti);
+    tau_ring[(size_t)slot * total_rep + G.rep_off + r] = G.tau[r];
+  }
+  __syncthreads();
+  if (do_exchange) {
+    for (int i = (int)(round & 1u) + 2 * threadIdx.x; i + 1 < G.n_rep; i += 2 * blockDim.x) {
+      const int r1 = G.rep_at[i], r2 = G.rep_at[i + 1];
+      const double x = (G.beta[i] - G.beta[i + 1]) * (s_E[r1] - s_E[r2]);
+      const uint4 w = philox_ks(make_uint4((uint32_t)i, round, (kTagExchange << 24) | (uint32_t)blockIdx.x, 0u), ks);
+      const double u = (double)w.x * (1.0 / 4294967296.0);
+      G.attempted[i] += 1;
+      if (x >= 0.0 || u < exp(x)) {
+        G.rep_at[i] = r2;
+        G.rep_at[i + 1] = r1;
+        G.tau[r1] = i + 1;
+        G.tau[r2] = i;
+        G.accepted[i] += 1;
+      }
+    }
+    __syncthreads();
+    msc_build_tabs(G, segs, tabs);
+  }
+}
+
+__global__ void msc_advance(MscDev* dev, uint32_t sweeps) {
+  dev->sweep0 += sweeps;
+  dev->round += 1;
+}
+
+// Initial state: bit l of word 0 of Philox(site, 0, tag, word id) is lane l.
+__global__ void msc_init(const MscSeg* __restrict__ segs, int nseg, KeySchedule ks) {
+  const MscSeg sg = segs[blockIdx.y];
+  const uint32_t Lx = 2u * (uint32_t)sg.Hx;
+  const uint32_t n = 2u * sg.n_c;
+  const FastDiv fLx = sg.fLx;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint4 w = philox_ks(make_uint4(i, 0u, kTagMscInit << 24, sg.word_id), ks);
+    const uint32_t r = fdiv(i, fLx), x = i - r * Lx;
+    const uint32_t zz = fdiv(r, sg.fLy), y = r - zz * (uint32_t)sg.Ly;
+    const int c = (int)((x + y + zz) & 1u);
+    sg.cls[c][r * (uint32_t)sg.Hx + (x >> 1)] = w.x;
+  }
+  (void)nseg;
+}
+
+// Unpack / pack one replica lane in site order.
+__global__ void msc_get(const MscSeg sg, uint32_t lane, int8_t* __restrict__ out) {
+  const uint32_t Lx = 2u * (uint32_t)sg.Hx, n = 2u * sg.n_c;
+  const FastDiv fLx = sg.fLx;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint32_t r = fdiv(i, fLx), x = i - r * Lx;
+    const uint32_t zz = fdiv(r, sg.fLy), y = r - zz * (uint32_t)sg.Ly;
+    const int c = (int)((x + y + zz) & 1u);
+    out[i] = (sg.cls[c][r * (uint32_t)sg.Hx + (x >> 1)] >> lane) & 1u ? 1 : -1;
+  }
+}
+
+__global__ void msc_set(const MscSeg sg, uint32_t lane, const int8_t* __restrict__ in, int* flag) {
+  const uint32_t Lx = 2u * (uint32_t)sg.Hx, n = 2u * sg.n_c;
+  const FastDiv fLx = sg.fLx;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int8_t v = in[i];
+    if (v != 1 && v != -1) atomicOr(flag, 1);
+    const uint32_t r = fdiv(i, fLx), x = i - r * Lx;
+    const uint32_t zz = fdiv(r, sg.fLy), y = r - zz * (uint32_t)sg.Ly;
+    const int c = (int)((x + y + zz) & 1u);
+    uint32_t* p = &sg.cls[c][r * (uint32_t)sg.Hx + (x >> 1)];
+    if (v > 0) atomicOr(p, 1u << lane);
+    else atomicAnd(p, ~(1u << lane));
+  }
+}
+
+struct GroupHost {
+  vg_lattice_desc lat;
+  int n_rep, z, nd, dn[4], seg0, rep_off;
+  long long n;
+  std::vector<double> temps;
+  double* d_beta = nullptr;
+  unsigned long long* d_thr = nullptr;
+  int* d_tau = nullptr;
+  int* d_rep_at = nullptr;
+  unsigned long long* d_acc = nullptr;
+  unsigned long long* d_att = nullptr;
+};
+
+}  // namespace
+
+struct vg_batch {
+  int device = 0;
+  cudaStream_t own_stream = nullptr, stream = nullptr;
+  double J = 1.0;
+  uint64_t seed = 0;
+  KeySchedule ks{};
+  int every = 10, exchange = 1, total_rep = 0;
+  std::vector<GroupHost> groups;
+  std::vector<MscSeg> segs;
+  MscSeg* d_segs = nullptr;
+  std::vector<int2> blocks;
+  int2* d_blocks = nullptr;
+  uint32_t* d_tabs = nullptr;
+  MscGroupDev* d_groups = nullptr;
+  MscDev* d_dev = nullptr;
+  uint32_t* d_spins = nullptr;
+  unsigned long long* d_obs = nullptr;
+  int* d_tau_ring = nullptr;
+  size_t ring_cap = 0;
+  uint64_t last_rounds = 0;
+  uint64_t sweep = 0;
+  uint32_t round = 0;
+  cudaGraphExec_t graph = nullptr;
+  int* d_flag = nullptr;
+  int8_t* d_stage = nullptr;
+  long long stage_n = 0;
+  long long replica_sites = 0;
+  std::string err;
+};
+
+extern "C" void vg_internal_set_last_error(const char* msg);
+
+namespace {
+
+int bfail(vg_batch* b, int code, const std::string& m) {
+  if (b) b->err = m;
+  vg_internal_set_last_error(m.c_str());
+  return code;
+}
+
+#define VG_BCUDA(b, expr)                                                                          \
+  do {                                                                                             \
+    cudaError_t _e = (expr);                                                                       \
+    if (_e != cudaSuccess)                                                                         \
+      return bfail((b), _e == cudaErrorMemoryAllocation ? VG_ERR_OOM : VG_ERR_CUDA,                \
+                   std::string(#expr) + ": " + cudaGetErrorString(_e));                            \
+  } while (0)
+
+template <typename T>
+int balloc(vg_batch* b, T** p, size_t count) {
+  VG_BCUDA(b, cudaMalloc((void**)p, std::max<size_t>(count, 1) * sizeof(T)));
+  return VG_OK;
+}
+
+void bdestroy(vg_batch* b) {
+  if (!b) return;
+  cudaSetDevice(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  for (auto& g : b->groups) {
+    cudaFree(g.d_beta);
+    cudaFree(g.d_thr);
+    cudaFree(g.d_tau);
+    cudaFree(g.d_rep_at);
+    cudaFree(g.d_acc);
+    cudaFree(g.d_att);
+  }
+  cudaFree(b->d_segs);
+  cudaFree(b->d_blocks);
+  cudaFree(b->d_tabs);
+  cudaFree(b->d_groups);
+  cudaFree(b->d_dev);
+  cudaFree(b->d_spins);
+  cudaFree(b->d_obs);
+  cudaFree(b->d_tau_ring);
+  cudaFree(b->d_flag);
+  cudaFree(b->d_stage);
+  if (b->own_stream) cudaStreamDestroy(b->own_stream);
+  delete b;
+}
+
+template <typename... P, typename... A>
+cudaError_t launch_pdl(void (*kern)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, A&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, std::forward<A>(args)...);
+}
+
+// One round on the stream: sweeps, measurement, exchange, advance.
+int enqueue_round(vg_batch* b) {
+  const int nb = (int)b->blocks.size();
+  for (int t = 0; t < b->every; ++t) {
+    const int jsign = b->J > 0.0 ? 1 : b->J < 0.0 ? -1 : 0;
+    VG_BCUDA(b, launch_pdl(msc_pass<0>, dim3(nb), dim3(256), 0, b->stream, (const MscSeg*)b->d_segs,
+                           (const int2*)b->d_blocks, (const uint32_t*)b->d_tabs, (const MscDev*)b->d_dev,
+                           (uint32_t)t, b->ks, jsign));
+    VG_BCUDA(b, launch_pdl(msc_pass<1>, dim3(nb), dim3(256), 0, b->stream, (const MscSeg*)b->d_segs,
+                           (const int2*)b->d_blocks, (const uint32_t*)b->d_tabs, (const MscDev*)b->d_dev,
+                           (uint32_t)t, b->ks, jsign));
+  }
+  msc_measure<<<nb, 256, 0, b->stream>>>(b->d_segs, b->d_blocks, b->d_dev, b->total_rep, b->d_obs);
+  VG_BCUDA(b, cudaGetLastError());
+  int maxrep = 0;
+  for (auto& g : b->groups) maxrep = std::max(maxrep, g.n_rep);
+  msc_exchange<<<(int)b->groups.size(), 256, sizeof(double) * maxrep, b->stream>>>(
+      b->d_groups, b->d_segs, b->d_tabs, b->d_dev, b->total_rep, b->d_obs, b->d_tau_ring, b->exchange, b->ks);
+  VG_BCUDA(b, cudaGetLastError());
+  msc_advance<<<1, 1, 0, b->stream>>>(b->d_dev, (uint32_t)b->every);
+  VG_BCUDA(b, cudaGetLastError());
+  return VG_OK;
+}
+
+// The per-round ring buffers are baked into the captured graph: growing them
+// drops the graph, which is captured again with the new pointers.
+int ensure_ring(vg_batch* b, uint64_t rounds) {
+  if (rounds <= b->ring_cap) return VG_OK;
+  rounds = std::max<uint64_t>(rounds, std::max<uint64_t>(64, 2 * b->ring_cap));
+  VG_BCUDA(b, cudaStreamSynchronize(b->stream));
+  if (b->graph) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  cudaFree(b->d_obs);
+  cudaFree(b->d_tau_ring);
+  b->d_obs = nullptr;
+  b->d_tau_ring = nullptr;
+  int rc;
+  if ((rc = balloc(b, &b->d_obs, (size_t)rounds * b->total_rep * 2))) return rc;
+  if ((rc = balloc(b, &b->d_tau_ring, (size_t)rounds * b->total_rep))) return rc;
+  b->ring_cap = rounds;
+  return VG_OK;
+}
+
+int find_replica(vg_batch* b, int g, int r, MscSeg* sg, uint32_t* lane) {
+  if (g < 0 || g >= (int)b->groups.size()) return bfail(b, VG_ERR_INVALID_ARG, "group index out of range");
+  const GroupHost& G = b->groups[g];
+  if (r < 0 || r >= G.n_rep) return bfail(b, VG_ERR_INVALID_ARG, "replica index out of range");
+  *sg = b->segs[G.seg0 + r / 32];
+  *lane = (uint32_t)(r % 32);
+  return VG_OK;
+}
+
+int ensure_stage(vg_batch* b, long long n) {
+  if (n <= b->stage_n) return VG_OK;
+  cudaFree(b->d_stage);
+  b->d_stage = nullptr;
+  int rc = balloc(b, &b->d_stage, (size_t)n);
+  if (rc) return rc;
+  b->stage_n = n;
+  return VG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int vg_batch_create(const vg_replica_group* groups, int32_t n_groups, double J, uint64_t seed,
+                    int32_t sweeps_per_round, int32_t replica_exchange, vg_batch** out) {
+  if (!out || !groups || n_groups < 1) return bfail(nullptr, VG_ERR_INVALID_ARG, "no replica groups");
+  *out = nullptr;
+  if (sweeps_per_round < 1) return bfail(nullptr, VG_ERR_INVALID_ARG, "sweeps_per_round must be >= 1");
+  if (!std::isfinite(J)) return bfail(nullptr, VG_ERR_INVALID_ARG, "exchange constant must be finite");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return bfail(nullptr, VG_ERR_NO_DEVICE, "no CUDA device is visible");
+  vg_batch* b = new (std::nothrow) vg_batch();
+  if (!b) return bfail(nullptr, VG_ERR_OOM, "host allocation failed");
+  cudaGetDevice(&b->device);
+  b->J = J;
+  b->seed = seed;
+  b->ks = make_key_schedule((uint32_t)seed, (uint32_t)(seed >> 32));
+  b->every = sweeps_per_round;
+  b->exchange = replica_exchange != 0;
+  if (cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    bdestroy(b);
+    return bfail(nullptr, VG_ERR_CUDA, "stream creation failed");
+  }
+  b->stream = b->own_stream;
+
+  // validate groups, lay out replica words
+  size_t words_total = 0;
+  int seg = 0, rep = 0;
+  for (int g = 0; g < n_groups; ++g) {
+    const vg_replica_group& rg = groups[g];
+    const vg_lattice_desc& L = rg.lattice;
+    const bool is3d = L.pbc_x && L.pbc_y && L.pbc_z;
+    const bool is2d = L.pbc_x && L.pbc_y && !L.pbc_z && L.nz == 1;
+    if (L.cell != VG_CELL_SC || !(is3d || is2d) || L.nx < 2 || L.ny < 2 || L.nx % 2 || L.ny % 2 ||
+        (is3d && (L.nz < 2 || L.nz % 2))) {
+      bdestroy(b);
+      return bfail(nullptr, VG_ERR_UNSUPPORTED,
+                   "batched groups need an sc lattice with even extents >= 2, periodic on every axis or 2D "
+                   "(nz = 1, open z)");
+    }
+    if (rg.n_replicas < 32 || rg.n_replicas % 32 || rg.n_replicas > 1024 || !rg.temperatures) {
+      bdestroy(b);
+      return bfail(nullptr, VG_ERR_INVALID_ARG, "n_replicas must be a multiple of 32 in [32, 1024] with temperatures");
+    }
+    const double n = (double)L.nx * L.ny * L.nz;
+    if (n > 2147483647.0) {
+      bdestroy(b);
+      return bfail(nullptr, VG_ERR_UNSUPPORTED, "lattice has more than 2^31-1 sites");
+    }
+    GroupHost G;
+    G.lat = L;
+    G.n_rep = rg.n_replicas;
+    G.n = (long long)L.nx * L.ny * L.nz;
+    G.z = is3d ? 6 : 4;
+    G.seg0 = seg;
+    G.rep_off = rep;
+    G.temps.assign(rg.temperatures, rg.temperatures + rg.n_replicas);
+    for (double t : G.temps)
+      if (!(t > 0.0) || !std::isfinite(t)) {
+        bdestroy(b);
+        return bfail(nullptr, VG_ERR_INVALID_ARG, "temperatures must be positive and finite");
+      }
+    G.nd = 0;
+    for (int na = 0; na <= G.z; ++na)
+      if (2.0 * J * (double)(G.z - 2 * na) > 0.0 && G.nd < 4) G.dn[G.nd++] = na;
+    b->groups.push_back(G);
+    seg += G.n_rep / 32;
+    rep += G.n_rep;
+    words_total += (size_t)(G.n_rep / 32) * (size_t)G.n;
+    b->replica_sites += (long long)G.n_rep * G.n;
+  }
+  b->total_rep = rep;
+  int rc = balloc(b, &b->d_spins, words_total);
+  size_t off = 0;
+  for (auto& G : b->groups) {
+    const uint32_t nc = (uint32_t)(G.n / 2);
+    for (int w = 0; w < G.n_rep / 32 && !rc; ++w) {
+      MscSeg s{};
+      s.cls[0] = b->d_spins + off;
+      s.cls[1] = b->d_spins + off + nc;
+      off += 2 * (size_t)nc;
+      s.n_c = nc;
+      s.Hx = G.lat.nx / 2;
+      s.Ly = G.lat.ny;
+      s.Lz = G.lat.nz;
+      s.dim3 = G.z == 6;
+      s.fHx = make_fastdiv((uint32_t)s.Hx);
+      s.fLy = make_fastdiv((uint32_t)s.Ly);
+      s.fLx = make_fastdiv((uint32_t)G.lat.nx);
+      s.word_id = (uint32_t)b->segs.size();
+      s.group = (int)(&G - &b->groups[0]);
+      s.nd = G.nd;
+      for (int q = 0; q < 4; ++q) s.dn[q] = q < G.nd ? G.dn[q] : 0;
+      s.rep0 = G.rep_off + 32 * w;
+      const int per = 256 * kWordsPerThread;
+      const int nbl = (int)((nc + per - 1) / per);
+      for (int k = 0; k < nbl; ++k) b->blocks.push_back(make_int2((int)b->segs.size(), k * per));
+      b->segs.push_back(s);
+    }
+  }
+  if (!rc) rc = balloc(b, &b->d_segs, b->segs.size());
+  if (!rc) rc = balloc(b, &b->d_blocks, b->blocks.size());
+  if (!rc) rc = balloc(b, &b->d_tabs, b->segs.size() * kTabWords);
+  if (!rc) rc = balloc(b, &b->d_groups, b->groups.size());
+  if (!rc) rc = balloc(b, &b->d_dev, 1);
+  if (!rc) rc = balloc(b, &b->d_flag, 1);
+  std::vector<MscGroupDev> gdev;
+  for (auto& G : b->groups) {
+    if (rc) break;
+    if ((rc = balloc(b, &G.d_beta, G.n_rep))) break;
+    if ((rc = balloc(b, &G.d_thr, (size_t)G.n_rep * (G.z + 1)))) break;
+    if ((rc = balloc(b, &G.d_tau, G.n_rep))) break;
+    if ((rc = balloc(b, &G.d_rep_at, G.n_rep))) break;
+    if ((rc = balloc(b, &G.d_acc, G.n_rep))) break;
+    if ((rc = balloc(b, &G.d_att, G.n_rep))) break;
+    std::vector<double> beta(G.n_rep);
+    std::vector<unsigned long long> thr((size_t)G.n_rep * (G.z + 1));
+    std::vector<int> ident(G.n_rep);
+    for (int i = 0; i < G.n_rep; ++i) {
+      const double T = std::max(G.temps[i], 2.220446049250313e-16);
+      beta[i] = 1.0 / G.temps[i];
+      ident[i] = i;
+      for (int na = 0; na <= G.z; ++na) {
+        // the Ising threshold rule for dE = 2 J (z - 2 n_anti)
+        const double de = 2.0 * J * (double)(G.z - 2 * na);
+        unsigned long long th;
+        if (de <= 0.0) {
+          th = 1ull << 32;
+        } else {
+          const double x = std::ceil(std::exp(-de / T) * 4294967296.0);
+          th = x >= 4294967296.0 ? (1ull << 32) : x <= 0.0 ? 0ull : (unsigned long long)x;
+        }
+        thr[(size_t)i * (G.z + 1) + na] = th;
+      }
+    }
+    cudaMemcpy(G.d_beta, beta.data(), sizeof(double) * G.n_rep, cudaMemcpyHostToDevice);
+    cudaMemcpy(G.d_thr, thr.data(), sizeof(unsigned long long) * thr.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(G.d_tau, ident.data(), sizeof(int) * G.n_rep, cudaMemcpyHostToDevice);
+    cudaMemcpy(G.d_rep_at, ident.data(), sizeof(int) * G.n_rep, cudaMemcpyHostToDevice);
+    cudaMemset(G.d_acc, 0, sizeof(unsigned long long) * G.n_rep);
+    cudaMemset(G.d_att, 0, sizeof(unsigned long long) * G.n_rep);
+    MscGroupDev d{};
+    d.n_rep = G.n_rep;
+    d.rep_off = G.rep_off;
+    d.seg0 = G.seg0;
+    d.z = G.z;
+    d.J = J;
+    d.nbonds = (double)G.z * (double)G.n / 2.0;
+    d.beta = G.d_beta;
+    d.thr = G.d_thr;
+    d.tau = G.d_tau;
+    d.rep_at = G.d_rep_at;
+    d.accepted = G.d_acc;
+    d.attempted = G.d_att;
+    gdev.push_back(d);
+  }
+  if (rc) {
+    const std::string e = b->err;
+    bdestroy(b);
+    return bfail(nullptr, rc, e);
+  }
+  cudaMemcpy(b->d_segs, b->segs.data(), sizeof(MscSeg) * b->segs.size(), cudaMemcpyHostToDevice);
+  cudaMemcpy(b->d_blocks, b->blocks.data(), sizeof(int2) * b->blocks.size(), cudaMemcpyHostToDevice);
+  cudaMemcpy(b->d_groups, gdev.data(), sizeof(MscGroupDev) * gdev.size(), cudaMemcpyHostToDevice);
+  MscDev d0{0, 0, 0, 0};
+  cudaMemcpy(b->d_dev, &d0, sizeof(d0), cudaMemcpyHostToDevice);
+  cudaMemset(b->d_spins, 0xFF, sizeof(uint32_t) * words_total);  // all up until initialised
+  msc_tabs_kernel<<<(int)b->groups.size(), 256, 0, b->stream>>>(b->d_groups, b->d_segs, b->d_tabs);
+  const cudaError_t e = cudaStreamSynchronize(b->stream);
+  if (e != cudaSuccess) {
+    bdestroy(b);
+    return bfail(nullptr, VG_ERR_CUDA, std::string("batch set-up: ") + cudaGetErrorString(e));
+  }
+  *out = b;
+  return VG_OK;
+}
+
+int vg_batch_destroy(vg_batch* b) {
+  if (!b) return VG_ERR_INVALID_ARG;
+  bdestroy(b);
+  return VG_OK;
+}
+
+const char* vg_batch_last_error(const vg_batch* b) { return b ? b->err.c_str() : ""; }
+
+int vg_batch_get_info(const vg_batch* b, vg_batch_info* o) {
+  if (!b || !o) return VG_ERR_INVALID_ARG;
+  o->n_groups = (int32_t)b->groups.size();
+  o->total_replicas = b->total_rep;
+  o->replica_words = (int32_t)b->segs.size();
+  o->replica_sites = b->replica_sites;
+  o->sweeps_per_round = b->every;
+  o->sweep_index = b->sweep;
+  o->round_index = b->round;
+  o->graph = b->graph != nullptr;
+  return VG_OK;
+}
+
+int vg_batch_get_stream(const vg_batch* b, void** s) {
+  if (!b || !s) return VG_ERR_INVALID_ARG;
+  *s = (void*)b->stream;
+  return VG_OK;
+}
+
+int vg_batch_init_random(vg_batch* b) {
+  if (!b) return VG_ERR_INVALID_ARG;
+  VG_BCUDA(b, cudaSetDevice(b->device));
+  msc_init<<<dim3(64, (unsigned)b->segs.size()), 256, 0, b->stream>>>(b->d_segs, (int)b->segs.size(), b->ks);
+  VG_BCUDA(b, cudaGetLastError());
+  VG_BCUDA(b, cudaStreamSynchronize(b->stream));
+  return VG_OK;
+}
+
+int vg_batch_run_async(vg_batch* b, uint64_t rounds) {
+  if (!b) return VG_ERR_INVALID_ARG;
+  VG_BCUDA(b, cudaSetDevice(b->device));
+  int rc = ensure_ring(b, std::max<uint64_t>(rounds, 1));
+  if (rc) return rc;
+  VG_BCUDA(b, cudaMemsetAsync(b->d_obs, 0, sizeof(unsigned long long) * rounds * b->total_rep * 2, b->stream));
+  MscDev d{(uint32_t)b->sweep, b->round, b->round, 0};
+  VG_BCUDA(b, cudaMemcpyAsync(b->d_dev, &d, sizeof(d), cudaMemcpyHostToDevice, b->stream));
+  if (!b->graph) {  // capture one round once
+    cudaGraph_t g = nullptr;
+    bool ok = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if (ok) {
+      const int erc = enqueue_round(b);
+      ok = cudaStreamEndCapture(b->stream, &g) == cudaSuccess && erc == VG_OK;
+    }
+    if (ok && cudaGraphInstantiate(&b->graph, g, 0) != cudaSuccess) {
+      b->graph = nullptr;
+      ok = false;
+    }
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();  // a failed capture falls back to direct launches
+  }
+  for (uint64_t r = 0; r < rounds; ++r) {
+    if (b->graph) {
+      VG_BCUDA(b, cudaGraphLaunch(b->graph, b->stream));
+    } else {
+      if ((rc = enqueue_round(b))) return rc;
+    }
+  }
+  b->sweep += rounds * (uint64_t)b->every;
+  b->round += (uint32_t)rounds;
+  b->last_rounds = rounds;
+  return VG_OK;
+}
+
+int vg_batch_synchronize(vg_batch* b) {
+  if (!b) return VG_ERR_INVALID_ARG;
+  VG_BCUDA(b, cudaStreamSynchronize(b->stream));
+  return VG_OK;
+}
+
+int vg_batch_run(vg_batch* b, uint64_t rounds) {
+  int rc = vg_batch_run_async(b, rounds);
+  if (rc) return rc;
+  return vg_batch_synchronize(b);
+}
+
+int vg_batch_observables(vg_batch* b, uint64_t round, int64_t* counts, int32_t* tau) {
+  if (!b) return VG_ERR_INVALID_ARG;
+  if (round >= b->last_rounds) return bfail(b, VG_ERR_INVALID_ARG, "round not in the last run");
+  VG_BCUDA(b, cudaStreamSynchronize(b->stream));
+  if (counts)
+    VG_BCUDA(b, cudaMemcpy(counts, b->d_obs + (size_t)round * b->total_rep * 2, sizeof(int64_t) * b->total_rep * 2,
+                           cudaMemcpyDeviceToHost));
+  if (tau)
+    VG_BCUDA(b, cudaMemcpy(tau, b->d_tau_ring + (size_t)round * b->total_rep, sizeof(int32_t) * b->total_rep,
+                           cudaMemcpyDeviceToHost));
+  return VG_OK;
+}
+
+int vg_batch_ladder(vg_batch* b, int32_t group, int32_t* tau) {
+  if (!b || !tau || group < 0 || group >= (int)b->groups.size()) return VG_ERR_INVALID_ARG;
+  VG_BCUDA(b, cudaStreamSynchronize(b->stream));
+  const GroupHost& G = b->groups[group];
+  VG_BCUDA(b, cudaMemcpy(tau, G.d_tau, sizeof(int) * G.n_rep, cudaMemcpyDeviceToHost));
+  return VG_OK;
+}
+
+int vg_batch_swap_stats(vg_batch* b, int32_t group, int64_t* accepted, int64_t* attempted) {
+  if (!b || group < 0 || group >= (int)b->groups.size()) return VG_ERR_INVALID_ARG;
+  VG_BCUDA(b, cudaStreamSynchronize(b->stream));
+  const GroupHost& G = b->groups[group];
+  if (accepted) VG_BCUDA(b, cudaMemcpy(accepted, G.d_acc, sizeof(int64_t) * G.n_rep, cudaMemcpyDeviceToHost));
+  if (attempted) VG_BCUDA(b, cudaMemcpy(attempted, G.d_att, sizeof(int64_t) * G.n_rep, cudaMemcpyDeviceToHost));
+  return VG_OK;
+}
+
+int vg_batch_get_replica(vg_batch* b, int32_t group, int32_t replica, int8_t* spins) {
+  if (!b || !spins) return VG_ERR_INVALID_ARG;
+  MscSeg sg;
+  uint32_t lane;
+  int rc = find_replica(b, group, replica, &sg, &lane);
+  if (rc) return rc;
+  const long long n = 2LL * sg.n_c;
+  if ((rc = ensure_stage(b, n))) return rc;
+  msc_get<<<256, 256, 0, b->stream>>>(sg, lane, b->d_stage);
+  VG_BCUDA(b, cudaGetLastError());
+  VG_BCUDA(b, cudaMemcpyAsync(spins, b->d_stage, (size_t)n, cudaMemcpyDeviceToHost, b->stream));
+  VG_BCUDA(b, cudaStreamSynchronize(b->stream));
+  return VG_OK;
+}
+
+int vg_batch_set_replica(vg_batch* b, int32_t group, int32_t replica, const int8_t* spins) {
+  if (!b || !spins) return VG_ERR_INVALID_ARG;
+  MscSeg sg;
+  uint32_t lane;
+  int rc = find_replica(b, group, replica, &sg, &lane);
+  if (rc) return rc;
+  const long long n = 2LL * sg.n_c;
+  if ((rc = ensure_stage(b, n))) return rc;
+  VG_BCUDA(b, cudaMemcpyAsync(b->d_stage, spins, (size_t)n, cudaMemcpyHostToDevice, b->stream));
+  VG_BCUDA(b, cudaMemsetAsync(b->d_flag, 0, sizeof(int), b->stream));
+  msc_set<<<256, 256, 0, b->stream>>>(sg, lane, b->d_stage, b->d_flag);
+  VG_BCUDA(b, cudaGetLastError());
+  int flag = 0;
+  VG_BCUDA(b, cudaMemcpyAsync(&flag, b->d_flag, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+  VG_BCUDA(b, cudaStreamSynchronize(b->stream));
+  if (flag) return bfail(b, VG_ERR_INVALID_ARG, "Ising spins must be +1 or -1");
+  return VG_OK;
+}
+
+}  // extern "C"

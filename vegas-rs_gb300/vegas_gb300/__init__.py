@@ -28,7 +28,7 @@ from ._abi import (CELL_BCC, CELL_FCC, CELL_SC, FP32, FP64, PATH_AUTO, PATH_GENE
 __all__ = [
     "Lattice", "Exchange", "UniaxialAnisotropy", "Zeeman", "Gauge", "CubicAnisotropy", "hamiltonian",
     "Engine", "Sums", "VegasGpuError", "lib", "SPIN_ISING", "SPIN_HEISENBERG", "PROPOSE_FLIP",
-    "PROPOSE_RANDOM", "PATH_AUTO", "PATH_GENERIC", "PATH_STRUCTURED", "FP32", "FP64",
+    "PROPOSE_RANDOM", "PATH_AUTO", "PATH_GENERIC", "PATH_STRUCTURED", "FP32", "FP64", "Batch",
 ]
 
 _lib = None
@@ -311,6 +311,104 @@ class Engine:
         e, m = C.c_double(), C.c_double()
         _check(lib().vg_energy_from_sums(self._h, C.byref(s), C.byref(e), C.byref(m)), self._h)
         return e.value, m.value
+
+
+class Batch:
+    """Replica groups of multi-spin-coded Ising lattices with on-device replica exchange.
+
+    groups: list of (Lattice, temperatures); each group's replica count is
+    len(temperatures) (a multiple of 32).  One round = sweeps_per_round
+    sweeps, then per-replica measurement and (if exchange) ladder swaps.
+    """
+
+    def __init__(self, groups, J: float = 1.0, seed: int = 0, sweeps_per_round: int = 10, exchange: bool = True):
+        L = lib()
+        self._temps = [np.ascontiguousarray(t, dtype=np.float64) for _, t in groups]
+        arr = (_abi.ReplicaGroup * len(groups))()
+        for k, (lat, _) in enumerate(groups):
+            arr[k] = _abi.ReplicaGroup(lat.desc(), self._temps[k].size,
+                                       self._temps[k].ctypes.data_as(C.POINTER(C.c_double)))
+        h = C.c_void_p()
+        rc = L.vg_batch_create(arr, len(groups), J, C.c_uint64(seed), sweeps_per_round, int(exchange), C.byref(h))
+        if rc:
+            raise VegasGpuError(rc, L.vg_last_error(None).decode())
+        self._h = h
+        self.lattices = [lat for lat, _ in groups]
+        self.J = J
+
+    def _chk(self, rc):
+        if rc:
+            raise VegasGpuError(rc, lib().vg_batch_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().vg_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def info(self) -> _abi.BatchInfo:
+        i = _abi.BatchInfo()
+        self._chk(lib().vg_batch_get_info(self._h, C.byref(i)))
+        return i
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        self._chk(lib().vg_batch_get_stream(self._h, C.byref(s)))
+        return s.value or 0
+
+    def init_random(self):
+        self._chk(lib().vg_batch_init_random(self._h))
+
+    def run(self, rounds: int):
+        self._chk(lib().vg_batch_run(self._h, C.c_uint64(rounds)))
+
+    def run_async(self, rounds: int):
+        self._chk(lib().vg_batch_run_async(self._h, C.c_uint64(rounds)))
+
+    def synchronize(self):
+        self._chk(lib().vg_batch_synchronize(self._h))
+
+    def observables(self, round_index: int):
+        n = self.info().total_replicas
+        counts = np.zeros((n, 2), dtype=np.int64)
+        tau = np.zeros(n, dtype=np.int32)
+        self._chk(lib().vg_batch_observables(self._h, C.c_uint64(round_index),
+                                             counts.ctypes.data_as(C.POINTER(C.c_int64)),
+                                             tau.ctypes.data_as(C.POINTER(C.c_int32))))
+        return counts, tau
+
+    def ladder(self, group: int) -> np.ndarray:
+        out = np.zeros(self._temps[group].size, dtype=np.int32)
+        self._chk(lib().vg_batch_ladder(self._h, group, out.ctypes.data_as(C.POINTER(C.c_int32))))
+        return out
+
+    def swap_stats(self, group: int):
+        n = self._temps[group].size
+        acc = np.zeros(n, dtype=np.int64)
+        att = np.zeros(n, dtype=np.int64)
+        self._chk(lib().vg_batch_swap_stats(self._h, group, acc.ctypes.data_as(C.POINTER(C.c_int64)),
+                                            att.ctypes.data_as(C.POINTER(C.c_int64))))
+        return acc, att
+
+    def get_replica(self, group: int, replica: int) -> np.ndarray:
+        out = np.empty(self.lattices[group].n_sites, dtype=np.int8)
+        self._chk(lib().vg_batch_get_replica(self._h, group, replica, out.ctypes.data_as(C.POINTER(C.c_int8))))
+        return out
+
+    def set_replica(self, group: int, replica: int, spins: np.ndarray):
+        a = np.ascontiguousarray(spins, dtype=np.int8)
+        self._chk(lib().vg_batch_set_replica(self._h, group, replica, a.ctypes.data_as(C.POINTER(C.c_int8))))
 
 
 def device_count() -> int:

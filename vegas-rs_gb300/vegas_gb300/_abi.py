@@ -52,6 +52,16 @@ class Info(C.Structure):
                 ("sweep_index", C.c_uint64)]
 
 
+class ReplicaGroup(C.Structure):
+    _fields_ = [("lattice", LatticeDesc), ("n_replicas", C.c_int32), ("temperatures", C.POINTER(C.c_double))]
+
+
+class BatchInfo(C.Structure):
+    _fields_ = [("n_groups", C.c_int32), ("total_replicas", C.c_int32), ("replica_words", C.c_int32),
+                ("sweeps_per_round", C.c_int32), ("replica_sites", C.c_int64), ("sweep_index", C.c_uint64),
+                ("round_index", C.c_uint32), ("graph", C.c_int32)]
+
+
 # symbol -> (restype, argtypes); the list the header declares
 P = C.POINTER
 SIGNATURES = {
@@ -82,6 +92,21 @@ SIGNATURES = {
     "vg_total_energy": (C.c_int, [C.c_void_p, P(C.c_double)]),
     "vg_magnetization": (C.c_int, [C.c_void_p, P(C.c_double), P(C.c_double)]),
     "vg_energy_from_sums": (C.c_int, [C.c_void_p, P(Sums), P(C.c_double), P(C.c_double)]),
+    "vg_batch_create": (C.c_int, [P(ReplicaGroup), C.c_int32, C.c_double, C.c_uint64, C.c_int32, C.c_int32,
+                                  P(C.c_void_p)]),
+    "vg_batch_destroy": (C.c_int, [C.c_void_p]),
+    "vg_batch_last_error": (C.c_char_p, [C.c_void_p]),
+    "vg_batch_get_info": (C.c_int, [C.c_void_p, P(BatchInfo)]),
+    "vg_batch_get_stream": (C.c_int, [C.c_void_p, P(C.c_void_p)]),
+    "vg_batch_init_random": (C.c_int, [C.c_void_p]),
+    "vg_batch_run": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "vg_batch_run_async": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "vg_batch_synchronize": (C.c_int, [C.c_void_p]),
+    "vg_batch_observables": (C.c_int, [C.c_void_p, C.c_uint64, P(C.c_int64), P(C.c_int32)]),
+    "vg_batch_ladder": (C.c_int, [C.c_void_p, C.c_int32, P(C.c_int32)]),
+    "vg_batch_swap_stats": (C.c_int, [C.c_void_p, C.c_int32, P(C.c_int64), P(C.c_int64)]),
+    "vg_batch_get_replica": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, P(C.c_int8)]),
+    "vg_batch_set_replica": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, P(C.c_int8)]),
     "vg_ising_sc_sweeps_noalloc": (C.c_int, [P(LatticeDesc), C.c_double, C.c_double, C.c_double, C.c_uint64,
                                              C.c_uint32, C.c_uint64, C.c_uint64, C.c_void_p, C.c_void_p,
                                              C.c_void_p, C.c_void_p]),
