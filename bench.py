@@ -168,6 +168,41 @@ def run_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
+def run_batched(V, torch, args):
+    """The batched form: 256 replicas in four size groups, multi-spin coded 32 per
+    word, replica exchange every 10 sweeps, each round one CUDA graph launch."""
+    import numpy as np
+
+    t2 = np.geomspace(2.0, 2.6, 64)
+    t3 = np.geomspace(4.2, 4.8, 64)
+    groups = [(V.Lattice.sc(64, 64, 1, pbc=(True, True, False)), t2),
+              (V.Lattice.sc(512, 512, 1, pbc=(True, True, False)), t2),
+              (V.Lattice.sc(32, 32, 32), t3), (V.Lattice.sc(128, 128, 128), t3)]
+    rounds = 20  # 200 sweeps per step, as the plain path
+    with V.Batch(groups, J=1.0, seed=SEED, sweeps_per_round=10, exchange=True) as b:
+        b.init_random()
+        for _ in range(max(args.warmup, 1)):
+            b.run(rounds)
+        s = torch.cuda.ExternalStream(b.stream())
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        for a, c in ev:
+            a.record(s)
+            b.run_async(rounds)
+            c.record(s)
+        b.synchronize()
+        ms = sum(a.elapsed_time(c) for a, c in ev)
+        info = b.info()
+        flips = float(info.replica_sites) * 10 * rounds * args.steps
+        acc, att = b.swap_stats(3)
+    return {"value": flips / (ms * 1e6), "unit": "flips/ns", "ms_per_step": ms / args.steps,
+            "replicas": int(info.total_replicas), "replica_sites": int(info.replica_sites),
+            "sweeps_per_step": 10 * rounds, "graph": bool(info.graph),
+            "workload": "256 replicas: 64 x 2D 64^2, 64 x 2D 512^2 (T 2.0-2.6), 64 x 3D 32^3, 64 x 3D 128^3 "
+                        "(T 4.2-4.8), geometric ladders, multi-spin coded 32 per word, exchange every 10 sweeps",
+            "bytes_per_flip": 0.375,
+            "swap_acceptance_3d128": float(acc[:-1].sum() / max(att[:-1].sum(), 1))}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -176,6 +211,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--lattice", type=int, default=L)
+    ap.add_argument("--no-batched", action="store_true")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -279,6 +315,10 @@ def main():
     lib.vg_host_free(hbuf)
     lib.vg_host_free(obuf)
 
+    batched = None
+    if not args.no_batched:
+        batched = run_batched(V, torch, args)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, dt = cpu_baseline_sample(threads=1, sweeps=2)
@@ -307,6 +347,8 @@ def main():
                     "d2h_bytes_per_step": N + 16 * SWEEPS_PER_STEP},
             "gpu_launches": launches_per_step * args.steps,
             "cpu_baseline": cpu,
+            "batched": batched,
+            "batched_vs_plain": (batched["value"] / value) if batched else None,
             "clocks": clk.summary(),
             "wall_s": wall,
             "sweep_ms": sweep_ms,
