@@ -54,8 +54,12 @@ enum vg_unit_cell { VG_CELL_SC = 0, VG_CELL_BCC = 1, VG_CELL_FCC = 2 };
 /* FLIP: MetropolisFlipIntegrator (src/integrator.rs:99-138).
  * RANDOM: MetropolisIntegrator, proposal Spin::rand (src/integrator.rs:56-92). */
 enum vg_proposal { VG_PROPOSE_FLIP = 0, VG_PROPOSE_RANDOM = 1 };
-/* Kernel family.  AUTO picks STRUCTURED when the lattice allows it. */
-enum vg_path { VG_PATH_AUTO = 0, VG_PATH_GENERIC = 1, VG_PATH_STRUCTURED = 2 };
+/* Kernel family.  AUTO picks RESIDENT for Ising lattices of at most 8192
+ * sites that admit STRUCTURED, else STRUCTURED when the lattice allows it,
+ * else GENERIC.  RESIDENT keeps the checkerboard layout of STRUCTURED in one
+ * thread block's shared memory and runs all sweeps of a call in one launch
+ * (Ising, at most 65536 sites); results are identical across paths. */
+enum vg_path { VG_PATH_AUTO = 0, VG_PATH_GENERIC = 1, VG_PATH_STRUCTURED = 2, VG_PATH_RESIDENT = 3 };
 enum vg_precision { VG_FP32 = 0, VG_FP64 = 1 };
 
 /* Lattice::sc/bcc/fcc(1.0).expand(nx, ny, nz) with drop_x/y/z on the open

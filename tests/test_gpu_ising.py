@@ -5,11 +5,13 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 CASES = [
-    # cell, extents, pbc, expected path
-    ("sc", (32, 4, 4), (1, 1, 1), "structured"),
-    ("sc", (32, 32, 1), (1, 1, 0), "structured"),   # 2D square lattice, open z
-    ("sc", (64, 6, 5), (1, 1, 0), "structured"),
-    ("sc", (32, 5, 4), (0, 0, 1), "structured"),    # open x and y boundaries
+    # cell, extents, pbc, expected path (AUTO: small checkerboard lattices run resident)
+    ("sc", (32, 4, 4), (1, 1, 1), "resident"),
+    ("sc", (32, 32, 1), (1, 1, 0), "resident"),     # 2D square lattice, open z
+    ("sc", (64, 6, 5), (1, 1, 0), "resident"),
+    ("sc", (32, 5, 4), (0, 0, 1), "resident"),      # open x and y boundaries
+    ("sc", (64, 16, 10), (1, 1, 1), "structured"),
+    ("sc", (96, 18, 6), (1, 0, 1), "structured"),
     ("sc", (16, 4, 4), (1, 1, 1), "generic"),       # x/2 not a multiple of 16
     ("sc", (33, 4, 4), (1, 1, 1), "generic"),       # odd periodic cycle: greedy colouring
     ("bcc", (4, 4, 4), (1, 1, 1), "generic"),
@@ -28,7 +30,7 @@ def _engine(V, cell, ext, pbc, ham, seed, **kw):
 def test_flip_sweeps_bit_exact(V, O, cell, ext, pbc, path):
     seed, J, T, n = 1234, 1.0, 3.2, 6
     with _engine(V, cell, ext, pbc, V.hamiltonian(V.Exchange(J)), seed) as eng:
-        want = V.PATH_STRUCTURED if path == "structured" else V.PATH_GENERIC
+        want = {"structured": V.PATH_STRUCTURED, "generic": V.PATH_GENERIC, "resident": V.PATH_RESIDENT}[path]
         assert eng.info().path == want
         eng.init_random()
         g = O.Graph(O.lattice(cell, *ext, pbc))
@@ -42,7 +44,7 @@ def test_flip_sweeps_bit_exact(V, O, cell, ext, pbc, path):
         np.testing.assert_array_equal(M, np.abs(obs[:, 1]).astype(float))
 
 
-@pytest.mark.parametrize("cell,ext,pbc,path", CASES[:2] + CASES[4:7])
+@pytest.mark.parametrize("cell,ext,pbc,path", CASES[:2] + CASES[4:9])
 def test_random_proposal_and_field_bit_exact(V, O, cell, ext, pbc, path):
     """MetropolisIntegrator (random +-1 proposal) with Exchange + Zeeman, field Down."""
     seed, J, T, mag, n = 99, 0.7, 2.1, 0.35, 5
@@ -62,17 +64,22 @@ def test_random_proposal_and_field_bit_exact(V, O, cell, ext, pbc, path):
         np.testing.assert_array_equal(M, np.abs(m))
 
 
-def test_generic_and_structured_paths_agree(V):
-    H = V.hamiltonian(V.Exchange(1.0))
+@pytest.mark.parametrize("proposal", [0, 1])
+@pytest.mark.parametrize("ext,pbc", [((64, 8, 6), (1, 1, 1)), ((32, 32, 1), (1, 1, 0)), ((32, 6, 5), (0, 1, 0))])
+def test_all_paths_agree(V, ext, pbc, proposal):
+    """Grid checkerboard, generic ELL and resident shared-memory kernels draw identical numbers."""
+    H = V.hamiltonian(V.Exchange(1.0), V.Zeeman())
     out = []
-    for path in (V.PATH_STRUCTURED, V.PATH_GENERIC):
-        with _engine(V, "sc", (64, 8, 6), (1, 1, 1), H, 5, path=path) as eng:
+    for path in (V.PATH_STRUCTURED, V.PATH_GENERIC, V.PATH_RESIDENT):
+        with _engine(V, "sc", ext, pbc, H, 5, path=path, proposal=proposal) as eng:
+            assert eng.info().path == path
             eng.init_random()
-            eng.set_thermostat(4.4)
+            eng.set_thermostat(2.9, (0, 0, 1), 0.2)
             E, M = eng.sweeps(20)
             out.append((eng.get_state(), E, M))
-    assert np.array_equal(out[0][0], out[1][0])
-    assert np.array_equal(out[0][1], out[1][1]) and np.array_equal(out[0][2], out[1][2])
+    for o in out[1:]:
+        assert np.array_equal(out[0][0], o[0])
+        assert np.array_equal(out[0][1], o[1]) and np.array_equal(out[0][2], o[2])
 
 
 def test_resume_from_sweep_index(V):

@@ -41,7 +41,7 @@ def test_noalloc_matches_context_api_on_two_calls(V):
     desc = lat.desc()
     seed = 11
     H = V.hamiltonian(V.Exchange(1.0), V.Zeeman())
-    with V.Engine(lat, H, spin=V.SPIN_ISING, seed=seed) as eng:
+    with V.Engine(lat, H, spin=V.SPIN_ISING, seed=seed, path=V.PATH_STRUCTURED) as eng:
         assert eng.info().path == V.PATH_STRUCTURED
         eng.init_random()
         s0 = eng.get_state()

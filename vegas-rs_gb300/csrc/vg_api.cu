@@ -375,6 +375,8 @@ __global__ void reduce_rows<long long>(const long long* __restrict__ part, long 
 constexpr int kChunk = 64;  // sweeps per reduction launch
 
 bool is_ising(const vg_ctx* c) { return c->opt.spin_kind == VG_SPIN_ISING; }
+// the checkerboard class layout (structured grid kernels or the resident kernel)
+bool sc_layout(const vg_ctx* c) { return c->path == VG_PATH_STRUCTURED || c->path == VG_PATH_RESIDENT; }
 bool fp64(const vg_ctx* c) { return c->opt.precision == VG_FP64; }
 size_t real_size(const vg_ctx* c) { return fp64(c) ? 8 : 4; }
 
@@ -447,7 +449,7 @@ IsingTable ising_table(const vg_ctx* c) {
     }
   // byte tables for lattices whose sites all have the same neighbour count
   t.zeff = -1;
-  if (c->path == VG_PATH_STRUCTURED) {
+  if (sc_layout(c)) {
     const int ext[3] = {c->lat.nx, c->lat.ny, c->lat.nz};
     const int per[3] = {c->lat.pbc_x, c->lat.pbc_y, c->lat.pbc_z};
     int zeff = 0;
@@ -527,6 +529,23 @@ int ensure_pinned(vg_ctx* c, size_t doubles) {
   return VG_OK;
 }
 
+IsingScArgs ising_sc_args(const vg_ctx* c) {
+  IsingScArgs a;
+  a.cls[0] = (uint8_t*)c->spin[0][0];
+  a.cls[1] = (uint8_t*)c->spin[1][0];
+  a.Hx = c->lat.nx / 2;
+  a.Ly = c->lat.ny;
+  a.Lz = c->lat.nz;
+  a.G = a.Hx / kIsingGroup;
+  a.groups = (uint32_t)a.G * (uint32_t)a.Ly * (uint32_t)a.Lz;
+  a.pbx = c->lat.pbc_x != 0;
+  a.pby = c->lat.pbc_y != 0;
+  a.pbz = c->lat.pbc_z != 0;
+  a.fG = make_fastdiv((uint32_t)a.G);
+  a.fLy = make_fastdiv((uint32_t)a.Ly);
+  return a;
+}
+
 // One colour pass.  part_row: first partial row of this pass (or null).
 int launch_pass(vg_ctx* c, int colour, bool update, uint64_t sweep, void* part_row) {
   const RngKey key = rng_key(c, sweep);
@@ -534,21 +553,9 @@ int launch_pass(vg_ctx* c, int colour, bool update, uint64_t sweep, void* part_r
   if (is_ising(c)) {
     const IsingTable tab = ising_table(c);
     long long* part = (long long*)part_row;
-    if (c->path == VG_PATH_STRUCTURED) {
-      IsingScArgs a;
-      a.cls[0] = (uint8_t*)c->spin[0][0];
-      a.cls[1] = (uint8_t*)c->spin[1][0];
-      a.Hx = c->lat.nx / 2;
-      a.Ly = c->lat.ny;
-      a.Lz = c->lat.nz;
-      a.G = a.Hx / kIsingGroup;
-      a.groups = (uint32_t)a.G * (uint32_t)a.Ly * (uint32_t)a.Lz;
-      a.pbx = c->lat.pbc_x != 0;
-      a.pby = c->lat.pbc_y != 0;
-      a.pbz = c->lat.pbc_z != 0;
-      a.fG = make_fastdiv((uint32_t)a.G);
-      a.fLy = make_fastdiv((uint32_t)a.Ly);
-      e = launch_ising_sc(a, tab, key, colour, c->opt.proposal, update, part, c->grid, c->tpb, c->stream);
+    if (sc_layout(c)) {
+      e = launch_ising_sc(ising_sc_args(c), tab, key, colour, c->opt.proposal, update, part, c->grid, c->tpb,
+                          c->stream);
     } else {
       IsingGenArgs a;
       a.spin = (uint8_t*)c->spin[0][0];
@@ -564,7 +571,7 @@ int launch_pass(vg_ctx* c, int colour, bool update, uint64_t sweep, void* part_r
     auto run = [&](auto zero) -> cudaError_t {
       using R = decltype(zero);
       const HeisParams<R> P = heis_params<R>(c);
-      if (c->path == VG_PATH_STRUCTURED) {
+      if (sc_layout(c)) {
         HeisScArgs<R> a;
         for (int k = 0; k < 2; ++k) {
           a.x[k] = (R*)c->spin[k][0];
@@ -613,6 +620,20 @@ int launch_reduce(vg_ctx* c, int sweeps, double* out) {
 // Enqueue n sweeps; with measure, per-sweep raw sums land in d_sums[0..n).
 int enqueue(vg_ctx* c, uint64_t n, bool measure) {
   int rc;
+  if (c->path == VG_PATH_RESIDENT) {  // all n sweeps in one launch
+    if (measure && (rc = ensure_sums(c, (size_t)std::max<uint64_t>(n, 1)))) return rc;
+    const IsingScArgs a = ising_sc_args(c);
+    const int tpb = (int)std::min<long long>(1024, ((long long)a.groups * 16 + 31) / 32 * 32);
+    for (uint64_t t0 = 0; t0 < n; t0 += (1u << 30)) {
+      const uint32_t m = (uint32_t)std::min<uint64_t>(n - t0, 1u << 30);
+      const cudaError_t e = launch_ising_resident(a, ising_table(c), rng_key(c, c->sweep + t0), c->opt.proposal, m,
+                                                  measure ? c->d_sums + t0 * kNumSums : nullptr, tpb, c->stream);
+      if (e != cudaSuccess) return cuda_fail(c, e, "resident kernel launch");
+    }
+    c->sweep += n;
+    if (measure) c->last_batch = n;
+    return VG_OK;
+  }
   if (measure) {
     if ((rc = ensure_sums(c, (size_t)std::max<uint64_t>(n, 1)))) return rc;
     if ((rc = ensure_part(c, rows_per_sweep(c) * kChunk))) return rc;
@@ -851,7 +872,7 @@ int vg_ctx_create_ex(const vg_lattice_desc* lat, const vg_hamiltonian_desc* ham,
     return fail(nullptr, VG_ERR_INVALID_ARG, "unknown proposal");
   if (opt->precision != VG_FP32 && opt->precision != VG_FP64)
     return fail(nullptr, VG_ERR_INVALID_ARG, "unknown precision");
-  if (opt->path < VG_PATH_AUTO || opt->path > VG_PATH_STRUCTURED) return fail(nullptr, VG_ERR_INVALID_ARG, "unknown path");
+  if (opt->path < VG_PATH_AUTO || opt->path > VG_PATH_RESIDENT) return fail(nullptr, VG_ERR_INVALID_ARG, "unknown path");
   if (opt->threads_per_block && (opt->threads_per_block % 32 || opt->threads_per_block > 256 ||
                                  opt->threads_per_block < 32))
     return fail(nullptr, VG_ERR_INVALID_ARG, "threads_per_block must be a multiple of 32 in [32, 256]");
@@ -900,9 +921,17 @@ int vg_ctx_create_ex(const vg_lattice_desc* lat, const vg_hamiltonian_desc* ham,
     destroy(c);
     return fail(nullptr, VG_ERR_UNSUPPORTED, "lattice does not admit the structured checkerboard path");
   }
-  c->path = (opt->path == VG_PATH_GENERIC || !sc_ok) ? VG_PATH_GENERIC : VG_PATH_STRUCTURED;
+  const bool res_ok = sc_ok && opt->spin_kind == VG_SPIN_ISING && g.n <= 65536;
+  if (opt->path == VG_PATH_RESIDENT && !res_ok) {
+    destroy(c);
+    return fail(nullptr, VG_ERR_UNSUPPORTED, "the resident path needs an Ising lattice of at most 65536 sites "
+                                             "that admits the checkerboard layout");
+  }
+  if (opt->path == VG_PATH_GENERIC || !sc_ok) c->path = VG_PATH_GENERIC;
+  else if (opt->path == VG_PATH_RESIDENT || (opt->path == VG_PATH_AUTO && res_ok && g.n <= 8192)) c->path = VG_PATH_RESIDENT;
+  else c->path = VG_PATH_STRUCTURED;
 
-  if (c->path == VG_PATH_STRUCTURED) {
+  if (sc_layout(c)) {
     c->ncol = 2;
     c->class_size.assign(2, g.n / 2);
     const size_t per = (size_t)(g.n / 2);
@@ -938,7 +967,7 @@ int vg_ctx_create_ex(const vg_lattice_desc* lat, const vg_hamiltonian_desc* ham,
     items = std::max(items, is_ising(c) ? (nc + 15) / 16 : nc);
   }
   c->grid = launch_grid(c, items);
-  if (is_ising(c) && c->path == VG_PATH_STRUCTURED && opt->blocks_per_sm <= 0) {
+  if (is_ising(c) && sc_layout(c) && opt->blocks_per_sm <= 0) {
     // one wave of resident blocks, each thread walking several 16-site groups
     const bool uniform = ising_table(c).zeff >= 0;
     const long long cap = (long long)c->sm_count * ising_sc_blocks_per_sm(uniform, c->tpb);
@@ -952,13 +981,13 @@ int vg_ctx_create_ex(const vg_lattice_desc* lat, const vg_hamiltonian_desc* ham,
   if (is_ising(c)) {
     for (int k = 0; k < 2; ++k)
       if (c->spin[k][0])
-        cudaMemsetAsync(c->spin[k][0], 1, c->path == VG_PATH_STRUCTURED ? (size_t)(g.n / 2) : (size_t)g.n, c->stream);
+        cudaMemsetAsync(c->spin[k][0], 1, sc_layout(c) ? (size_t)(g.n / 2) : (size_t)g.n, c->stream);
   } else {
     for (int k = 0; k < 2; ++k)
       for (int a = 0; a < 3; ++a)
         if (c->spin[k][a])
           cudaMemsetAsync(c->spin[k][a], 0,
-                          (c->path == VG_PATH_STRUCTURED ? (size_t)(g.n / 2) : (size_t)g.n) * real_size(c), c->stream);
+                          (sc_layout(c) ? (size_t)(g.n / 2) : (size_t)g.n) * real_size(c), c->stream);
   }
   e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) {
@@ -1021,7 +1050,7 @@ int vg_init_random(vg_ctx* c) {
   if (!c) return VG_ERR_INVALID_ARG;
   VG_CUDA(c, cudaSetDevice(c->device));
   const RngKey key = rng_key(c, 0);
-  const int structured = c->path == VG_PATH_STRUCTURED;
+  const int structured = sc_layout(c);
   const ScMap m = sc_map(c);
   if (is_ising(c)) {
     ising_init<<<copy_grid(c, (c->n + 15) / 16), 256, 0, c->stream>>>(c->n, structured, m, (uint8_t*)c->spin[0][0],
@@ -1057,7 +1086,7 @@ int vg_set_state(vg_ctx* c, const void* host, int64_t n) {
   if (rc) return rc;
   VG_CUDA(c, cudaMemcpyAsync(c->d_stage, host, bytes, cudaMemcpyHostToDevice, c->stream));
   VG_CUDA(c, cudaMemsetAsync(c->d_flag, 0, sizeof(int), c->stream));
-  const int structured = c->path == VG_PATH_STRUCTURED;
+  const int structured = sc_layout(c);
   const ScMap m = sc_map(c);
   if (is_ising(c)) {
     ising_import<<<copy_grid(c, n), 256, 0, c->stream>>>((const int8_t*)c->d_stage, n, structured, m,
@@ -1098,7 +1127,7 @@ int vg_get_state(vg_ctx* c, void* host, int64_t n) {
   const size_t bytes = is_ising(c) ? (size_t)n : (size_t)n * 3 * sizeof(double);
   int rc = ensure_stage(c, bytes);
   if (rc) return rc;
-  const int structured = c->path == VG_PATH_STRUCTURED;
+  const int structured = sc_layout(c);
   const ScMap m = sc_map(c);
   if (is_ising(c)) {
     ising_export<<<copy_grid(c, n), 256, 0, c->stream>>>((int8_t*)c->d_stage, n, structured, m,

@@ -22,13 +22,13 @@ from typing import Optional, Sequence, Tuple
 import numpy as np
 
 from . import _abi
-from ._abi import (CELL_BCC, CELL_FCC, CELL_SC, FP32, FP64, PATH_AUTO, PATH_GENERIC, PATH_STRUCTURED,
+from ._abi import (CELL_BCC, CELL_FCC, CELL_SC, FP32, FP64, PATH_AUTO, PATH_GENERIC, PATH_RESIDENT, PATH_STRUCTURED,
                    PROPOSE_FLIP, PROPOSE_RANDOM, SPIN_HEISENBERG, SPIN_ISING, Sums, VegasGpuError)
 
 __all__ = [
     "Lattice", "Exchange", "UniaxialAnisotropy", "Zeeman", "Gauge", "CubicAnisotropy", "hamiltonian",
     "Engine", "Sums", "VegasGpuError", "lib", "SPIN_ISING", "SPIN_HEISENBERG", "PROPOSE_FLIP",
-    "PROPOSE_RANDOM", "PATH_AUTO", "PATH_GENERIC", "PATH_STRUCTURED", "FP32", "FP64", "Batch",
+    "PROPOSE_RANDOM", "PATH_AUTO", "PATH_GENERIC", "PATH_STRUCTURED", "PATH_RESIDENT", "FP32", "FP64", "Batch",
 ]
 
 _lib = None

@@ -15,7 +15,7 @@ VG_OK, VG_ERR_INVALID_ARG, VG_ERR_CUDA, VG_ERR_TIMEOUT, VG_ERR_OOM, VG_ERR_UNSUP
 SPIN_ISING, SPIN_HEISENBERG = 0, 1
 CELL_SC, CELL_BCC, CELL_FCC = 0, 1, 2
 PROPOSE_FLIP, PROPOSE_RANDOM = 0, 1
-PATH_AUTO, PATH_GENERIC, PATH_STRUCTURED = 0, 1, 2
+PATH_AUTO, PATH_GENERIC, PATH_STRUCTURED, PATH_RESIDENT = 0, 1, 2, 3
 FP32, FP64 = 0, 1
 
 
@@ -117,7 +117,9 @@ SIGNATURES = {
 }
 
 
-def load(path: str = LIB_PATH) -> C.CDLL:
+def load(path: str = "") -> C.CDLL:
+    """Load the library (VEGAS_GPU_LIB overrides the in-tree build's path)."""
+    path = path or os.environ.get("VEGAS_GPU_LIB") or LIB_PATH
     if not os.path.exists(path):
         raise RuntimeError(f"{path} is missing: build the CUDA library first (__graft_entry__.build())")
     lib = C.CDLL(path)
