@@ -83,13 +83,32 @@ __device__ __forceinline__ void add_site_sums(R (&acc)[kNumSums], const V3<R>& s
   acc[6] += s.z;
 }
 
-// Thread-level partials in R, block reduction in FP64.
+// Thread partials in R, warp sums in R, then FP64 across the block's warps
+// (a block row of kNumSums doubles).
 template <typename R>
 __device__ __forceinline__ void flush_sums(R (&acc)[kNumSums], double* part) {
-  double v[kNumSums];
+  __shared__ double red[32][kNumSums];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-  for (int i = 0; i < kNumSums; ++i) v[i] = (double)acc[i];
-  block_sum_store(v, part + (long long)blockIdx.x * kNumSums);
+  for (int i = 0; i < kNumSums; ++i) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc[i] += __shfl_down_sync(0xffffffffu, acc[i], o);
+  }
+  if (lane == 0) {
+#pragma unroll
+    for (int i = 0; i < kNumSums; ++i) red[warp][i] = (double)acc[i];
+  }
+  __syncthreads();
+  if (threadIdx.x < kNumSums) {
+    double t = 0.0, c = 0.0;  // Kahan over the warps, in a fixed order
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      const double y = red[w][threadIdx.x] - c;
+      const double u = t + y;
+      c = (u - t) - y;
+      t = u;
+    }
+    part[(size_t)blockIdx.x * kNumSums + threadIdx.x] = t;
+  }
 }
 
 // ------------------------------------------------------------------ sc
@@ -161,6 +180,134 @@ __global__ void __launch_bounds__(256) heis_sc_kernel(const HeisScArgs<R> a, con
   if (MEASURE) flush_sums(acc, part);
 }
 
+// Four consecutive class entries per thread (x extent a multiple of 8):
+// float4 loads of the SoA planes; the x neighbour outside the same float4 is
+// one scalar per plane, as in the Ising checkerboard kernel.
+template <typename R>
+struct Vec4 {
+  R v[4];
+};
+__device__ __forceinline__ Vec4<float> ld4(const float* p) {
+  const float4 t = __ldg(reinterpret_cast<const float4*>(p));
+  return Vec4<float>{{t.x, t.y, t.z, t.w}};
+}
+__device__ __forceinline__ Vec4<double> ld4(const double* p) {
+  const double2 a = __ldg(reinterpret_cast<const double2*>(p)), b = __ldg(reinterpret_cast<const double2*>(p) + 1);
+  return Vec4<double>{{a.x, a.y, b.x, b.y}};
+}
+__device__ __forceinline__ void st4(float* p, const Vec4<float>& v) {
+  *reinterpret_cast<float4*>(p) = make_float4(v.v[0], v.v[1], v.v[2], v.v[3]);
+}
+__device__ __forceinline__ void st4(double* p, const Vec4<double>& v) {
+  reinterpret_cast<double2*>(p)[0] = make_double2(v.v[0], v.v[1]);
+  reinterpret_cast<double2*>(p)[1] = make_double2(v.v[2], v.v[3]);
+}
+
+template <typename R, int C, bool ALLPER, bool MEASURE, bool UPDATE, int PROP>
+__global__ void __launch_bounds__(256) heis_sc4_kernel(const HeisScArgs<R> a, const HeisParams<R> P, const RngKey key,
+                                                       double* __restrict__ part) {
+  R* own[3] = {a.x[C], a.y[C], a.z[C]};
+  const R* oth[3] = {a.x[C ^ 1], a.y[C ^ 1], a.z[C ^ 1]};
+  R acc[kNumSums];
+#pragma unroll
+  for (int i = 0; i < kNumSums; ++i) acc[i] = (R)0;
+  const uint32_t n4 = a.n_c >> 2;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n4; q += stride) {
+    const uint32_t j0 = q << 2;
+    const int row = (int)fdiv(j0, a.fHx);
+    const int h0 = (int)(j0 - (uint32_t)row * a.Hx);
+    const int z = (int)fdiv((uint32_t)row, a.fLy);
+    const int y = row - z * a.Ly;
+    const int p = (y + z + C) & 1;
+    const int rb = row * a.Hx;
+    const int plane = a.Ly * a.Hx;
+    const int rym = y > 0 ? rb - a.Hx : ((ALLPER || a.pby) ? rb + (a.Ly - 1) * a.Hx : -1);
+    const int ryp = y < a.Ly - 1 ? rb + a.Hx : ((ALLPER || a.pby) ? rb - (a.Ly - 1) * a.Hx : -1);
+    const int rzm = z > 0 ? rb - plane : ((ALLPER || a.pbz) ? rb + (a.Lz - 1) * plane : -1);
+    const int rzp = z < a.Lz - 1 ? rb + plane : ((ALLPER || a.pbz) ? rb - (a.Lz - 1) * plane : -1);
+    // x neighbour not inside the float4: h0-1 (p = 0) or h0+4 (p = 1)
+    int xe;
+    bool xok = true;
+    if (p == 0) {
+      xe = h0 > 0 ? rb + h0 - 1 : rb + a.Hx - 1;
+      xok = h0 > 0 || ALLPER || a.pbx;
+    } else {
+      xe = h0 + 4 < a.Hx ? rb + h0 + 4 : rb;
+      xok = h0 + 4 < a.Hx || ALLPER || a.pbx;
+    }
+    Vec4<R> hs[3], S[3];
+#pragma unroll
+    for (int c3 = 0; c3 < 3; ++c3) {
+      const Vec4<R> X0 = ld4(oth[c3] + rb + h0);
+      const R e = xok ? __ldg(oth[c3] + xe) : (R)0;
+      Vec4<R> t = X0;
+      if (p == 0) {
+        t.v[0] += e;
+        t.v[1] += X0.v[0];
+        t.v[2] += X0.v[1];
+        t.v[3] += X0.v[2];
+      } else {
+        t.v[0] += X0.v[1];
+        t.v[1] += X0.v[2];
+        t.v[2] += X0.v[3];
+        t.v[3] += e;
+      }
+      if (rym >= 0) {
+        const Vec4<R> u = ld4(oth[c3] + rym + h0);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) t.v[k] += u.v[k];
+      }
+      if (ryp >= 0) {
+        const Vec4<R> u = ld4(oth[c3] + ryp + h0);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) t.v[k] += u.v[k];
+      }
+      if (rzm >= 0) {
+        const Vec4<R> u = ld4(oth[c3] + rzm + h0);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) t.v[k] += u.v[k];
+      }
+      if (rzp >= 0) {
+        const Vec4<R> u = ld4(oth[c3] + rzp + h0);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) t.v[k] += u.v[k];
+      }
+      hs[c3] = t;
+      S[c3] = ld4(own[c3] + rb + h0);
+    }
+    bool changed = false;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      V3<R> s = {S[0].v[k], S[1].v[k], S[2].v[k]};
+      const V3<R> h = {hs[0].v[k], hs[1].v[k], hs[2].v[k]};
+      if (UPDATE) {
+        const uint4 w = philox_ks(make_uint4(j0 + (uint32_t)k, key.sweep, (kTagHeis << 24) | ((uint32_t)C << 8),
+                                             key.replica),
+                                  key.ks);
+        V3<R> sn;
+        if (heis_update<R, PROP>(s, h, P, w, sn)) {
+          S[0].v[k] = sn.x;
+          S[1].v[k] = sn.y;
+          S[2].v[k] = sn.z;
+          s = sn;
+          changed = true;
+          acc[7] += (R)1;
+        }
+      }
+      if (MEASURE) {
+        const V3<R> low = C == 1 ? h : V3<R>{(R)0, (R)0, (R)0};
+        add_site_sums(acc, s, low, P);
+      }
+    }
+    if (changed) {
+#pragma unroll
+      for (int c3 = 0; c3 < 3; ++c3) st4(own[c3] + rb + h0, S[c3]);
+    }
+  }
+  if (MEASURE) flush_sums(acc, part);
+}
+
 // ------------------------------------------------------------- generic
 template <typename R, int ZT, bool MEASURE, bool UPDATE, int PROP>
 __global__ void __launch_bounds__(256) heis_gen_kernel(const HeisGenArgs<R> a, const HeisParams<R> P, const RngKey key,
@@ -224,10 +371,35 @@ static void sc_go(const HeisScArgs<R>& a, const HeisParams<R>& p, RngKey key, in
   }
 }
 
+template <typename R, int C, bool ALLPER>
+static void sc4_go(const HeisScArgs<R>& a, const HeisParams<R>& p, RngKey key, int proposal, bool update, double* part,
+                   int grid, int tpb, cudaStream_t s) {
+  const bool m = part != nullptr;
+  if (!update) {
+    heis_sc4_kernel<R, C, ALLPER, true, false, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, p, key, part);
+  } else if (proposal == VG_PROPOSE_RANDOM) {
+    if (m) heis_sc4_kernel<R, C, ALLPER, true, true, VG_PROPOSE_RANDOM><<<grid, tpb, 0, s>>>(a, p, key, part);
+    else heis_sc4_kernel<R, C, ALLPER, false, true, VG_PROPOSE_RANDOM><<<grid, tpb, 0, s>>>(a, p, key, part);
+  } else {
+    if (m) heis_sc4_kernel<R, C, ALLPER, true, true, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, p, key, part);
+    else heis_sc4_kernel<R, C, ALLPER, false, true, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, p, key, part);
+  }
+}
+
 template <typename R>
 cudaError_t launch_heis_sc(const HeisScArgs<R>& a, const HeisParams<R>& p, RngKey key, int colour, int proposal,
                            bool update, double* part, int grid, int tpb, cudaStream_t s) {
   const bool allper = a.pbx && a.pby && a.pbz;
+  if (a.Hx % 4 == 0) {  // four sites per thread
+    if (colour == 0) {
+      if (allper) sc4_go<R, 0, true>(a, p, key, proposal, update, part, grid, tpb, s);
+      else sc4_go<R, 0, false>(a, p, key, proposal, update, part, grid, tpb, s);
+    } else {
+      if (allper) sc4_go<R, 1, true>(a, p, key, proposal, update, part, grid, tpb, s);
+      else sc4_go<R, 1, false>(a, p, key, proposal, update, part, grid, tpb, s);
+    }
+    return cudaGetLastError();
+  }
   if (colour == 0) {
     if (allper) sc_go<R, 0, true>(a, p, key, proposal, update, part, grid, tpb, s);
     else sc_go<R, 0, false>(a, p, key, proposal, update, part, grid, tpb, s);
