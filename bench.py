@@ -56,6 +56,12 @@ def ladder():
     return out
 
 
+def aggregate_value(flips_per_rank, world, max_ms):
+    """Whole-job flips/ns: every rank runs its own replica (same work per rank),
+    timed by the slowest rank."""
+    return flips_per_rank * world / (max_ms * 1e6)
+
+
 def peaks():
     try:
         with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
@@ -281,7 +287,7 @@ def main():
         dev_ms = float(t.item())
         dist.barrier()
     flips_rank = float(N) * SWEEPS_PER_STEP * args.steps
-    value = flips_rank * world / (dev_ms * 1e6)
+    value = aggregate_value(flips_rank, world, dev_ms)
 
     # dominant kernel: one colour pass, timed per launch with CUDA events
     pass_ms, sweep_ms = eng.time_passes(50, measure=True)

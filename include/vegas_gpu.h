@@ -98,6 +98,7 @@ typedef struct {
   int32_t threads_per_block;  /* 0 = library default */
   int32_t blocks_per_sm;      /* 0 = library default (grid-stride cap) */
   int32_t device;             /* -1 = current device */
+  int64_t max_device_bytes;   /* 0 = no cap; beyond it allocations fail with VG_ERR_OOM */
 } vg_options;
 
 /* Raw per-sweep lattice sums (FP64), from which every total the reference

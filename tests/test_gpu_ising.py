@@ -157,3 +157,14 @@ def test_acceptance_counts(V):
         n = 32 * 8 * 8
         # at T -> infinity every flip with dE > 0 is accepted with probability ~1
         assert np.all(sums[:, 7] > 0.99 * n)
+
+
+def test_device_memory_cap_reports_oom(V):
+    """Out-of-memory is reported as a status, without exhausting the device."""
+    H = V.hamiltonian(V.Exchange(1.0))
+    with pytest.raises(V.VegasGpuError) as e:
+        V.Engine(V.Lattice.sc(256, 256, 256), H, max_device_bytes=1 << 20)
+    assert e.value.status == 4  # VG_ERR_OOM
+    with _engine(V, "sc", (64, 16, 16), (1, 1, 1), H, 1, max_device_bytes=1 << 26) as eng:
+        eng.init_random()
+        eng.sweeps(2)  # within the cap the context works

@@ -382,6 +382,8 @@ size_t real_size(const vg_ctx* c) { return fp64(c) ? 8 : 4; }
 
 int dalloc(vg_ctx* c, void** p, size_t bytes) {
   if (bytes == 0) bytes = 16;
+  if (c->opt.max_device_bytes > 0 && c->device_bytes + (int64_t)bytes > c->opt.max_device_bytes)
+    return fail(c, VG_ERR_OOM, "device memory cap of " + std::to_string(c->opt.max_device_bytes) + " bytes reached");
   cudaError_t e = cudaMalloc(p, bytes);
   if (e != cudaSuccess) return cuda_fail(c, e, "cudaMalloc");
   c->device_bytes += (int64_t)bytes;

@@ -176,7 +176,7 @@ class Engine:
 
     def __init__(self, lattice: Lattice, ham: _abi.HamiltonianDesc, spin: int = SPIN_ISING, seed: int = 0,
                  proposal: Optional[int] = None, path: int = PATH_AUTO, precision: int = FP32, replica: int = 0,
-                 threads_per_block: int = 0, blocks_per_sm: int = 0, device: int = -1):
+                 threads_per_block: int = 0, blocks_per_sm: int = 0, device: int = -1, max_device_bytes: int = 0):
         L = lib()
         o = _abi.Options()
         _check(L.vg_options_default(spin, C.byref(o)))
@@ -184,6 +184,7 @@ class Engine:
             o.proposal = proposal
         o.path, o.precision, o.replica = path, precision, replica
         o.threads_per_block, o.blocks_per_sm, o.device = threads_per_block, blocks_per_sm, device
+        o.max_device_bytes = max_device_bytes
         self.lattice, self.ham, self.spin_kind = lattice, ham, spin
         d = lattice.desc()
         h = C.c_void_p()

@@ -36,7 +36,7 @@ class HamiltonianDesc(C.Structure):
 class Options(C.Structure):
     _fields_ = [("spin_kind", C.c_int32), ("proposal", C.c_int32), ("path", C.c_int32),
                 ("precision", C.c_int32), ("replica", C.c_uint32), ("threads_per_block", C.c_int32),
-                ("blocks_per_sm", C.c_int32), ("device", C.c_int32)]
+                ("blocks_per_sm", C.c_int32), ("device", C.c_int32), ("max_device_bytes", C.c_int64)]
 
 
 class Sums(C.Structure):
