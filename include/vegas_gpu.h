@@ -242,6 +242,81 @@ int vg_batch_swap_stats(vg_batch* batch, int32_t group, int64_t* accepted, int64
 int vg_batch_get_replica(vg_batch* batch, int32_t group, int32_t replica, int8_t* spins);
 int vg_batch_set_replica(vg_batch* batch, int32_t group, int32_t replica, const int8_t* spins);
 
+/* -------------------------------------------- batched Heisenberg replicas
+ * Many Heisenberg replicas of one bcc or fcc lattice swept together under a
+ * shared field schedule (hysteresis loops; HysteresisLoop::run,
+ * src/program.rs:281-335, and MetropolisIntegrator::step for every replica,
+ * src/integrator.rs:66-92).  Every replica has its own seed, Philox stream
+ * id, temperature and energy constants.  The colour classes are the basis
+ * sublattices (bcc 2, fcc 4), which is what the greedy colouring of these
+ * lattices gives, and a class entry is the cell index, so a replica draws
+ * exactly the numbers of a single-lattice context with the same seed and
+ * replica id and follows its trajectory (up to summation order).
+ * Per-site energy: -J sum_j s.s_j + K (s.e)^2 + zeeman_sign h (s.b)
+ *                  - Kc (sx^4 + sy^4 + sz^4), h the field point's value
+ * (signed), e the anisotropy axis and b the field axis. */
+typedef struct {
+  uint64_t seed;
+  uint32_t replica;           /* Philox stream id (counter word 3) */
+  uint32_t reserved;
+  double temperature;
+  double exchange;            /* J */
+  double anisotropy;          /* uniaxial K */
+  double cubic;               /* Kc */
+} vg_heis_replica;
+
+typedef struct {
+  vg_lattice_desc lattice;    /* VG_CELL_BCC or VG_CELL_FCC */
+  double anisotropy_axis[3];
+  double field_axis[3];
+  double zeeman_sign;         /* +1: the reference's per-site sign; -1: spins align with the field */
+  int32_t precision;          /* VG_FP32 or VG_FP64 */
+  int32_t proposal;           /* VG_PROPOSE_RANDOM or VG_PROPOSE_FLIP */
+} vg_hbatch_desc;
+
+/* Per (field point, replica), sums over the point's measured sweeps of:
+ * 0 bond sum s_i.s_j, 1 sum (s.e)^2, 2 sum s.b, 3 sum (sx^4+sy^4+sz^4),
+ * 4-6 Mx, My, Mz, 7 accepted moves, 8 |M|, 9 |M|^2, 10 E, 11 E^2, with
+ * E = sum_i energy(i) (the reference's Compound total:
+ * -2 J bond + K aniso + zeeman_sign h zeeman - Kc cubic). */
+#define VG_HB_NSUMS 12
+
+typedef struct vg_hbatch vg_hbatch;
+typedef struct {
+  int32_t n_replicas;
+  int32_t n_classes;
+  int64_t sites_per_replica;
+  uint64_t sweep_index;
+  int32_t sites_per_thread;    /* 4: float4 runs along x; 1: scalar */
+  int32_t graph;               /* 1 if a field point is replayed as a CUDA graph */
+  int64_t device_bytes;
+} vg_hbatch_info;
+
+int vg_hbatch_create(const vg_hbatch_desc* desc, const vg_heis_replica* replicas, int32_t n_replicas,
+                     vg_hbatch** out);
+int vg_hbatch_destroy(vg_hbatch* batch);
+const char* vg_hbatch_last_error(const vg_hbatch* batch);
+int vg_hbatch_get_info(const vg_hbatch* batch, vg_hbatch_info* out);
+int vg_hbatch_get_stream(const vg_hbatch* batch, void** cuda_stream);
+/* Every replica random, as vg_init_random of a context with its seed and id. */
+int vg_hbatch_init_random(vg_hbatch* batch);
+/* Replica state as n_sites x 3 doubles in the reference's site order. */
+int vg_hbatch_set_replica(vg_hbatch* batch, int32_t replica, const double* xyz, int64_t n_sites);
+int vg_hbatch_get_replica(vg_hbatch* batch, int32_t replica, double* xyz, int64_t n_sites);
+/* For each of the n_points field values: relax_sweeps sweeps, then
+ * measure_sweeps sweeps whose sums are accumulated (VG_HB_NSUMS per point
+ * and replica).  A point is one CUDA graph launch. */
+int vg_hbatch_run(vg_hbatch* batch, const double* fields, int32_t n_points, uint32_t relax_sweeps,
+                  uint32_t measure_sweeps);
+int vg_hbatch_run_async(vg_hbatch* batch, const double* fields, int32_t n_points, uint32_t relax_sweeps,
+                        uint32_t measure_sweeps);
+int vg_hbatch_synchronize(vg_hbatch* batch);
+/* out[(point * n_replicas + replica) * VG_HB_NSUMS + k] of the last run. */
+int vg_hbatch_point_sums(vg_hbatch* batch, double* out, int64_t capacity);
+/* Mean device time of one sweep's colour passes (all replicas, update only,
+ * field 0), over n_sweeps sweeps timed with CUDA events on the batch stream. */
+int vg_hbatch_time_passes(vg_hbatch* batch, uint32_t n_sweeps, double* ms_per_sweep);
+
 /* ------------------------------------------------------ no-alloc sweeps */
 /* No counterpart in the reference.  n Ising flip-proposal sweeps of an sc
  * lattice (x a multiple of 32, even extents on periodic axes) that allocate

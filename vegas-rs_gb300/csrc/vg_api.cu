@@ -21,7 +21,7 @@
 #include <string>
 #include <vector>
 
-#include "vg_internal.cuh"
+#include "vg_heis_common.cuh"
 
 using namespace vg;
 
@@ -299,28 +299,12 @@ __global__ void heis_export(double* __restrict__ dst, long long n, int structure
   }
 }
 
-// State::rand_with_size for Heisenberg: the same uniform-on-sphere map as
-// the proposals, from block (i, 0, tag).
+// State::rand_with_size for Heisenberg (heis_init_spin).
 template <typename R>
 __global__ void heis_init(long long n, int structured, ScMap m, Planes<R> P, RngKey key) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const uint4 w = philox(make_uint4((uint32_t)i, 0u, kTagInitHeis << 24, key.replica), key.k0, key.k1);
-    const R z = (R)((int)((w.x >> 8) << 1) + 1 - (1 << 24)) * (R)(1.0 / 16777216.0);
-    const R t = (R)(w.y >> 8) * (R)(1.0 / 8388608.0);
-    R sn, cs;
-    if (sizeof(R) == 4) {
-      float a, b;
-      sincospif((float)t, &a, &b);
-      sn = (R)a;
-      cs = (R)b;
-    } else {
-      double a, b;
-      sincospi((double)t, &a, &b);
-      sn = (R)a;
-      cs = (R)b;
-    }
-    const R r = (R)sqrt((double)(((R)1 - z) * ((R)1 + z)));
-    heis_put<R>(i, structured, m, P, r * cs, r * sn, z);
+    const V3<R> s = heis_init_spin<R>((uint32_t)i, key);
+    heis_put<R>(i, structured, m, P, s.x, s.y, s.z);
   }
 }
 

@@ -14,102 +14,9 @@
 // Per-sweep sums: each site adds its terms after its own update; the bond
 // sum takes, for each site, only neighbours of lower colour, which are final
 // for the sweep when that site's pass runs, so every bond is counted once.
-#include "vg_internal.cuh"
+#include "vg_heis_common.cuh"
 
 namespace vg {
-
-__device__ __forceinline__ void sincospi_(float t, float* s, float* c) { sincospif(t, s, c); }
-__device__ __forceinline__ void sincospi_(double t, double* s, double* c) { sincospi(t, s, c); }
-__device__ __forceinline__ float sqrt_(float x) { return sqrtf(x); }
-__device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
-__device__ __forceinline__ float exp_(float x) { return expf(x); }
-__device__ __forceinline__ double exp_(double x) { return exp(x); }
-
-template <typename R>
-struct V3 {
-  R x, y, z;
-};
-
-template <typename R>
-__device__ __forceinline__ R quart(const V3<R>& s) {
-  const R a = s.x * s.x, b = s.y * s.y, c = s.z * s.z;
-  return a * a + b * b + c * c;
-}
-
-// Proposal and acceptance draw of one site; returns the new spin and whether
-// it was accepted.
-template <typename R, int PROP>
-__device__ __forceinline__ bool heis_update(const V3<R>& s, const V3<R>& h, const HeisParams<R>& P, const uint4& w,
-                                            V3<R>& out) {
-  V3<R> p;
-  if (PROP == VG_PROPOSE_RANDOM) {
-    // z = (2k + 1 - 2^24) / 2^24 is exact in FP32; azimuth pi * t, t in [0, 2)
-    const R z = (R)((int)((w.x >> 8) << 1) + 1 - (1 << 24)) * (R)(1.0 / 16777216.0);
-    const R t = (R)(w.y >> 8) * (R)(1.0 / 8388608.0);
-    R sn, cs;
-    sincospi_(t, &sn, &cs);
-    const R r = sqrt_(((R)1 - z) * ((R)1 + z));
-    p.x = r * cs;
-    p.y = r * sn;
-    p.z = z;
-  } else {
-    p.x = -s.x;
-    p.y = -s.y;
-    p.z = -s.z;
-  }
-  const R dx = p.x - s.x, dy = p.y - s.y, dz = p.z - s.z;
-  const R pe = p.x * P.ax + p.y * P.ay + p.z * P.az;
-  const R se = s.x * P.ax + s.y * P.ay + s.z * P.az;
-  R de = -P.J * (dx * h.x + dy * h.y + dz * h.z);
-  de += P.K * (pe * pe - se * se);
-  de += P.hz * (dx * P.bx + dy * P.by + dz * P.bz);
-  de -= P.Kc * (quart(p) - quart(s));
-  const R u = (R)(w.z >> 8) * (R)(1.0 / 16777216.0);
-  const bool acc = de <= (R)0 || u < exp_(-de * P.beta);
-  out = acc ? p : s;
-  return acc;
-}
-
-template <typename R>
-__device__ __forceinline__ void add_site_sums(R (&acc)[kNumSums], const V3<R>& s, const V3<R>& low,
-                                              const HeisParams<R>& P) {
-  const R se = s.x * P.ax + s.y * P.ay + s.z * P.az;
-  acc[0] += s.x * low.x + s.y * low.y + s.z * low.z;
-  acc[1] += se * se;
-  acc[2] += s.x * P.bx + s.y * P.by + s.z * P.bz;
-  acc[3] += quart(s);
-  acc[4] += s.x;
-  acc[5] += s.y;
-  acc[6] += s.z;
-}
-
-// Thread partials in R, warp sums in R, then FP64 across the block's warps
-// (a block row of kNumSums doubles).
-template <typename R>
-__device__ __forceinline__ void flush_sums(R (&acc)[kNumSums], double* part) {
-  __shared__ double red[32][kNumSums];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-  for (int i = 0; i < kNumSums; ++i) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc[i] += __shfl_down_sync(0xffffffffu, acc[i], o);
-  }
-  if (lane == 0) {
-#pragma unroll
-    for (int i = 0; i < kNumSums; ++i) red[warp][i] = (double)acc[i];
-  }
-  __syncthreads();
-  if (threadIdx.x < kNumSums) {
-    double t = 0.0, c = 0.0;  // Kahan over the warps, in a fixed order
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
-      const double y = red[w][threadIdx.x] - c;
-      const double u = t + y;
-      c = (u - t) - y;
-      t = u;
-    }
-    part[(size_t)blockIdx.x * kNumSums + threadIdx.x] = t;
-  }
-}
 
 // ------------------------------------------------------------------ sc
 template <typename R, int C, bool ALLPER, bool MEASURE, bool UPDATE, int PROP>
@@ -183,26 +90,6 @@ __global__ void __launch_bounds__(256) heis_sc_kernel(const HeisScArgs<R> a, con
 // Four consecutive class entries per thread (x extent a multiple of 8):
 // float4 loads of the SoA planes; the x neighbour outside the same float4 is
 // one scalar per plane, as in the Ising checkerboard kernel.
-template <typename R>
-struct Vec4 {
-  R v[4];
-};
-__device__ __forceinline__ Vec4<float> ld4(const float* p) {
-  const float4 t = __ldg(reinterpret_cast<const float4*>(p));
-  return Vec4<float>{{t.x, t.y, t.z, t.w}};
-}
-__device__ __forceinline__ Vec4<double> ld4(const double* p) {
-  const double2 a = __ldg(reinterpret_cast<const double2*>(p)), b = __ldg(reinterpret_cast<const double2*>(p) + 1);
-  return Vec4<double>{{a.x, a.y, b.x, b.y}};
-}
-__device__ __forceinline__ void st4(float* p, const Vec4<float>& v) {
-  *reinterpret_cast<float4*>(p) = make_float4(v.v[0], v.v[1], v.v[2], v.v[3]);
-}
-__device__ __forceinline__ void st4(double* p, const Vec4<double>& v) {
-  reinterpret_cast<double2*>(p)[0] = make_double2(v.v[0], v.v[1]);
-  reinterpret_cast<double2*>(p)[1] = make_double2(v.v[2], v.v[3]);
-}
-
 template <typename R, int C, bool ALLPER, bool MEASURE, bool UPDATE, int PROP>
 __global__ void __launch_bounds__(256) heis_sc4_kernel(const HeisScArgs<R> a, const HeisParams<R> P, const RngKey key,
                                                        double* __restrict__ part) {

@@ -29,6 +29,7 @@ __all__ = [
     "Lattice", "Exchange", "UniaxialAnisotropy", "Zeeman", "Gauge", "CubicAnisotropy", "hamiltonian",
     "Engine", "Sums", "VegasGpuError", "lib", "SPIN_ISING", "SPIN_HEISENBERG", "PROPOSE_FLIP",
     "PROPOSE_RANDOM", "PATH_AUTO", "PATH_GENERIC", "PATH_STRUCTURED", "PATH_RESIDENT", "FP32", "FP64", "Batch",
+    "HeisReplica", "HysteresisBatch", "hysteresis_fields", "loop_area", "coercive_fields",
 ]
 
 _lib = None
@@ -410,6 +411,157 @@ class Batch:
     def set_replica(self, group: int, replica: int, spins: np.ndarray):
         a = np.ascontiguousarray(spins, dtype=np.int8)
         self._chk(lib().vg_batch_set_replica(self._h, group, replica, a.ctypes.data_as(C.POINTER(C.c_int8))))
+
+
+class HeisReplica:
+    """One replica of a HysteresisBatch: seed and Philox stream id, temperature
+    and energy constants (exchange J, uniaxial K, cubic Kc)."""
+
+    def __init__(self, seed: int, replica: int = 0, temperature: float = 1.0, exchange: float = 1.0,
+                 anisotropy: float = 0.0, cubic: float = 0.0):
+        self.seed, self.replica, self.temperature = seed, replica, temperature
+        self.exchange, self.anisotropy, self.cubic = exchange, anisotropy, cubic
+
+    def _c(self) -> _abi.HeisReplica:
+        return _abi.HeisReplica(C.c_uint64(self.seed).value, self.replica, 0, self.temperature, self.exchange,
+                                self.anisotropy, self.cubic)
+
+
+class HysteresisBatch:
+    """Heisenberg replicas of one bcc or fcc lattice swept through a shared
+    field schedule (the vg_hbatch_* ABI).
+
+    Per-site energy -J sum s.s_j + K (s.e)^2 + zeeman_sign h (s.b) - Kc sum s_a^4;
+    zeeman_sign = +1 is the reference's per-site sign, -1 aligns the spins with
+    the field.  run(fields, relax, measure) returns the per-point sums
+    (points x replicas x 12, see VG_HB_NSUMS in vegas_gpu.h).
+    """
+
+    def __init__(self, lattice: "Lattice", replicas: Sequence[HeisReplica], anisotropy_axis=(0.0, 0.0, 1.0),
+                 field_axis=(0.0, 0.0, 1.0), zeeman_sign: float = 1.0, precision: int = FP32,
+                 proposal: int = PROPOSE_RANDOM):
+        L = lib()
+        d = _abi.HBatchDesc()
+        d.lattice = lattice.desc()
+        d.anisotropy_axis[:] = tuple(float(v) for v in anisotropy_axis)
+        d.field_axis[:] = tuple(float(v) for v in field_axis)
+        d.zeeman_sign = zeeman_sign
+        d.precision = precision
+        d.proposal = proposal
+        arr = (_abi.HeisReplica * len(replicas))(*[r._c() for r in replicas])
+        h = C.c_void_p()
+        rc = L.vg_hbatch_create(C.byref(d), arr, len(replicas), C.byref(h))
+        if rc:
+            raise VegasGpuError(rc, L.vg_last_error(None).decode())
+        self._h = h
+        self.lattice = lattice
+        self.replicas = list(replicas)
+        self.zeeman_sign = zeeman_sign
+
+    def _chk(self, rc):
+        if rc:
+            raise VegasGpuError(rc, lib().vg_hbatch_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().vg_hbatch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def info(self) -> _abi.HBatchInfo:
+        i = _abi.HBatchInfo()
+        self._chk(lib().vg_hbatch_get_info(self._h, C.byref(i)))
+        return i
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        self._chk(lib().vg_hbatch_get_stream(self._h, C.byref(s)))
+        return s.value or 0
+
+    def init_random(self):
+        self._chk(lib().vg_hbatch_init_random(self._h))
+
+    def get_replica(self, r: int) -> np.ndarray:
+        n = self.lattice.n_sites
+        out = np.empty((n, 3), dtype=np.float64)
+        self._chk(lib().vg_hbatch_get_replica(self._h, r, out.ctypes.data_as(C.POINTER(C.c_double)), n))
+        return out
+
+    def set_replica(self, r: int, xyz: np.ndarray):
+        a = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        self._chk(lib().vg_hbatch_set_replica(self._h, r, a.ctypes.data_as(C.POINTER(C.c_double)), a.shape[0]))
+
+    def run_async(self, fields, relax: int, measure: int):
+        f = np.ascontiguousarray(fields, dtype=np.float64)
+        self._fields = f
+        self._chk(lib().vg_hbatch_run_async(self._h, f.ctypes.data_as(C.POINTER(C.c_double)), f.size, relax,
+                                            measure))
+
+    def synchronize(self):
+        self._chk(lib().vg_hbatch_synchronize(self._h))
+
+    def point_sums(self) -> np.ndarray:
+        n = self._fields.size * len(self.replicas) * _abi.HB_NSUMS
+        out = np.empty(n, dtype=np.float64)
+        self._chk(lib().vg_hbatch_point_sums(self._h, out.ctypes.data_as(C.POINTER(C.c_double)), n))
+        return out.reshape(self._fields.size, len(self.replicas), _abi.HB_NSUMS)
+
+    def run(self, fields, relax: int, measure: int) -> np.ndarray:
+        self.run_async(fields, relax, measure)
+        self.synchronize()
+        return self.point_sums()
+
+    def time_passes(self, n_sweeps: int) -> float:
+        ms = C.c_double()
+        self._chk(lib().vg_hbatch_time_passes(self._h, n_sweeps, C.byref(ms)))
+        return ms.value
+
+
+def hysteresis_fields(max_field: float, step: float) -> np.ndarray:
+    """Signed field values of a closed loop +max -> -max -> +max in steps of
+    `step` (2 n + 1 points for n = max / step; each value is computed as
+    max - k step, so the schedule does not drift).  The reference's own
+    HysteresisLoop (src/program.rs:281-335, magnitude 0 -> max -> -max -> max
+    with accumulated steps) is mirrored by the C++ host's HysteresisLoop."""
+    n = int(round(max_field / step))
+    down = max_field - step * np.arange(0, 2 * n + 1)
+    up = -max_field + step * np.arange(1, 2 * n + 1)
+    return np.concatenate([down, up])
+
+
+def loop_area(fields: np.ndarray, m: np.ndarray) -> float:
+    """Area enclosed by the closed loop (h, m): |trapezoid integral of m dh|."""
+    h = np.append(fields, fields[0])
+    mm = np.append(m, m[0])
+    return float(abs(np.sum(0.5 * (mm[1:] + mm[:-1]) * np.diff(h))))
+
+
+def coercive_fields(fields: np.ndarray, m: np.ndarray):
+    """Fields where m changes sign on the descending and the ascending branch
+    (linear interpolation between the bracketing points; NaN if none)."""
+    res = []
+    for sgn in (-1.0, 1.0):
+        hc = float("nan")
+        for i in range(len(fields) - 1):
+            if np.sign(fields[i + 1] - fields[i]) != sgn:
+                continue
+            a, b = m[i], m[i + 1]
+            if a == 0.0 or a * b < 0.0:
+                hc = float(fields[i] if a == 0.0 else fields[i] + (fields[i + 1] - fields[i]) * a / (a - b))
+                break
+        res.append(hc)
+    return tuple(res)
 
 
 def device_count() -> int:

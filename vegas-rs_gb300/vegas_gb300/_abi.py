@@ -62,6 +62,25 @@ class BatchInfo(C.Structure):
                 ("round_index", C.c_uint32), ("graph", C.c_int32)]
 
 
+class HeisReplica(C.Structure):
+    _fields_ = [("seed", C.c_uint64), ("replica", C.c_uint32), ("reserved", C.c_uint32),
+                ("temperature", C.c_double), ("exchange", C.c_double), ("anisotropy", C.c_double),
+                ("cubic", C.c_double)]
+
+
+class HBatchDesc(C.Structure):
+    _fields_ = [("lattice", LatticeDesc), ("anisotropy_axis", C.c_double * 3), ("field_axis", C.c_double * 3),
+                ("zeeman_sign", C.c_double), ("precision", C.c_int32), ("proposal", C.c_int32)]
+
+
+class HBatchInfo(C.Structure):
+    _fields_ = [("n_replicas", C.c_int32), ("n_classes", C.c_int32), ("sites_per_replica", C.c_int64),
+                ("sweep_index", C.c_uint64), ("sites_per_thread", C.c_int32), ("graph", C.c_int32),
+                ("device_bytes", C.c_int64)]
+
+
+HB_NSUMS = 12
+
 # symbol -> (restype, argtypes); the list the header declares
 P = C.POINTER
 SIGNATURES = {
@@ -107,6 +126,19 @@ SIGNATURES = {
     "vg_batch_swap_stats": (C.c_int, [C.c_void_p, C.c_int32, P(C.c_int64), P(C.c_int64)]),
     "vg_batch_get_replica": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, P(C.c_int8)]),
     "vg_batch_set_replica": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, P(C.c_int8)]),
+    "vg_hbatch_create": (C.c_int, [P(HBatchDesc), P(HeisReplica), C.c_int32, P(C.c_void_p)]),
+    "vg_hbatch_destroy": (C.c_int, [C.c_void_p]),
+    "vg_hbatch_last_error": (C.c_char_p, [C.c_void_p]),
+    "vg_hbatch_get_info": (C.c_int, [C.c_void_p, P(HBatchInfo)]),
+    "vg_hbatch_get_stream": (C.c_int, [C.c_void_p, P(C.c_void_p)]),
+    "vg_hbatch_init_random": (C.c_int, [C.c_void_p]),
+    "vg_hbatch_set_replica": (C.c_int, [C.c_void_p, C.c_int32, P(C.c_double), C.c_int64]),
+    "vg_hbatch_get_replica": (C.c_int, [C.c_void_p, C.c_int32, P(C.c_double), C.c_int64]),
+    "vg_hbatch_run": (C.c_int, [C.c_void_p, P(C.c_double), C.c_int32, C.c_uint32, C.c_uint32]),
+    "vg_hbatch_run_async": (C.c_int, [C.c_void_p, P(C.c_double), C.c_int32, C.c_uint32, C.c_uint32]),
+    "vg_hbatch_synchronize": (C.c_int, [C.c_void_p]),
+    "vg_hbatch_point_sums": (C.c_int, [C.c_void_p, P(C.c_double), C.c_int64]),
+    "vg_hbatch_time_passes": (C.c_int, [C.c_void_p, C.c_uint32, P(C.c_double)]),
     "vg_ising_sc_sweeps_noalloc": (C.c_int, [P(LatticeDesc), C.c_double, C.c_double, C.c_double, C.c_uint64,
                                              C.c_uint32, C.c_uint64, C.c_uint64, C.c_void_p, C.c_void_p,
                                              C.c_void_p, C.c_void_p]),
