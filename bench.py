@@ -209,6 +209,114 @@ def run_batched(V, torch, args):
             "swap_acceptance_3d128": float(acc[:-1].sum() / max(att[:-1].sum(), 1))}
 
 
+def run_heisenberg(V, torch, args):
+    """Heisenberg sc 128^3, J=1, K=0.1 along z, B=0.05 along z, uniform-on-sphere
+    proposals, FP32 updates with FP64 sums; a step is 100 measured sweeps at the
+    next temperature of the 0.2-2.0 ladder.  Beside the throughput: the error of
+    the device sums (FP32 partials, FP64 combination) against an FP64
+    recomputation from the exported state, and an all-FP64 run's throughput."""
+    import numpy as np
+
+    n_l, sweeps = 128, 100
+    lat = V.Lattice.sc(n_l, n_l, n_l)
+    H = V.hamiltonian(V.Exchange(1.0), V.UniaxialAnisotropy((0, 0, 1), 0.1), V.Zeeman())
+    temps = [0.2 + 0.1 * k for k in range(19)]
+    out = {}
+    for prec, steps in ((V.FP32, args.steps), (V.FP64, 1)):
+        with V.Engine(lat, H, spin=V.SPIN_HEISENBERG, seed=SEED, precision=prec) as eng:
+            eng.init_random()
+            eng.set_thermostat(temps[0], (0, 0, 1), 0.05)
+            eng.sweeps(sweeps)
+            s = torch.cuda.ExternalStream(eng.stream())
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+            for k, (a, c) in enumerate(ev):
+                eng.set_thermostat(temps[(k + 1) % len(temps)], (0, 0, 1), 0.05)
+                a.record(s)
+                eng.sweeps_async(sweeps, measure=True)
+                c.record(s)
+            eng.synchronize()
+            ms = sum(a.elapsed_time(c) for a, c in ev)
+            pass_ms, _ = eng.time_passes(20, measure=False)
+            key = "fp32" if prec == V.FP32 else "fp64"
+            out[key] = {"value": lat.n_sites * sweeps * steps / (ms * 1e6), "pass_ms": pass_ms}
+            if prec == V.FP32:
+                st = eng.get_state().reshape(n_l, n_l, n_l, 3)
+                got = eng.current_sums()
+                bond = sum(float(np.sum(st * np.roll(st, 1, axis=a))) for a in range(3))
+                ref = {"bond": (0, bond), "anisotropy": (1, float(np.sum(st[..., 2] ** 2))),
+                       "mz": (6, float(st[..., 2].sum()))}
+                out["sum_rel_err"] = {k: abs(float(got[i]) - v) / abs(v) for k, (i, v) in ref.items()}
+    alg = 18.0 * lat.n_sites  # per pass: read both classes (12 B each), write one class
+    peak, _ = peaks()
+    ach = alg / (out["fp32"]["pass_ms"] * 1e-3) / 1e9
+    return {"workload": "heisenberg-sc-128^3-pbc J=1 K=0.1 z B=0.05 z, random proposals, FP32 update / FP64 sums",
+            "value": out["fp32"]["value"], "unit": "flips/ns", "sweeps_per_step": sweeps,
+            "fp64_value": out["fp64"]["value"], "bytes_per_flip": 36.0,
+            "roofline": {"achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                         "pass_ms": out["fp32"]["pass_ms"], "kernel": "heis_sc4_kernel (one colour pass)"},
+            "sum_rel_err_vs_fp64_recompute": out["sum_rel_err"]}
+
+
+def run_hysteresis(V, torch, args):
+    """Batched Heisenberg hysteresis: fcc 64^3 cells (1,048,576 spins), 64
+    replicas (8 seeds x 8 cubic constants 0-0.1), T=0.5, J=1, field along z
+    from +5 to -5 and back in steps of 0.1 (201 points).  Throughput on a
+    bounded sample of the schedule (a step = 4 field points x (10 relax + 40
+    measured sweeps) of all 64 replicas); loop area and coercive fields of a
+    full loop on fcc 8^3 cells in FP32 and FP64 (same seeds)."""
+    import numpy as np
+
+    def replicas():
+        return [V.HeisReplica(seed=SEED + 7919 * (r // 8), replica=r, temperature=0.5, exchange=1.0,
+                              anisotropy=0.0, cubic=0.1 * (r % 8) / 7) for r in range(64)]
+
+    fields = V.hysteresis_fields(5.0, 0.1)
+    lat = V.Lattice.fcc(64, 64, 64)
+    relax, measure, pts = 10, 40, 4
+    with V.HysteresisBatch(lat, replicas(), field_axis=(0, 0, 1), zeeman_sign=-1.0) as hb:
+        hb.init_random()
+        hb.run(fields[:pts], relax, measure)  # warm-up (graph capture)
+        s = torch.cuda.ExternalStream(hb.stream())
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        for k, (a, c) in enumerate(ev):
+            a.record(s)
+            hb.run_async(fields[(k * pts) % 200:(k * pts) % 200 + pts], relax, measure)
+            c.record(s)
+        hb.synchronize()
+        ms = sum(a.elapsed_time(c) for a, c in ev)
+        sweep_ms = hb.time_passes(10)
+        info = hb.info()
+    n_total = float(lat.n_sites) * 64
+    value = n_total * pts * (relax + measure) * args.steps / (ms * 1e6)
+    alg = 15.0 * n_total  # per colour pass (4 classes, 12 B payload): read all, write one class
+    peak, _ = peaks()
+    ach = alg / (sweep_ms / 4 * 1e-3) / 1e9
+    # full loop, small lattice, FP32 against FP64
+    small = V.Lattice.fcc(8, 8, 8)
+    loops = {}
+    for prec in (V.FP32, V.FP64):
+        with V.HysteresisBatch(small, replicas(), field_axis=(0, 0, 1), zeeman_sign=-1.0, precision=prec) as hb:
+            hb.init_random()
+            sums = hb.run(fields, 20, 30)
+        m = sums[:, :, 6] / (30 * small.n_sites)
+        loops[prec] = ([V.loop_area(fields, m[:, r]) for r in range(64)],
+                       [V.coercive_fields(fields, m[:, r]) for r in range(64)])
+    a32, a64 = np.array(loops[V.FP32][0]), np.array(loops[V.FP64][0])
+    h32, h64 = np.array(loops[V.FP32][1]), np.array(loops[V.FP64][1])
+    return {"workload": "fcc 64^3 cells x 64 replicas (8 seeds x 8 Kc in 0-0.1), T=0.5, B_z +5 -> -5 -> +5 "
+                        "step 0.1, FP32 updates, FP64 sums",
+            "value": value, "unit": "flips/ns", "ms_per_step": ms / args.steps,
+            "sample": f"{pts} field points x ({relax} relax + {measure} measured sweeps) per step",
+            "graph": bool(info.graph), "sites_per_thread": int(info.sites_per_thread), "bytes_per_flip": 60.0,
+            "roofline": {"achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                         "sweep_ms": sweep_ms, "kernel": "hb_pass (one colour pass, all replicas)"},
+            "loop_fcc8": {"area_fp64_mean": float(a64.mean()), "area_fp32_mean": float(a32.mean()),
+                          "area_rel_diff_mean": float(np.mean(np.abs(a32 - a64) / np.abs(a64))),
+                          "hc_fp64_mean": [float(np.nanmean(h64[:, 0])), float(np.nanmean(h64[:, 1]))],
+                          "hc_abs_diff_mean": float(np.nanmean(np.abs(h32 - h64))),
+                          "schedule": "201 points x (20 relax + 30 measured sweeps)"}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -218,6 +326,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--lattice", type=int, default=L)
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-heisenberg", action="store_true")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -325,6 +434,11 @@ def main():
     if not args.no_batched:
         batched = run_batched(V, torch, args)
 
+    heis = hyst = None
+    if not args.no_heisenberg:
+        heis = run_heisenberg(V, torch, args)
+        hyst = run_hysteresis(V, torch, args)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, dt = cpu_baseline_sample(threads=1, sweeps=2)
@@ -355,6 +469,8 @@ def main():
             "cpu_baseline": cpu,
             "batched": batched,
             "batched_vs_plain": (batched["value"] / value) if batched else None,
+            "heisenberg": heis,
+            "hysteresis_batch": hyst,
             "clocks": clk.summary(),
             "wall_s": wall,
             "sweep_ms": sweep_ms,

@@ -188,3 +188,25 @@ def test_rejections(V):
         assert e.value.status == 1 and "unit" in str(e.value)
         with pytest.raises(V.VegasGpuError):
             hb.get_replica(3)
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+def test_tracked_sums_do_not_drift(V, prec):
+    """Measured sweeps update the lattice sums by the changes of the accepted
+    moves.  300 tracked sweeps of one field point against the same 300 sweeps
+    measured as 300 one-sweep points (each starting from an exact sum)."""
+    p = V.FP32 if prec == "fp32" else V.FP64
+    lat = V.Lattice.fcc(8, 8, 4)
+    reps = _replicas(V, 2)
+    n = 300
+    with V.HysteresisBatch(lat, reps, anisotropy_axis=(0, 0, 1), zeeman_sign=-1.0, precision=p) as a, \
+            V.HysteresisBatch(lat, reps, anisotropy_axis=(0, 0, 1), zeeman_sign=-1.0, precision=p) as b:
+        a.init_random()
+        b.init_random()
+        sa = a.run([0.3], 0, n)[0]
+        sb = b.run(np.full(n, 0.3), 0, 1).sum(axis=0)
+        np.testing.assert_array_equal(a.get_replica(1), b.get_replica(1))
+    rtol = 2e-5 if prec == "fp32" else 1e-11
+    for k in (0, 1, 3, 4, 5, 6, 10):   # bond, aniso, cubic, M, E
+        np.testing.assert_allclose(sa[:, k], sb[:, k], rtol=rtol, atol=rtol * lat.n_sites * n)
+    np.testing.assert_array_equal(sa[:, 7], sb[:, 7])  # accepted moves

@@ -20,12 +20,18 @@
 // axis a, -1 otherwise.  A run of four cells along x is one float4 per
 // plane; the x-shifted run reuses it plus one scalar at the run's edge.
 //
-// One launch per colour covers every replica (grid.y = replica).  Per-sweep
-// sums (FP32 per thread and warp, FP64 per block) land in block rows that a
-// reduction kernel adds, in a fixed order, into per-point accumulators.  A
-// field point (relax + measure sweeps, reductions, counter advance) is
-// captured once into a CUDA graph and replayed for every point; the kernels
-// read the sweep counter and the field value from device memory.
+// One launch per colour covers every replica (grid.y = replica).  The
+// lattice sums a measured sweep reports are tracked, not recomputed: before
+// the measured sweeps of a field point one kernel sums the state exactly
+// (each bond from its higher-class end); during them every accepted move
+// adds its change of each sum, which the pass already has in registers (the
+// field h of the site is current, so the bond-sum change (s' - s).h is
+// exact).  Partials are FP32 per thread and warp and FP64 per block row; a
+// reduction kernel adds the rows, in a fixed order, to FP64 running totals
+// and those to the per-point accumulators.  A field point (relax sweeps,
+// exact sums, measured sweeps, counter advance) is captured once into a
+// CUDA graph and replayed for every point; the kernels read the sweep
+// counter and the field value from device memory.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -42,7 +48,10 @@ using namespace vg;
 namespace {
 
 constexpr int kHbSums = VG_HB_NSUMS;
-constexpr int kTpb = 256;
+constexpr int kTpb = 256;            // reduction and set-up kernels
+constexpr int kPassTpb = 256;        // colour passes and measurement
+constexpr int kPassMinBlocks = 4;    // 64 registers: 32 resident warps per SM (latency-bound loads)
+constexpr int kTrackMinBlocks = 4;   // tracked passes too (partials in shared memory)
 
 // Basis positions in half lattice constants: bcc (0,0,0) (1,1,1); fcc
 // (0,0,0) (1,1,0) (1,0,1) (0,1,1) -- the order of Lattice::bcc / fcc.
@@ -67,10 +76,18 @@ struct HbRep {         // per replica
   KeySchedule ks;
   uint32_t replica, k0, k1, pad;
   double beta, J, K, Kc;
+  float fbeta, fJ, fK, fKc;  // the same constants in FP32 for the FP32 kernels
+};
+
+// The per-point field value in both precisions.
+struct HbField {
+  double h;
+  float hf, pad;
 };
 
 struct HbShared {      // per batch
   double ax, ay, az, bx, by, bz, zsign;
+  float fax, fay, faz, fbx, fby, fbz, fzsign, pad;
 };
 
 struct HbDev {         // device counters read by every kernel of a point
@@ -155,11 +172,8 @@ __device__ __forceinline__ void add_class(const HbArgs<R>& a, const R* rep_base,
   }
 }
 
-// Neighbour field of a run of W cells of class CLS, split into the lower
-// classes (final for this sweep, used by the bond sum) and the higher ones.
-template <typename R, int NB, int CLS, int W>
-__device__ __forceinline__ void run_field(const HbArgs<R>& a, const R* rep_base, int x0, int y, int z,
-                                          Run<R, W> (&lo)[3], Run<R, W> (&hi)[3]) {
+template <int NB, int CLS, int W, typename A>
+__device__ __forceinline__ RunNbr make_nbr(const A& a, int x0, int y, int z) {
   constexpr int dx = half_pos<NB>(CLS, 0) ? 1 : -1;
   constexpr int dy = half_pos<NB>(CLS, 1) ? 1 : -1;
   constexpr int dz = half_pos<NB>(CLS, 2) ? 1 : -1;
@@ -185,41 +199,89 @@ __device__ __forceinline__ void run_field(const HbArgs<R>& a, const R* rep_base,
     nb.zs = nb.zs < 0 ? a.nz - 1 : 0;
     nb.zok = a.pbz;
   }
+  return nb;
+}
+
+template <typename R, int W>
+__device__ __forceinline__ void zero_runs(Run<R, W> (&v)[3]) {
 #pragma unroll
   for (int c = 0; c < 3; ++c)
 #pragma unroll
-    for (int k = 0; k < W; ++k) lo[c].v[k] = hi[c].v[k] = (R)0;
-  if constexpr (CLS != 0) add_class<R, NB, CLS, 0, W>(a, rep_base, x0, y, z, nb, lo);
-  if constexpr (CLS != 1) add_class<R, NB, CLS, 1, W>(a, rep_base, x0, y, z, nb, CLS > 1 ? lo : hi);
+    for (int k = 0; k < W; ++k) v[c].v[k] = (R)0;
+}
+
+// Neighbour field of a run of W cells of class CLS.
+template <typename R, int NB, int CLS, int W>
+__device__ __forceinline__ void run_field(const HbArgs<R>& a, const R* rep_base, int x0, int y, int z,
+                                          Run<R, W> (&h)[3]) {
+  const RunNbr nb = make_nbr<NB, CLS, W>(a, x0, y, z);
+  zero_runs(h);
+  if constexpr (CLS != 0) add_class<R, NB, CLS, 0, W>(a, rep_base, x0, y, z, nb, h);
+  if constexpr (CLS != 1) add_class<R, NB, CLS, 1, W>(a, rep_base, x0, y, z, nb, h);
   if constexpr (NB == 4) {
-    if constexpr (CLS != 2) add_class<R, NB, CLS, 2, W>(a, rep_base, x0, y, z, nb, CLS > 2 ? lo : hi);
-    if constexpr (CLS != 3) add_class<R, NB, CLS, 3, W>(a, rep_base, x0, y, z, nb, hi);
+    if constexpr (CLS != 2) add_class<R, NB, CLS, 2, W>(a, rep_base, x0, y, z, nb, h);
+    if constexpr (CLS != 3) add_class<R, NB, CLS, 3, W>(a, rep_base, x0, y, z, nb, h);
   }
 }
 
+// Field of the classes below CLS only (each bond counted once, from its
+// higher-class end).
+template <typename R, int NB, int CLS, int W>
+__device__ __forceinline__ void low_field(const HbArgs<R>& a, const R* rep_base, int x0, int y, int z,
+                                          Run<R, W> (&h)[3]) {
+  const RunNbr nb = make_nbr<NB, CLS, W>(a, x0, y, z);
+  zero_runs(h);
+  if constexpr (CLS > 0) add_class<R, NB, CLS, 0, W>(a, rep_base, x0, y, z, nb, h);
+  if constexpr (CLS > 1) add_class<R, NB, CLS, 1, W>(a, rep_base, x0, y, z, nb, h);
+  if constexpr (CLS > 2) add_class<R, NB, CLS, 2, W>(a, rep_base, x0, y, z, nb, h);
+}
+
 template <typename R>
-__device__ __forceinline__ HeisParams<R> rep_params(const HbRep& rp, const HbShared& sh, double h) {
+__device__ __forceinline__ HeisParams<R> rep_params(const HbRep& rp, const HbShared& sh, const HbField& f) {
   HeisParams<R> P;
-  P.J = (R)rp.J;
-  P.K = (R)rp.K;
-  P.ax = (R)sh.ax;
-  P.ay = (R)sh.ay;
-  P.az = (R)sh.az;
-  P.hz = (R)(sh.zsign * h);
-  P.bx = (R)sh.bx;
-  P.by = (R)sh.by;
-  P.bz = (R)sh.bz;
-  P.Kc = (R)rp.Kc;
-  P.beta = (R)rp.beta;
-  P.T = (R)(1.0 / rp.beta);
+  if constexpr (sizeof(R) == 4) {
+    P.J = rp.fJ;
+    P.K = rp.fK;
+    P.Kc = rp.fKc;
+    P.beta = rp.fbeta;
+    P.hz = sh.fzsign * f.hf;
+    P.ax = sh.fax;
+    P.ay = sh.fay;
+    P.az = sh.faz;
+    P.bx = sh.fbx;
+    P.by = sh.fby;
+    P.bz = sh.fbz;
+  } else {
+    P.J = rp.J;
+    P.K = rp.K;
+    P.Kc = rp.Kc;
+    P.beta = rp.beta;
+    P.hz = sh.zsign * f.h;
+    P.ax = sh.ax;
+    P.ay = sh.ay;
+    P.az = sh.az;
+    P.bx = sh.bx;
+    P.by = sh.by;
+    P.bz = sh.bz;
+  }
+  P.T = (R)0;  // unused by the update
   return P;
 }
 
 // One colour pass of every replica: grid (blocks per replica, replicas).
-template <typename R, int NB, int CLS, int W, bool MEASURE, int PROP>
-__global__ void __launch_bounds__(kTpb) hb_pass(const HbArgs<R> a, const HbRep* __restrict__ reps, const HbShared sh,
-                                                const double* __restrict__ fields, const HbDev* __restrict__ dev,
-                                                const uint32_t t, double* __restrict__ part) {
+// TRACK (measured sweeps): every accepted move adds its change of the
+// lattice sums to the thread's partials -- bond sum (s' - s).h, which is
+// exact because no two sites of a class are neighbours and h is the current
+// field; (s'.e)^2 - (s.e)^2; the quartic sum; s' - s; one accepted move --
+// and the block writes one row [class][replica][block].  (The Zeeman sum is
+// M.b and follows from the magnetisation.)  The partials live in the
+// thread's own shared-memory slots, which keeps the registers of the
+// update free.
+template <typename R, int NB, int CLS, int W, bool TRACK, int PROP>
+__global__ void __launch_bounds__(kPassTpb, TRACK ? kTrackMinBlocks : kPassMinBlocks) hb_pass(const HbArgs<R> a, const HbRep* __restrict__ reps,
+                                                                  const HbShared sh, const HbField* __restrict__ fields,
+                                                                  const HbDev* __restrict__ dev, const uint32_t t,
+                                                                  double* __restrict__ part) {
   const int r = blockIdx.y;
   const HbRep rp = reps[r];
   const HbDev d = *dev;
@@ -229,6 +291,94 @@ __global__ void __launch_bounds__(kTpb) hb_pass(const HbArgs<R> a, const HbRep* 
   R* own[3];
 #pragma unroll
   for (int c = 0; c < 3; ++c) own[c] = rep_base + (size_t)(CLS * 3 + c) * a.ncell;
+  constexpr int kTracked = 7;  // bond, aniso, cubic, mx, my, mz, accepted
+  __shared__ R s_dl[TRACK ? kTracked : 1][kPassTpb];
+  if (TRACK) {
+#pragma unroll
+    for (int i = 0; i < kTracked; ++i) s_dl[i][threadIdx.x] = (R)0;
+  }
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < a.runs; u += stride) {
+    const int row = (int)fdiv(u, a.frow);
+    const int x0 = (int)(u - (uint32_t)row * (uint32_t)a.rpr) * W;
+    const int z = (int)fdiv((uint32_t)row, a.fny);
+    const int y = row - z * a.ny;
+    Run<R, W> hf[3];
+    run_field<R, NB, CLS, W>(a, rep_base, x0, y, z, hf);
+    const uint32_t j0 = (uint32_t)row * (uint32_t)a.nx + (uint32_t)x0;
+    Run<R, W> S[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) S[c] = load_run<R, W>(own[c] + j0);
+    bool changed = false;
+#pragma unroll
+    for (int k = 0; k < W; ++k) {
+      const V3<R> s = {S[0].v[k], S[1].v[k], S[2].v[k]};
+      const V3<R> h = {hf[0].v[k], hf[1].v[k], hf[2].v[k]};
+      const uint4 w =
+          philox_ks(make_uint4(j0 + (uint32_t)k, sweep, (kTagHeis << 24) | ((uint32_t)CLS << 8), rp.replica), rp.ks);
+      V3<R> sn;
+      if (heis_update<R, PROP>(s, h, P, w, sn)) {
+        S[0].v[k] = sn.x;
+        S[1].v[k] = sn.y;
+        S[2].v[k] = sn.z;
+        changed = true;
+        if (TRACK) {
+          const V3<R> ds = {sn.x - s.x, sn.y - s.y, sn.z - s.z};
+          const R pe = sn.x * P.ax + sn.y * P.ay + sn.z * P.az;
+          const R se = s.x * P.ax + s.y * P.ay + s.z * P.az;
+          const int q = threadIdx.x;
+          s_dl[0][q] += ds.x * h.x + ds.y * h.y + ds.z * h.z;
+          s_dl[1][q] += pe * pe - se * se;
+          s_dl[2][q] += quart(sn) - quart(s);
+          s_dl[3][q] += ds.x;
+          s_dl[4][q] += ds.y;
+          s_dl[5][q] += ds.z;
+          s_dl[6][q] += (R)1;
+        }
+      }
+    }
+    if (changed) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) store_run<R, W>(own[c] + j0, S[c]);
+    }
+  }
+  if (TRACK) {
+    const int q = threadIdx.x;
+    R dl[kNumSums] = {s_dl[0][q], s_dl[1][q], (R)0, s_dl[2][q], s_dl[3][q], s_dl[4][q], s_dl[5][q], s_dl[6][q]};
+    flush_sums(dl, part + ((size_t)CLS * gridDim.y + r) * gridDim.x * kNumSums);
+  }
+}
+
+// Lattice sums of every replica after a sweep (all classes final): per run
+// of W cells, each class's site terms and its bonds to the lower classes.
+// FP32 per thread and warp, FP64 per block row [replica][block].
+template <typename R, int NB, int CLS, int W>
+__device__ __forceinline__ void measure_class(const HbArgs<R>& a, const R* rep_base, int x0, int y, int z,
+                                              uint32_t j0, const HeisParams<R>& P, R (&acc)[kNumSums]) {
+  Run<R, W> S[3], lo[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) S[c] = load_run<R, W>(rep_base + (size_t)(CLS * 3 + c) * a.ncell + j0);
+  low_field<R, NB, CLS, W>(a, rep_base, x0, y, z, lo);
+#pragma unroll
+  for (int k = 0; k < W; ++k) {
+    const V3<R> s = {S[0].v[k], S[1].v[k], S[2].v[k]};
+    const V3<R> low = {lo[0].v[k], lo[1].v[k], lo[2].v[k]};
+    add_site_sums(acc, s, low, P);
+  }
+}
+
+template <typename R, int NB, int W>
+__global__ void __launch_bounds__(kPassTpb) hb_measure(const HbArgs<R> a, const HbShared sh,
+                                                       double* __restrict__ part) {
+  const int r = blockIdx.y;
+  HeisParams<R> P{};
+  P.ax = (R)sh.ax;
+  P.ay = (R)sh.ay;
+  P.az = (R)sh.az;
+  P.bx = (R)sh.bx;
+  P.by = (R)sh.by;
+  P.bz = (R)sh.bz;
+  const R* rep_base = a.spin + (size_t)r * NB * 3 * a.ncell;
   R acc[kNumSums];
 #pragma unroll
   for (int i = 0; i < kNumSums; ++i) acc[i] = (R)0;
@@ -238,77 +388,78 @@ __global__ void __launch_bounds__(kTpb) hb_pass(const HbArgs<R> a, const HbRep* 
     const int x0 = (int)(u - (uint32_t)row * (uint32_t)a.rpr) * W;
     const int z = (int)fdiv((uint32_t)row, a.fny);
     const int y = row - z * a.ny;
-    Run<R, W> lo[3], hi[3];
-    run_field<R, NB, CLS, W>(a, rep_base, x0, y, z, lo, hi);
     const uint32_t j0 = (uint32_t)row * (uint32_t)a.nx + (uint32_t)x0;
-    Run<R, W> S[3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) S[c] = load_run<R, W>(own[c] + j0);
-    bool changed = false;
-#pragma unroll
-    for (int k = 0; k < W; ++k) {
-      V3<R> s = {S[0].v[k], S[1].v[k], S[2].v[k]};
-      const V3<R> h = {lo[0].v[k] + hi[0].v[k], lo[1].v[k] + hi[1].v[k], lo[2].v[k] + hi[2].v[k]};
-      const uint4 w =
-          philox_ks(make_uint4(j0 + (uint32_t)k, sweep, (kTagHeis << 24) | ((uint32_t)CLS << 8), rp.replica), rp.ks);
-      V3<R> sn;
-      if (heis_update<R, PROP>(s, h, P, w, sn)) {
-        S[0].v[k] = sn.x;
-        S[1].v[k] = sn.y;
-        S[2].v[k] = sn.z;
-        s = sn;
-        changed = true;
-        acc[7] += (R)1;
-      }
-      if (MEASURE) {
-        const V3<R> low = {lo[0].v[k], lo[1].v[k], lo[2].v[k]};
-        add_site_sums(acc, s, low, P);
-      }
-    }
-    if (changed) {
-#pragma unroll
-      for (int c = 0; c < 3; ++c) store_run<R, W>(own[c] + j0, S[c]);
+    measure_class<R, NB, 0, W>(a, rep_base, x0, y, z, j0, P, acc);
+    measure_class<R, NB, 1, W>(a, rep_base, x0, y, z, j0, P, acc);
+    if constexpr (NB == 4) {
+      measure_class<R, NB, 2, W>(a, rep_base, x0, y, z, j0, P, acc);
+      measure_class<R, NB, 3, W>(a, rep_base, x0, y, z, j0, P, acc);
     }
   }
-  if (MEASURE) flush_sums(acc, part + ((size_t)CLS * gridDim.y + r) * gridDim.x * kNumSums);
+  flush_sums(acc, part + (size_t)r * gridDim.x * kNumSums);
 }
 
-// Sums one measured sweep of every replica (block r = replica): rows
-// [class][replica][block] in a fixed order with Kahan compensation, then
-// adds the sweep's values into the point accumulators.
-__global__ void __launch_bounds__(kTpb) hb_reduce(const double* __restrict__ part, int nb, int nbx, int n_rep,
-                                                  const HbRep* __restrict__ reps, const HbShared sh,
-                                                  const double* __restrict__ fields, const HbDev* __restrict__ dev,
-                                                  double* __restrict__ acc) {
+// Block rows [rows][replica r][nbx] of replica r summed in a fixed order
+// with Kahan compensation (block r = replica; 256 threads: value v = tid % 8,
+// lane tid / 8), then the 32 lanes of each value combined by a fixed
+// shuffle tree; thread 0 returns the totals.  (FP64 latency is long on this
+// part, so no thread walks a long serial chain.)
+__device__ __forceinline__ void sum_rows(const double* __restrict__ part, int rows, int nbx, int n_rep, int r,
+                                         double (&s)[kNumSums]) {
   __shared__ double s_sum[kNumSums][32];
-  const int r = blockIdx.x;
+  __shared__ double s_tot[kNumSums];
   const int v = threadIdx.x % kNumSums, lane = threadIdx.x / kNumSums;
-  const int rows = nb * nbx;
   double sum = 0.0, comp = 0.0;
-  for (int i = lane; i < rows; i += 32) {
-    const int c = i / nbx, bx = i - c * nbx;
-    const double y = part[(((size_t)c * n_rep + r) * nbx + bx) * kNumSums + v] - comp;
-    const double t = sum + y;
-    comp = (t - sum) - y;
-    sum = t;
-  }
-  s_sum[v][lane] = sum;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double s[kNumSums];
-    for (int k = 0; k < kNumSums; ++k) {
-      double tt = 0.0, cc = 0.0;
-      for (int l = 0; l < 32; ++l) {
-        const double y = s_sum[k][l] - cc;
-        const double u = tt + y;
-        cc = (u - tt) - y;
-        tt = u;
-      }
-      s[k] = tt;
+  for (int c = 0; c < rows; ++c) {
+    const double* p = part + (((size_t)c * n_rep + r) * nbx) * kNumSums + v;
+    for (int bx = lane; bx < nbx; bx += 32) {
+      const double y = p[(size_t)bx * kNumSums] - comp;
+      const double t = sum + y;
+      comp = (t - sum) - y;
+      sum = t;
     }
+  }
+  s_sum[v][lane] = sum - comp;
+  __syncthreads();
+  if (threadIdx.x < 32 * kNumSums) {  // warp w combines value w (blockDim = 256)
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    double x = s_sum[w][l];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (l == 0) s_tot[w] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int k = 0; k < kNumSums; ++k) s[k] = s_tot[k];
+}
+
+// Exact lattice sums of every replica (hb_measure rows) become the running
+// totals that the tracked sweeps update.
+__global__ void __launch_bounds__(kTpb) hb_sync(const double* __restrict__ part, int nbx, int n_rep,
+                                                double* __restrict__ tot) {
+  double s[kNumSums];
+  sum_rows(part, 1, nbx, n_rep, blockIdx.x, s);
+  if (threadIdx.x == 0)
+    for (int k = 0; k < 7; ++k) tot[(size_t)blockIdx.x * kNumSums + k] = s[k];
+}
+
+// After a measured sweep: adds the sweep's changes (rows of the nb passes)
+// to the running totals and the totals to the point accumulators.
+__global__ void __launch_bounds__(kTpb) hb_reduce(const double* __restrict__ part, int nb, int nbx, int n_rep,
+                                                  double* __restrict__ tot, const HbRep* __restrict__ reps,
+                                                  const HbShared sh, const HbField* __restrict__ fields,
+                                                  const HbDev* __restrict__ dev, double* __restrict__ acc) {
+  const int r = blockIdx.x;
+  double s[kNumSums];
+  sum_rows(part, nb, nbx, n_rep, r, s);
+  if (threadIdx.x == 0) {
+    double* T = tot + (size_t)r * kNumSums;
+    for (int k = 0; k < 7; ++k) T[k] += s[k];
+    T[2] = sh.bx * T[4] + sh.by * T[5] + sh.bz * T[6];  // sum s.b = M.b
+    for (int k = 0; k < 7; ++k) s[k] = T[k];
     const HbDev d = *dev;
     const HbRep rp = reps[r];
-    const double h = fields[d.point];
+    const double h = fields[d.point].h;
     const double m2 = s[4] * s[4] + s[5] * s[5] + s[6] * s[6];
     const double m = sqrt(m2);
     const double e = -2.0 * rp.J * s[0] + rp.K * s[1] + sh.zsign * h * s[2] - rp.Kc * s[3];
@@ -371,37 +522,42 @@ __global__ void hb_export(const R* base, uint32_t ncell, int nb, double* __restr
 }
 
 // ------------------------------------------------------------ dispatch
-using PassFn = void (*)(const void* args, const HbRep* reps, const HbShared& sh, const double* fields,
+using PassFn = void (*)(const void* args, const HbRep* reps, const HbShared& sh, const HbField* fields,
                         const HbDev* dev, uint32_t t, double* part, dim3 grid, cudaStream_t s);
 
-template <typename R, int NB, int CLS, int W, bool MEASURE, int PROP>
-void pass_launch(const void* args, const HbRep* reps, const HbShared& sh, const double* fields, const HbDev* dev,
+template <typename R, int NB, int CLS, int W, bool COUNT, int PROP>
+void pass_launch(const void* args, const HbRep* reps, const HbShared& sh, const HbField* fields, const HbDev* dev,
                  uint32_t t, double* part, dim3 grid, cudaStream_t s) {
-  hb_pass<R, NB, CLS, W, MEASURE, PROP>
-      <<<grid, kTpb, 0, s>>>(*static_cast<const HbArgs<R>*>(args), reps, sh, fields, dev, t, part);
+  hb_pass<R, NB, CLS, W, COUNT, PROP>
+      <<<grid, kPassTpb, 0, s>>>(*static_cast<const HbArgs<R>*>(args), reps, sh, fields, dev, t, part);
 }
 
-template <typename R, int NB, int W, bool MEASURE, int PROP>
+template <typename R, int NB, int W, bool COUNT, int PROP>
 PassFn pick_cls(int cls) {
   switch (cls) {
-    case 0: return pass_launch<R, NB, 0, W, MEASURE, PROP>;
-    case 1: return pass_launch<R, NB, 1, W, MEASURE, PROP>;
-    case 2: return NB == 4 ? pass_launch<R, NB, (NB == 4 ? 2 : 0), W, MEASURE, PROP> : nullptr;
-    default: return NB == 4 ? pass_launch<R, NB, (NB == 4 ? 3 : 0), W, MEASURE, PROP> : nullptr;
+    case 0: return pass_launch<R, NB, 0, W, COUNT, PROP>;
+    case 1: return pass_launch<R, NB, 1, W, COUNT, PROP>;
+    case 2: return NB == 4 ? pass_launch<R, NB, (NB == 4 ? 2 : 0), W, COUNT, PROP> : nullptr;
+    default: return NB == 4 ? pass_launch<R, NB, (NB == 4 ? 3 : 0), W, COUNT, PROP> : nullptr;
   }
 }
 
 template <typename R, int NB, int W>
-PassFn pick_mp(int cls, bool measure, int proposal) {
+PassFn pick_mp(int cls, bool count, int proposal) {
   if (proposal == VG_PROPOSE_RANDOM)
-    return measure ? pick_cls<R, NB, W, true, VG_PROPOSE_RANDOM>(cls) : pick_cls<R, NB, W, false, VG_PROPOSE_RANDOM>(cls);
-  return measure ? pick_cls<R, NB, W, true, VG_PROPOSE_FLIP>(cls) : pick_cls<R, NB, W, false, VG_PROPOSE_FLIP>(cls);
+    return count ? pick_cls<R, NB, W, true, VG_PROPOSE_RANDOM>(cls) : pick_cls<R, NB, W, false, VG_PROPOSE_RANDOM>(cls);
+  return count ? pick_cls<R, NB, W, true, VG_PROPOSE_FLIP>(cls) : pick_cls<R, NB, W, false, VG_PROPOSE_FLIP>(cls);
 }
 
-PassFn pick_pass(bool fp64, int nb, int w, int cls, bool measure, int proposal) {
-  if (fp64) return nb == 2 ? pick_mp<double, 2, 1>(cls, measure, proposal) : pick_mp<double, 4, 1>(cls, measure, proposal);
-  if (w == 4) return nb == 2 ? pick_mp<float, 2, 4>(cls, measure, proposal) : pick_mp<float, 4, 4>(cls, measure, proposal);
-  return nb == 2 ? pick_mp<float, 2, 1>(cls, measure, proposal) : pick_mp<float, 4, 1>(cls, measure, proposal);
+PassFn pick_pass(bool fp64, int nb, int w, int cls, bool count, int proposal) {
+  if (fp64) return nb == 2 ? pick_mp<double, 2, 1>(cls, count, proposal) : pick_mp<double, 4, 1>(cls, count, proposal);
+  if (w == 4) return nb == 2 ? pick_mp<float, 2, 4>(cls, count, proposal) : pick_mp<float, 4, 4>(cls, count, proposal);
+  return nb == 2 ? pick_mp<float, 2, 1>(cls, count, proposal) : pick_mp<float, 4, 1>(cls, count, proposal);
+}
+
+template <typename R, int NB, int W>
+void measure_launch(const HbArgs<R>& a, const HbShared& sh, double* part, dim3 grid, cudaStream_t s) {
+  hb_measure<R, NB, W><<<grid, kPassTpb, 0, s>>>(a, sh, part);
 }
 
 }  // namespace
@@ -420,7 +576,9 @@ struct vg_hbatch {
   void* d_spin = nullptr;
   HbRep* d_reps = nullptr;
   double* d_part = nullptr;
-  double* d_fields = nullptr;
+  double* d_mpart = nullptr;     // hb_measure rows [replica][block]
+  double* d_tot = nullptr;       // running totals [replica][kNumSums]
+  HbField* d_fields = nullptr;
   int fields_cap = 0;
   double* d_acc = nullptr;
   size_t acc_points = 0;
@@ -469,6 +627,8 @@ void hdestroy(vg_hbatch* b) {
   cudaFree(b->d_spin);
   cudaFree(b->d_reps);
   cudaFree(b->d_part);
+  cudaFree(b->d_mpart);
+  cudaFree(b->d_tot);
   cudaFree(b->d_fields);
   cudaFree(b->d_acc);
   cudaFree(b->d_dev);
@@ -490,17 +650,41 @@ int enqueue_sweep(vg_hbatch* b, uint32_t t, bool measure) {
     VG_HCUDA(b, cudaGetLastError());
   }
   if (measure) {
-    hb_reduce<<<b->n_rep, kTpb, 0, b->stream>>>(b->d_part, b->nb, b->nbx, b->n_rep, b->d_reps, b->sh, b->d_fields,
-                                                b->d_dev, b->d_acc);
+    hb_reduce<<<b->n_rep, kTpb, 0, b->stream>>>(b->d_part, b->nb, b->nbx, b->n_rep, b->d_tot, b->d_reps, b->sh,
+                                                b->d_fields, b->d_dev, b->d_acc);
     VG_HCUDA(b, cudaGetLastError());
   }
   return VG_OK;
 }
 
+// Exact sums of the current state into the running totals.
+int enqueue_sync(vg_hbatch* b) {
+  const dim3 grid((unsigned)b->nbx, (unsigned)b->n_rep);
+  if (b->fp64) {
+    if (b->nb == 2) measure_launch<double, 2, 1>(b->a64, b->sh, b->d_mpart, grid, b->stream);
+    else measure_launch<double, 4, 1>(b->a64, b->sh, b->d_mpart, grid, b->stream);
+  } else if (b->w == 4) {
+    if (b->nb == 2) measure_launch<float, 2, 4>(b->a32, b->sh, b->d_mpart, grid, b->stream);
+    else measure_launch<float, 4, 4>(b->a32, b->sh, b->d_mpart, grid, b->stream);
+  } else {
+    if (b->nb == 2) measure_launch<float, 2, 1>(b->a32, b->sh, b->d_mpart, grid, b->stream);
+    else measure_launch<float, 4, 1>(b->a32, b->sh, b->d_mpart, grid, b->stream);
+  }
+  VG_HCUDA(b, cudaGetLastError());
+  hb_sync<<<b->n_rep, kTpb, 0, b->stream>>>(b->d_mpart, b->nbx, b->n_rep, b->d_tot);
+  VG_HCUDA(b, cudaGetLastError());
+  return VG_OK;
+}
+
+// One field point: relax sweeps, exact sums, measured (tracked) sweeps,
+// counter advance.
 int enqueue_point(vg_hbatch* b, uint32_t relax, uint32_t measure) {
   int rc;
-  for (uint32_t t = 0; t < relax + measure; ++t)
-    if ((rc = enqueue_sweep(b, t, t >= relax))) return rc;
+  for (uint32_t t = 0; t < relax; ++t)
+    if ((rc = enqueue_sweep(b, t, false))) return rc;
+  if (measure && (rc = enqueue_sync(b))) return rc;
+  for (uint32_t t = relax; t < relax + measure; ++t)
+    if ((rc = enqueue_sweep(b, t, true))) return rc;
   hb_advance<<<1, 1, 0, b->stream>>>(b->d_dev, relax + measure);
   VG_HCUDA(b, cudaGetLastError());
   return VG_OK;
@@ -560,7 +744,7 @@ int vg_hbatch_create(const vg_hbatch_desc* d, const vg_heis_replica* reps, int32
   b->ncell = (uint32_t)ncell;
   b->w = (!b->fp64 && L.nx % 4 == 0) ? 4 : 1;
   const uint32_t runs = b->ncell / (uint32_t)b->w;
-  b->nbx = (int)std::min<uint32_t>((runs + kTpb - 1) / kTpb, 4096u);
+  b->nbx = (int)std::min<uint32_t>((runs + kPassTpb - 1) / kPassTpb, 4096u);
   auto fill = [&](auto& a) {
     a.ncell = b->ncell;
     a.nx = L.nx;
@@ -584,7 +768,9 @@ int vg_hbatch_create(const vg_hbatch_desc* d, const vg_heis_replica* reps, int32
   double ax[3], bx[3];
   unit(d->anisotropy_axis, ax);
   unit(d->field_axis, bx);
-  b->sh = HbShared{ax[0], ax[1], ax[2], bx[0], bx[1], bx[2], d->zeeman_sign};
+  b->sh = HbShared{ax[0], ax[1], ax[2], bx[0], bx[1], bx[2], d->zeeman_sign,
+                   (float)ax[0], (float)ax[1], (float)ax[2], (float)bx[0], (float)bx[1], (float)bx[2],
+                   (float)d->zeeman_sign, 0.f};
 
   std::vector<HbRep> h(n_rep);
   for (int r = 0; r < n_rep; ++r) {
@@ -602,6 +788,10 @@ int vg_hbatch_create(const vg_hbatch_desc* d, const vg_heis_replica* reps, int32
     h[r].J = q.exchange;
     h[r].K = q.anisotropy;
     h[r].Kc = q.cubic;
+    h[r].fbeta = (float)h[r].beta;
+    h[r].fJ = (float)q.exchange;
+    h[r].fK = (float)q.anisotropy;
+    h[r].fKc = (float)q.cubic;
   }
   const size_t planes = (size_t)n_rep * nb * 3 * b->ncell;
   int rc = 0;
@@ -618,6 +808,8 @@ int vg_hbatch_create(const vg_hbatch_desc* d, const vg_heis_replica* reps, int32
   }
   if (!rc) rc = halloc(b, &b->d_reps, (size_t)n_rep);
   if (!rc) rc = halloc(b, &b->d_part, (size_t)nb * n_rep * b->nbx * kNumSums);
+  if (!rc) rc = halloc(b, &b->d_mpart, (size_t)n_rep * b->nbx * kNumSums);
+  if (!rc) rc = halloc(b, &b->d_tot, (size_t)n_rep * kNumSums);
   if (!rc) rc = halloc(b, &b->d_dev, 1);
   if (!rc) rc = halloc(b, &b->d_flag, 1);
   if (!rc) rc = halloc(b, &b->d_fields, 1);
@@ -627,12 +819,13 @@ int vg_hbatch_create(const vg_hbatch_desc* d, const vg_heis_replica* reps, int32
     return hfail(nullptr, rc, e);
   }
   b->fields_cap = 1;
-  const double zero = 0.0;
+  const HbField zero{0.0, 0.f, 0.f};
   const HbDev d0{0u, 0};
   cudaError_t e = cudaMemcpyAsync(b->d_reps, h.data(), sizeof(HbRep) * n_rep, cudaMemcpyHostToDevice, b->stream);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_fields, &zero, sizeof(double), cudaMemcpyHostToDevice, b->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_fields, &zero, sizeof(HbField), cudaMemcpyHostToDevice, b->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_dev, &d0, sizeof(HbDev), cudaMemcpyHostToDevice, b->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(b->d_spin, 0, planes * (b->fp64 ? 8 : 4), b->stream);
+
   if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
   if (e != cudaSuccess) {
     hdestroy(b);
@@ -755,7 +948,9 @@ int vg_hbatch_run_async(vg_hbatch* b, const double* fields, int32_t n_points, ui
     cudaGraphExecDestroy(b->graph);
     b->graph = nullptr;
   }
-  VG_HCUDA(b, cudaMemcpyAsync(b->d_fields, fields, sizeof(double) * n_points, cudaMemcpyHostToDevice, b->stream));
+  std::vector<HbField> fv((size_t)n_points);
+  for (int i = 0; i < n_points; ++i) fv[i] = HbField{fields[i], (float)fields[i], 0.f};
+  VG_HCUDA(b, cudaMemcpyAsync(b->d_fields, fv.data(), sizeof(HbField) * n_points, cudaMemcpyHostToDevice, b->stream));
   VG_HCUDA(b, cudaMemsetAsync(b->d_acc, 0, sizeof(double) * n_points * b->n_rep * kHbSums, b->stream));
   const HbDev d0{(uint32_t)b->sweep, 0};
   VG_HCUDA(b, cudaMemcpyAsync(b->d_dev, &d0, sizeof(d0), cudaMemcpyHostToDevice, b->stream));
@@ -811,9 +1006,10 @@ int vg_hbatch_point_sums(vg_hbatch* b, double* out, int64_t cap) {
 int vg_hbatch_time_passes(vg_hbatch* b, uint32_t n, double* ms) {
   if (!b || !ms || n == 0) return VG_ERR_INVALID_ARG;
   VG_HCUDA(b, cudaSetDevice(b->device));
-  const double zero = 0.0;
+  const HbField zero{0.0, 0.f, 0.f};
   const HbDev d0{(uint32_t)b->sweep, 0};
-  VG_HCUDA(b, cudaMemcpyAsync(b->d_fields, &zero, sizeof(double), cudaMemcpyHostToDevice, b->stream));
+  VG_HCUDA(b, cudaMemcpyAsync(b->d_fields, &zero, sizeof(HbField), cudaMemcpyHostToDevice, b->stream));
+  VG_HCUDA(b, cudaStreamSynchronize(b->stream));
   VG_HCUDA(b, cudaMemcpyAsync(b->d_dev, &d0, sizeof(d0), cudaMemcpyHostToDevice, b->stream));
   cudaEvent_t e0, e1;
   VG_HCUDA(b, cudaEventCreate(&e0));

@@ -18,6 +18,41 @@ __device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
 __device__ __forceinline__ float exp_(float x) { return expf(x); }
 __device__ __forceinline__ double exp_(double x) { return exp(x); }
 
+// Uniform variates from Philox words without the integer-to-float
+// conversion instruction (it issues to the FP64 pipe, which is narrow on
+// this part): k * 2^-24 for k < 2^24 is built exactly from the 23 high bits
+// as the mantissa of a number in [1, 2), minus 1, plus 2^-24 if k is odd.
+__device__ __forceinline__ float u24_unit(uint32_t k) {
+  const float hi = __uint_as_float(0x3F800000u | (k >> 1)) - 1.0f;
+  return hi + __uint_as_float((k & 1u) * 0x33800000u);
+}
+
+// (2k + 1 - 2^24) * 2^-24 for k < 2^24 (an odd multiple of 2^-24 in (-1, 1)).
+__device__ __forceinline__ float z_unit(uint32_t k) {
+  const int m = (int)(k << 1) + 1 - (1 << 24);
+  const uint32_t a = (uint32_t)(m < 0 ? -m : m);
+  return __uint_as_float(__float_as_uint(u24_unit(a)) | ((uint32_t)m & 0x80000000u));
+}
+
+// The three variates of a proposal and its acceptance: z in (-1, 1), the
+// azimuth t in [0, 2) (angle pi t) and u in [0, 1), each a 24-bit value.
+template <typename R>
+__device__ __forceinline__ void draw_zt(const uint4& w, R& z, R& t) {
+  if constexpr (sizeof(R) == 4) {
+    z = z_unit(w.x >> 8);
+    t = 2.0f * u24_unit(w.y >> 8);
+  } else {
+    z = (R)((int)((w.x >> 8) << 1) + 1 - (1 << 24)) * (R)(1.0 / 16777216.0);
+    t = (R)(w.y >> 8) * (R)(1.0 / 8388608.0);
+  }
+}
+
+template <typename R>
+__device__ __forceinline__ R draw_u(const uint4& w) {
+  if constexpr (sizeof(R) == 4) return u24_unit(w.z >> 8);
+  else return (R)(w.z >> 8) * (R)(1.0 / 16777216.0);
+}
+
 template <typename R>
 struct V3 {
   R x, y, z;
@@ -37,8 +72,8 @@ __device__ __forceinline__ bool heis_update(const V3<R>& s, const V3<R>& h, cons
   V3<R> p;
   if (PROP == VG_PROPOSE_RANDOM) {
     // z = (2k + 1 - 2^24) / 2^24 is exact in FP32; azimuth pi * t, t in [0, 2)
-    const R z = (R)((int)((w.x >> 8) << 1) + 1 - (1 << 24)) * (R)(1.0 / 16777216.0);
-    const R t = (R)(w.y >> 8) * (R)(1.0 / 8388608.0);
+    R z, t;
+    draw_zt<R>(w, z, t);
     R sn, cs;
     sincospi_(t, &sn, &cs);
     const R r = sqrt_(((R)1 - z) * ((R)1 + z));
@@ -57,7 +92,7 @@ __device__ __forceinline__ bool heis_update(const V3<R>& s, const V3<R>& h, cons
   de += P.K * (pe * pe - se * se);
   de += P.hz * (dx * P.bx + dy * P.by + dz * P.bz);
   de -= P.Kc * (quart(p) - quart(s));
-  const R u = (R)(w.z >> 8) * (R)(1.0 / 16777216.0);
+  const R u = draw_u<R>(w);
   const bool acc = de <= (R)0 || u < exp_(-de * P.beta);
   out = acc ? p : s;
   return acc;
@@ -76,11 +111,13 @@ __device__ __forceinline__ void add_site_sums(R (&acc)[kNumSums], const V3<R>& s
   acc[6] += s.z;
 }
 
-// Thread partials in R, warp sums in R, then FP64 across the block's warps
-// (a block row of kNumSums doubles).
+// Thread partials in R, warp sums in R, the block's warps summed in R in a
+// fixed order by threads 0..kNumSums-1, which store the block row of
+// kNumSums doubles (FP32 kernels convert once per value: the FP64 pipe is
+// narrow, and the FP64 combination happens across blocks).
 template <typename R>
 __device__ __forceinline__ void flush_sums(R (&acc)[kNumSums], double* part) {
-  __shared__ double red[32][kNumSums];
+  __shared__ R red[32][kNumSums];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int i = 0; i < kNumSums; ++i) {
@@ -89,18 +126,13 @@ __device__ __forceinline__ void flush_sums(R (&acc)[kNumSums], double* part) {
   }
   if (lane == 0) {
 #pragma unroll
-    for (int i = 0; i < kNumSums; ++i) red[warp][i] = (double)acc[i];
+    for (int i = 0; i < kNumSums; ++i) red[warp][i] = acc[i];
   }
   __syncthreads();
   if (threadIdx.x < kNumSums) {
-    double t = 0.0, c = 0.0;  // Kahan over the warps, in a fixed order
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
-      const double y = red[w][threadIdx.x] - c;
-      const double u = t + y;
-      c = (u - t) - y;
-      t = u;
-    }
-    part[(size_t)blockIdx.x * kNumSums + threadIdx.x] = t;
+    R t = (R)0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w][threadIdx.x];
+    part[(size_t)blockIdx.x * kNumSums + threadIdx.x] = (double)t;
   }
 }
 
