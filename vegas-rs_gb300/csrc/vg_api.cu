@@ -955,8 +955,7 @@ int vg_ctx_create_ex(const vg_lattice_desc* lat, const vg_hamiltonian_desc* ham,
   c->grid = launch_grid(c, items);
   if (is_ising(c) && sc_layout(c) && opt->blocks_per_sm <= 0) {
     // one wave of resident blocks, each thread walking several 16-site groups
-    const bool uniform = ising_table(c).zeff >= 0;
-    const long long cap = (long long)c->sm_count * ising_sc_blocks_per_sm(uniform, c->tpb);
+    const long long cap = (long long)c->sm_count * ising_sc_blocks_per_sm(ising_sc_args(c), ising_table(c), c->tpb);
     c->grid = (int)std::max(1LL, std::min((items + c->tpb - 1) / c->tpb, cap));
   }
   if ((rc = dalloc(c, (void**)&c->d_flag, sizeof(int)))) {

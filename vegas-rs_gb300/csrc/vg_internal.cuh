@@ -160,7 +160,7 @@ struct HeisParams {
 // Heisenberg).  update = false only measures.
 cudaError_t launch_ising_sc(const IsingScArgs& a, const IsingTable& tab, RngKey key, int colour,
                             int proposal, bool update, long long* part, int grid, int tpb, cudaStream_t s);
-int ising_sc_blocks_per_sm(bool uniform, int tpb);
+int ising_sc_blocks_per_sm(const IsingScArgs& a, const IsingTable& tab, int tpb);
 size_t ising_resident_smem(const IsingScArgs& a);
 cudaError_t launch_ising_resident(const IsingScArgs& a, const IsingTable& tab, RngKey key, int proposal,
                                   uint32_t n_sweeps, double* sums, int tpb, cudaStream_t s);

@@ -88,12 +88,14 @@ __device__ __forceinline__ uint32_t nibble_selector(uint32_t a) {
   const uint32_t y = (a | (a >> 4)) & 0x00770077u;
   return (y | (y >> 8)) & 0x7777u;
 }
-// 0x01 in each byte where r >= t (unsigned): two 16-bit lanes per word, the
-// borrow of 0x100 + r - t never crosses a lane.
-__device__ __forceinline__ uint32_t bytes_ge(uint32_t r, uint32_t t) {
-  const uint32_t e = ((r & 0x00FF00FFu) | 0x01000100u) - (t & 0x00FF00FFu);
-  const uint32_t o = (((r >> 8) & 0x00FF00FFu) | 0x01000100u) - ((t >> 8) & 0x00FF00FFu);
-  return ((e >> 8) & 0x00010001u) | (o & 0x01000100u);
+// 0x80 in each byte where t > r (unsigned): the carry out of each byte of
+// t + ~r (= 255 + t - r), a majority of bit 7 of t, bit 7 of ~r and the
+// carry into bit 7 (bit 7 of the 7-bit partial sums, which cannot overflow
+// into the next byte).
+__device__ __forceinline__ uint32_t bytes_gt80(uint32_t t, uint32_t r) {
+  const uint32_t nr = ~r;
+  const uint32_t s = (t & 0x7F7F7F7Fu) + (nr & 0x7F7F7F7Fu);
+  return ((t & nr) | ((t | nr) & s)) & 0x80808080u;
 }
 // 0x01 in each byte of x that is zero
 __device__ __forceinline__ uint32_t bytes_zero(uint32_t x) {
@@ -309,7 +311,7 @@ __global__ void __launch_bounds__(256, UNIFORM ? 4 : 2) ising_sc_kernel(const Is
             const uint32_t sm = S[i] * 0xFFu;
             thr[i] = (__byte_perm(tab.top[1][0], tab.top[1][1], sel) & sm) |
                      (__byte_perm(tab.top[0][0], tab.top[0][1], sel) & ~sm);
-            F[i] = (bytes_ge(R[i], thr[i]) ^ 0x01010101u) & cand[i];
+            F[i] = (bytes_gt80(thr[i], R[i]) >> 7) & cand[i];
             const uint32_t x = R[i] ^ thr[i];
             anytie |= (x - 0x01010101u) & ~x & 0x80808080u;  // nonzero iff some byte of x is zero
           }
@@ -378,6 +380,216 @@ __global__ void __launch_bounds__(256, UNIFORM ? 4 : 2) ising_sc_kernel(const Is
     }
   }
   if (UNIFORM && UPDATE && qn > 0) drain(qn);
+  if (MEASURE) block_sum3_store(bond, ups, nacc, part + (size_t)blockIdx.x * kNumSums);
+}
+
+// Two 16-site groups per thread (32 consecutive class sites of a row; rows
+// hold an even number of groups), uniform coordination only.  Index
+// arithmetic, neighbour rows and the x-edge byte are shared by the pair;
+// every group draws and decides exactly as in ising_sc_kernel (same Philox
+// blocks, same tie resolution), so results are identical.  ALLPER: all axes
+// periodic, no missing rows.
+constexpr int kSc2MinBlocks = 3;  // 80 registers: the pair state stays in registers
+template <int C, bool MEASURE, bool UPDATE, int PROP, bool ALLPER>
+__global__ void __launch_bounds__(256, kSc2MinBlocks) ising_sc2_kernel(const IsingScArgs a, const FastDiv fG2, const IsingTable tab,
+                                                           const RngKey key, long long* __restrict__ part) {
+  constexpr int Z = 6, W = 2 * Z + 1;
+  constexpr int kQ = 64;  // per-warp tie queue
+  __shared__ unsigned long long s_thr[2 * W];
+  __shared__ uint2 s_q[8][kQ];
+  pdl_launch_dependents();
+  for (int i = threadIdx.x; i < 2 * W; i += blockDim.x) s_thr[i] = tab.thr[i];
+  __syncthreads();
+  pdl_wait();
+
+  uint8_t* __restrict__ own = a.cls[C];
+  const uint8_t* __restrict__ oth = a.cls[C ^ 1];
+  const uint32_t zoff = (uint32_t)(Z - tab.zeff) * 0x01010101u;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int G2 = a.G >> 1;
+  const uint32_t pairs = a.groups >> 1;
+  int bond = 0, ups = 0, nacc = 0;
+  int qn = 0;  // warp-uniform queue length
+
+  auto drain = [&](int n) {
+    __syncwarp();
+    if (lane < n) {
+      const uint2 e = s_q[warp][lane];
+      const int k = (int)(e.y & 15u);
+      const uint32_t s01 = (e.y >> 4) & 1u, nu = e.y >> 5;
+      if (resolve_tie(e.x, k, s01, nu, tab.zeff, C, s_thr, key)) {
+        own[(size_t)e.x * 16 + k] = (uint8_t)(s01 ^ 1u);
+        ups += 1 - 2 * (int)s01;
+        nacc += 1;
+        if (C == 1) bond -= 2 * (2 * (int)s01 - 1) * (2 * (int)nu - tab.zeff);
+      }
+    }
+    __syncwarp();
+    const int rest = qn - n;
+    uint2 mv = make_uint2(0, 0);
+    if (lane < rest) mv = s_q[warp][n + lane];
+    __syncwarp();
+    if (lane < rest) s_q[warp][lane] = mv;
+    __syncwarp();
+    qn = rest;
+  };
+
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < pairs; base += stride) {
+    const uint32_t q = base + lane;
+    const bool active = q < pairs;
+    uint32_t tm = 0;  // tied sites: bit k -> group 2q + (k >> 4), site k & 15
+    uint32_t S[8], A[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) S[i] = A[i] = 0u;
+    if (active) {
+      const int row = (int)fdiv(q, fG2);
+      const int h0 = (int)(q - (uint32_t)row * (uint32_t)G2) << 5;
+      const int z = (int)fdiv((uint32_t)row, a.fLy);
+      const int y = row - z * a.Ly;
+      const int p = (y + z + C) & 1;
+      const size_t rb = (size_t)row * a.Hx;
+
+      const uint4 Sa = *reinterpret_cast<const uint4*>(own + rb + h0);
+      const uint4 Sb = *reinterpret_cast<const uint4*>(own + rb + h0 + 16);
+      const uint4 Xa = __ldg(reinterpret_cast<const uint4*>(oth + rb + h0));
+      const uint4 Xb = __ldg(reinterpret_cast<const uint4*>(oth + rb + h0 + 16));
+      uint32_t e = 0;
+      if (p == 0) {
+        if (h0 > 0) e = __ldg(oth + rb + h0 - 1);
+        else if (ALLPER || a.pbx) e = __ldg(oth + rb + a.Hx - 1);
+      } else {
+        if (h0 + 32 < a.Hx) e = __ldg(oth + rb + h0 + 32);
+        else if (ALLPER || a.pbx) e = __ldg(oth + rb);
+      }
+      const uint32_t X0[8] = {Xa.x, Xa.y, Xa.z, Xa.w, Xb.x, Xb.y, Xb.z, Xb.w};
+      uint32_t X1[8];
+      if (p == 0) {
+        X1[0] = __byte_perm(e << 24, X0[0], 0x6543);
+#pragma unroll
+        for (int i = 1; i < 8; ++i) X1[i] = __byte_perm(X0[i - 1], X0[i], 0x6543);
+      } else {
+#pragma unroll
+        for (int i = 0; i < 7; ++i) X1[i] = __byte_perm(X0[i], X0[i + 1], 0x4321);
+        X1[7] = __byte_perm(X0[7], e, 0x4321);
+      }
+      const size_t plane = (size_t)a.Ly * a.Hx;
+      size_t oym, oyp, ozm, ozp;  // neighbour row offsets
+      bool hym = true, hyp = true, hzm = true, hzp = true;
+      oym = y > 0 ? rb - a.Hx : rb + (size_t)(a.Ly - 1) * a.Hx;
+      oyp = y < a.Ly - 1 ? rb + a.Hx : rb - (size_t)(a.Ly - 1) * a.Hx;
+      ozm = z > 0 ? rb - plane : rb + (size_t)(a.Lz - 1) * plane;
+      ozp = z < a.Lz - 1 ? rb + plane : rb - (size_t)(a.Lz - 1) * plane;
+      if (!ALLPER) {
+        hym = y > 0 || a.pby;
+        hyp = y < a.Ly - 1 || a.pby;
+        hzm = z > 0 || a.pbz;
+        hzp = z < a.Lz - 1 || a.pbz;
+      }
+      const uint4 zero4 = make_uint4(0, 0, 0, 0);
+      auto ld2 = [&](bool has, size_t off, uint32_t (&v)[8]) {
+        const uint4 u0 = has ? __ldg(reinterpret_cast<const uint4*>(oth + off + h0)) : zero4;
+        const uint4 u1 = has ? __ldg(reinterpret_cast<const uint4*>(oth + off + h0 + 16)) : zero4;
+        v[0] = u0.x; v[1] = u0.y; v[2] = u0.z; v[3] = u0.w;
+        v[4] = u1.x; v[5] = u1.y; v[6] = u1.z; v[7] = u1.w;
+      };
+      uint32_t Ym[8], Yp[8], Zm[8], Zp[8];
+      ld2(hym, oym, Ym);
+      ld2(hyp, oyp, Yp);
+      ld2(hzm, ozm, Zm);
+      ld2(hzp, ozp, Zp);
+      S[0] = Sa.x; S[1] = Sa.y; S[2] = Sa.z; S[3] = Sa.w;
+      S[4] = Sb.x; S[5] = Sb.y; S[6] = Sb.z; S[7] = Sb.w;
+#pragma unroll
+      for (int i = 0; i < 8; ++i) A[i] = X0[i] + X1[i] + Ym[i] + Yp[i] + Zm[i] + Zp[i];
+
+      uint32_t F[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) F[i] = 0u;
+      if (UPDATE) {
+#pragma unroll
+        for (int g = 0; g < 2; ++g) {
+          const uint32_t gid = 2u * q + (uint32_t)g;
+          uint32_t cand[4] = {0x01010101u, 0x01010101u, 0x01010101u, 0x01010101u};
+          if (PROP == VG_PROPOSE_RANDOM) {
+            const uint4 b = philox_ks(
+                make_uint4(gid, key.sweep, (kTagIsingPropose << 24) | ((uint32_t)C << 8), key.replica), key.ks);
+            const uint32_t w[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+            for (int i = 0; i < 4; ++i) cand[i] = ((~w[i] >> 7) & 0x01010101u) ^ S[4 * g + i];
+          }
+          const uint4 b = philox_ks(
+              make_uint4(gid, key.sweep, (kTagIsingAccept << 24) | ((uint32_t)C << 8), key.replica), key.ks);
+          const uint32_t R[4] = {b.x, b.y, b.z, b.w};
+          uint32_t thr[4], anytie = 0;
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            const int wi = 4 * g + i;
+            const uint32_t sel = nibble_selector(A[wi]);
+            const uint32_t sm = S[wi] * 0xFFu;
+            thr[i] = (__byte_perm(tab.top[1][0], tab.top[1][1], sel) & sm) |
+                     (__byte_perm(tab.top[0][0], tab.top[0][1], sel) & ~sm);
+            F[wi] = (bytes_gt80(thr[i], R[i]) >> 7) & cand[i];
+            const uint32_t x = R[i] ^ thr[i];
+            anytie |= (x - 0x01010101u) & ~x & 0x80808080u;  // nonzero iff some byte of x is zero
+          }
+          if (anytie) {
+#pragma unroll
+            for (int i = 0; i < 4; ++i) tm |= gather4(bytes_zero(R[i] ^ thr[i]) & cand[i]) << (16 * g + 4 * i);
+          }
+        }
+      }
+      uint32_t Sn[8], anyf = 0;
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        Sn[i] = S[i] ^ F[i];
+        anyf |= F[i];
+      }
+      if (anyf) {
+        *reinterpret_cast<uint4*>(own + rb + h0) = make_uint4(Sn[0], Sn[1], Sn[2], Sn[3]);
+        *reinterpret_cast<uint4*>(own + rb + h0 + 16) = make_uint4(Sn[4], Sn[5], Sn[6], Sn[7]);
+      }
+      if (MEASURE) {
+        int u = 0, f = 0;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          u += __popc(Sn[i]);
+          f += __popc(F[i]);
+        }
+        ups += u;
+        nacc += f;
+        if (C == 1) {  // every neighbour of class 1 has the lower colour: all bonds counted here
+          unsigned sm = 0, m = 0;
+#pragma unroll
+          for (int i = 0; i < 8; ++i) {
+            const uint32_t M = 2u * A[i] + zoff;  // neighbour sum + Z per byte
+            sm = __dp4a(Sn[i], M, sm);
+            m = __dp4a(M, 0x01010101u, m);
+          }
+          bond += 2 * (int)sm - (int)m - Z * (2 * u - 32);
+        }
+      }
+    }
+    if (UPDATE) {
+      unsigned lanes = __ballot_sync(0xffffffffu, tm != 0u);
+      while (lanes) {
+        if (qn + 32 > kQ) drain(32 < qn ? 32 : qn);
+        const int pos = qn + __popc(lanes & ((1u << lane) - 1u));
+        if (tm) {
+          const int k = __ffs(tm) - 1;
+          tm &= tm - 1u;
+          const int wi = k >> 2;
+          const uint32_t sk = (S[wi] >> (8 * (k & 3))) & 0xFFu;
+          const uint32_t nk = (A[wi] >> (8 * (k & 3))) & 0xFFu;
+          s_q[warp][pos] = make_uint2(2u * q + (uint32_t)(k >> 4), (uint32_t)(k & 15) | (sk << 4) | (nk << 5));
+        }
+        qn += __popc(lanes);
+        if (qn >= 32) drain(32);
+        lanes = __ballot_sync(0xffffffffu, tm != 0u);
+      }
+    }
+  }
+  if (UPDATE && qn > 0) drain(qn);
   if (MEASURE) block_sum3_store(bond, ups, nacc, part + (size_t)blockIdx.x * kNumSums);
 }
 
@@ -485,16 +697,49 @@ static cudaError_t sc_dispatch(const IsingScArgs& a, const IsingTable& tab, RngK
   return launch_pdl(ising_sc_kernel<C, UNIFORM, false, true, VG_PROPOSE_RANDOM>, grid, tpb, s, a, tab, key, part);
 }
 
-// Resident blocks per SM of the sc kernel (for grid sizing).
-int ising_sc_blocks_per_sm(bool uniform, int tpb) {
+template <int C, bool ALLPER>
+static cudaError_t sc2_dispatch(const IsingScArgs& a, const IsingTable& tab, RngKey key, int proposal, bool update,
+                                long long* part, int grid, int tpb, cudaStream_t s) {
+  const bool m = part != nullptr;
+  const FastDiv f2 = make_fastdiv((uint32_t)(a.G >> 1));
+  if (!update)
+    return launch_pdl(ising_sc2_kernel<C, true, false, VG_PROPOSE_FLIP, ALLPER>, grid, tpb, s, a, f2, tab, key, part);
+  if (proposal == VG_PROPOSE_FLIP) {
+    if (m) return launch_pdl(ising_sc2_kernel<C, true, true, VG_PROPOSE_FLIP, ALLPER>, grid, tpb, s, a, f2, tab, key, part);
+    return launch_pdl(ising_sc2_kernel<C, false, true, VG_PROPOSE_FLIP, ALLPER>, grid, tpb, s, a, f2, tab, key, part);
+  }
+  if (m) return launch_pdl(ising_sc2_kernel<C, true, true, VG_PROPOSE_RANDOM, ALLPER>, grid, tpb, s, a, f2, tab, key, part);
+  return launch_pdl(ising_sc2_kernel<C, false, true, VG_PROPOSE_RANDOM, ALLPER>, grid, tpb, s, a, f2, tab, key, part);
+}
+
+// Pairs of groups per thread when every site has the same coordination and
+// rows hold an even number of groups.
+static bool use_pairs(const IsingScArgs& a, const IsingTable& tab) { return tab.zeff >= 0 && a.G % 2 == 0; }
+
+// Resident blocks per SM of the sc kernel that launch_ising_sc runs for
+// these arguments (for grid sizing).
+int ising_sc_blocks_per_sm(const IsingScArgs& a, const IsingTable& tab, int tpb) {
   int n = 0;
-  if (uniform) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ising_sc_kernel<1, true, true, true, VG_PROPOSE_FLIP>, tpb, 0);
-  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ising_sc_kernel<1, false, true, true, VG_PROPOSE_FLIP>, tpb, 0);
+  if (use_pairs(a, tab))
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ising_sc2_kernel<1, true, true, VG_PROPOSE_FLIP, true>, tpb, 0);
+  else if (tab.zeff >= 0)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ising_sc_kernel<1, true, true, true, VG_PROPOSE_FLIP>, tpb, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ising_sc_kernel<1, false, true, true, VG_PROPOSE_FLIP>, tpb, 0);
   return n > 0 ? n : 1;
 }
 
 cudaError_t launch_ising_sc(const IsingScArgs& a, const IsingTable& tab, RngKey key, int colour, int proposal,
                             bool update, long long* part, int grid, int tpb, cudaStream_t s) {
+  if (use_pairs(a, tab)) {
+    const bool allper = a.pbx && a.pby && a.pbz;
+    if (colour == 0) {
+      return allper ? sc2_dispatch<0, true>(a, tab, key, proposal, update, part, grid, tpb, s)
+                    : sc2_dispatch<0, false>(a, tab, key, proposal, update, part, grid, tpb, s);
+    }
+    return allper ? sc2_dispatch<1, true>(a, tab, key, proposal, update, part, grid, tpb, s)
+                  : sc2_dispatch<1, false>(a, tab, key, proposal, update, part, grid, tpb, s);
+  }
   const bool uniform = tab.zeff >= 0;
   if (colour == 0) {
     return uniform ? sc_dispatch<0, true>(a, tab, key, proposal, update, part, grid, tpb, s)
