@@ -206,6 +206,7 @@ def run_batched(V, torch, args):
     rounds = 20  # 200 sweeps per step, as the plain path
     with V.Batch(groups, J=1.0, seed=SEED, sweeps_per_round=10, exchange=True) as b:
         b.init_random()
+        shape, tune_ms = b.autotune(rounds=3)  # times every launch shape, restores the state
         for _ in range(max(args.warmup, 1)):
             b.run(rounds)
         s = torch.cuda.ExternalStream(b.stream())
@@ -225,6 +226,8 @@ def run_batched(V, torch, args):
             "workload": "256 replicas: 64 x 2D 64^2, 64 x 2D 512^2 (T 2.0-2.6), 64 x 3D 32^3, 64 x 3D 128^3 "
                         "(T 4.2-4.8), geometric ladders, multi-spin coded 32 per word, exchange every 10 sweeps",
             "bytes_per_flip": 0.375,
+            "tuning": {"threads_per_block": shape[0], "words_per_thread": shape[1], "words_in_flight": shape[2],
+                       "ms_per_round_when_tuned": tune_ms},
             "swap_acceptance_3d128": float(acc[:-1].sum() / max(att[:-1].sum(), 1))}
 
 

@@ -129,6 +129,8 @@ typedef struct {
 const char* vg_status_string(int status);
 int vg_abi_version(void);
 int vg_device_count(int32_t* count);
+/* Name of a CUDA device (for tuning caches); NUL-terminated, truncated to capacity. */
+int vg_device_name(int32_t device, char* name, int32_t capacity);
 
 /* ------------------------------------------------------------- lifecycle */
 /* Defaults: flip proposal for Ising, random proposal for Heisenberg (the
@@ -224,6 +226,23 @@ int vg_batch_destroy(vg_batch* batch);
 const char* vg_batch_last_error(const vg_batch* batch);
 int vg_batch_get_info(const vg_batch* batch, vg_batch_info* out);
 int vg_batch_get_stream(const vg_batch* batch, void** cuda_stream);
+/* Launch shape of the multi-spin-coded passes.  Every supported shape gives
+ * identical results: threads_per_block 128 or 256, words_per_thread 2, 4 or
+ * 8 (a block covers threads x words consecutive words), words_in_flight 1 or
+ * 2 (words a thread decides together).  Default {256, 4, 1}. */
+typedef struct {
+  int32_t threads_per_block;
+  int32_t words_per_thread;
+  int32_t words_in_flight;
+} vg_batch_tuning;
+int vg_batch_get_tuning(const vg_batch* batch, vg_batch_tuning* out);
+int vg_batch_set_tuning(vg_batch* batch, const vg_batch_tuning* tuning);
+/* Times every supported shape over `rounds` rounds (after one warm-up
+ * round each) on this batch and keeps the fastest.  The spins, ladders,
+ * tables, counters and the last run's observables are saved before and
+ * restored after, so the batch continues exactly as if it had not been
+ * tuned.  best / best_ms_per_round may be NULL. */
+int vg_batch_autotune(vg_batch* batch, uint32_t rounds, vg_batch_tuning* best, double* best_ms_per_round);
 /* Every replica random (bit l of Philox(site, 0, tag, word)), ladder reset. */
 int vg_batch_init_random(vg_batch* batch);
 /* rounds x sweeps_per_round sweeps (synchronous / enqueue only). */

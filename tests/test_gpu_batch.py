@@ -92,3 +92,70 @@ def test_batch_rejects_bad_groups(V):
         V.Batch([(V.Lattice.sc(16, 16, 1, pbc=(True, True, False)), np.ones(20))])
     with pytest.raises(V.VegasGpuError):
         V.Batch([(V.Lattice.bcc(4, 4, 4), np.ones(32))])
+
+
+def _snapshot(b, groups):
+    spins = [[b.get_replica(gi, r) for r in range(t.size)] for gi, (_, t) in enumerate(groups)]
+    ladders = [b.ladder(gi) for gi in range(len(groups))]
+    stats = [b.swap_stats(gi) for gi in range(len(groups))]
+    return spins, ladders, stats
+
+
+@pytest.mark.parametrize("shape", [(128, 2, 1), (128, 8, 2), (256, 2, 2), (256, 8, 1)])
+def test_every_launch_shape_gives_the_oracle_result(V, O, shape):
+    seed, every, rounds = 17, 2, 3
+    gpu, cpu = _groups(V, O)
+    ref = O.MscBatch(cpu)
+    ref.init(seed)
+    with V.Batch(gpu, J=1.0, seed=seed, sweeps_per_round=every, exchange=True) as b:
+        b.set_tuning(*shape)
+        assert b.tuning() == shape
+        b.init_random()
+        b.run(rounds)
+        obs_ref, _ = ref.run(1.0, seed, 0, 0, every, rounds, True)
+        for gi, g in enumerate(ref.groups):
+            for r in (0, 13, g["temps"].size - 1):
+                assert np.array_equal(b.get_replica(gi, r), g["spins"][r]), (shape, gi, r)
+            assert np.array_equal(b.ladder(gi), g["tau"])
+        for rd in range(rounds):
+            assert np.array_equal(b.observables(rd)[0], obs_ref[rd])
+
+
+def test_autotune_leaves_the_trajectory_unchanged(V, O, tmp_path):
+    seed, every = 23, 2
+    gpu, _ = _groups(V, O)
+    with V.Batch(gpu, J=1.0, seed=seed, sweeps_per_round=every) as a, \
+            V.Batch(gpu, J=1.0, seed=seed, sweeps_per_round=every) as c:
+        a.init_random()
+        c.init_random()
+        a.run(3)
+        c.run(3)
+        obs_before = [a.observables(rd)[0] for rd in range(3)]
+        cache = str(tmp_path / "tune.json")
+        shape, ms = a.autotune(rounds=1, cache=cache)
+        assert ms is not None and ms > 0 and a.tuning() == shape
+        # the last run's observables and the counters survive the tuning rounds
+        assert [np.array_equal(a.observables(rd)[0], o) for rd, o in enumerate(obs_before)] == [True] * 3
+        assert a.info().sweep_index == c.info().sweep_index and a.info().round_index == c.info().round_index
+        a.run(2)
+        c.run(2)
+        sa, sc = _snapshot(a, gpu), _snapshot(c, gpu)
+        for x, y in zip(sa[0], sc[0]):
+            for u, v in zip(x, y):
+                assert np.array_equal(u, v)
+        for x, y in zip(sa[1], sc[1]):
+            assert np.array_equal(x, y)
+        for (x1, x2), (y1, y2) in zip(sa[2], sc[2]):
+            assert np.array_equal(x1, y1) and np.array_equal(x2, y2)
+        # a second batch of the same shape takes the cached shape without timing
+        with V.Batch(gpu, J=1.0, seed=1, sweeps_per_round=every) as d:
+            shape2, ms2 = d.autotune(cache=cache)
+            assert shape2 == shape and ms2 is None and d.tuning() == shape
+
+
+def test_unsupported_tuning_is_rejected(V, O):
+    gpu, _ = _groups(V, O)
+    with V.Batch(gpu, J=1.0, seed=1) as b:
+        with pytest.raises(V.VegasGpuError) as e:
+            b.set_tuning(512, 4, 1)
+        assert e.value.status == 5

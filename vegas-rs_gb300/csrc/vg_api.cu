@@ -825,6 +825,17 @@ int vg_device_count(int32_t* count) {
   return e == cudaSuccess ? VG_OK : fail(nullptr, VG_ERR_NO_DEVICE, cudaGetErrorString(e));
 }
 
+int vg_device_name(int32_t device, char* name, int32_t capacity) {
+  if (!name || capacity < 1) return VG_ERR_INVALID_ARG;
+  name[0] = '\0';
+  cudaDeviceProp prop;
+  const cudaError_t e = cudaGetDeviceProperties(&prop, device);
+  if (e != cudaSuccess) return fail(nullptr, VG_ERR_NO_DEVICE, cudaGetErrorString(e));
+  std::strncpy(name, prop.name, (size_t)capacity - 1);
+  name[capacity - 1] = '\0';
+  return VG_OK;
+}
+
 int vg_options_default(int32_t spin_kind, vg_options* o) {
   if (!o || (spin_kind != VG_SPIN_ISING && spin_kind != VG_SPIN_HEISENBERG)) return VG_ERR_INVALID_ARG;
   std::memset(o, 0, sizeof(*o));

@@ -179,14 +179,18 @@ __device__ __forceinline__ WordState<ZZ / 2> msc_word_start(const MscSeg& sg, ui
   return w;
 }
 
-constexpr int kWordsPerThread = 4;  // block covers 256 x 4 consecutive words of one segment
-
+// Launch shape of a pass (chosen by the autotuner, vg_batch_autotune): a
+// block of TPB threads covers TPB x WPT consecutive words of one segment;
+// each thread takes its WPT words WIF at a time (WIF = 2 interleaves two
+// independent words' Philox chains and loads).  Every shape makes the same
+// decisions for every word.
+//
 // Words still undecided after 8 planes are queued per warp and finished 32
 // at a time, so the rare long comparisons run with full warps.
 constexpr int kQueue = 64;          // per-warp queue entries
 constexpr int kQueueWords = 4 + 3;  // j, s, und, acc, m[<= 3]
 
-template <int C, int ZZ>
+template <int C, int ZZ, int TPB, int WPT, int WIF>
 __device__ __forceinline__ void msc_pass_body(const MscSeg& sg, uint32_t j0, uint32_t* own, const uint32_t* oth,
                                               const uint32_t* s_tab, uint32_t sweep, const KeySchedule& ks,
                                               int jsign, uint32_t (*s_q)[kQueue][kQueueWords]) {
@@ -221,42 +225,47 @@ __device__ __forceinline__ void msc_pass_body(const MscSeg& sg, uint32_t j0, uin
     qn = rest;
   };
 #pragma unroll 1
-  for (int u = 0; u < kWordsPerThread; ++u) {
-    const uint32_t j = j0 + (uint32_t)(u * 256) + threadIdx.x;
-    const bool live = j < sg.n_c;
-    bool pend = false;
-    WordState<ND> w;
-    uint32_t s = 0;
-    if (live) {
-      s = own[j];
-      w = msc_word_start<C, ZZ>(sg, j, s, oth, s_tab, sweep, ks, jsign);
-      pend = w.und != 0u;
-      if (!pend && w.acc) own[j] = s ^ w.acc;
-    }
-    const unsigned pmask = __ballot_sync(0xffffffffu, pend);
-    if (pmask) {
-      if (pend) {
-        uint32_t* e = s_q[warp][qn + __popc(pmask & ((1u << lane) - 1u))];
-        e[0] = j;
-        e[1] = s;
-        e[2] = w.und;
-        e[3] = w.acc;
+  for (int u = 0; u < WPT; u += WIF) {
+    uint32_t j[WIF], s[WIF];
+    bool live[WIF], pend[WIF];
+    WordState<ND> w[WIF];
 #pragma unroll
-        for (int q = 0; q < ND; ++q) e[4 + q] = w.m[q];
+    for (int i = 0; i < WIF; ++i) {
+      j[i] = j0 + (uint32_t)((u + i) * TPB) + threadIdx.x;
+      live[i] = j[i] < sg.n_c;
+      const uint32_t jj = live[i] ? j[i] : 0u;  // dead lanes work on a valid word and discard it
+      s[i] = own[jj];
+      w[i] = msc_word_start<C, ZZ>(sg, jj, s[i], oth, s_tab, sweep, ks, jsign);
+      pend[i] = live[i] && w[i].und != 0u;
+      if (live[i] && !pend[i] && w[i].acc) own[j[i]] = s[i] ^ w[i].acc;
+    }
+#pragma unroll
+    for (int i = 0; i < WIF; ++i) {
+      const unsigned pmask = __ballot_sync(0xffffffffu, pend[i]);
+      if (pmask) {
+        if (pend[i]) {
+          uint32_t* e = s_q[warp][qn + __popc(pmask & ((1u << lane) - 1u))];
+          e[0] = j[i];
+          e[1] = s[i];
+          e[2] = w[i].und;
+          e[3] = w[i].acc;
+#pragma unroll
+          for (int q = 0; q < ND; ++q) e[4 + q] = w[i].m[q];
+        }
+        qn += __popc(pmask);
+        if (qn >= 32) finish(32);
       }
-      qn += __popc(pmask);
-      if (qn >= 32) finish(32);
     }
   }
   if (qn > 0) finish(qn);
 }
 
-template <int C>
-__global__ void __launch_bounds__(256) msc_pass(const MscSeg* __restrict__ segs, const int2* __restrict__ blocks,
+template <int C, int TPB, int WPT, int WIF>
+__global__ void __launch_bounds__(TPB) msc_pass(const MscSeg* __restrict__ segs, const int2* __restrict__ blocks,
                                                 const uint32_t* __restrict__ tabs, const MscDev* __restrict__ dev,
                                                 uint32_t t_off, KeySchedule ks, int jsign) {
   __shared__ uint32_t s_tab[kTabWords];
-  __shared__ uint32_t s_q[8][kQueue][kQueueWords];
+  __shared__ uint32_t s_q[TPB / 32][kQueue][kQueueWords];
   pdl_launch_dependents();
   const int2 bl = blocks[blockIdx.x];
   const MscSeg sg = segs[bl.x];
@@ -269,15 +278,15 @@ __global__ void __launch_bounds__(256) msc_pass(const MscSeg* __restrict__ segs,
   pdl_wait();
   uint32_t* own = sg.cls[C];
   const uint32_t* oth = sg.cls[C ^ 1];
-  if (sg.dim3) msc_pass_body<C, 6>(sg, (uint32_t)bl.y, own, oth, s_tab, sweep, ks, jsign, s_q);
-  else msc_pass_body<C, 4>(sg, (uint32_t)bl.y, own, oth, s_tab, sweep, ks, jsign, s_q);
+  if (sg.dim3) msc_pass_body<C, 6, TPB, WPT, WIF>(sg, (uint32_t)bl.y, own, oth, s_tab, sweep, ks, jsign, s_q);
+  else msc_pass_body<C, 4, TPB, WPT, WIF>(sg, (uint32_t)bl.y, own, oth, s_tab, sweep, ks, jsign, s_q);
 }
 
 // Per replica: anti-aligned bonds (over class-1 sites, whose neighbours are
 // all class 0) and up spins, added into obs[slot][replica][2].
 __global__ void __launch_bounds__(256) msc_measure(const MscSeg* __restrict__ segs, const int2* __restrict__ blocks,
-                                                   const MscDev* __restrict__ dev, int total_rep,
-                                                   unsigned long long* __restrict__ obs) {
+                                                   int words_per_block, const MscDev* __restrict__ dev,
+                                                   int total_rep, unsigned long long* __restrict__ obs) {
   __shared__ unsigned int s_cnt[2][32];
   const int2 bl = blocks[blockIdx.x];
   const MscSeg& sg = segs[bl.x];
@@ -288,10 +297,10 @@ __global__ void __launch_bounds__(256) msc_measure(const MscSeg* __restrict__ se
   __syncthreads();
   const int lane = threadIdx.x & 31;
   unsigned int ca = 0, cu = 0;
-  for (int w = 0; w < kWordsPerThread; ++w) {
+  for (int w = 0; w * 256 < words_per_block; ++w) {
     const uint32_t j = (uint32_t)bl.y + (uint32_t)(w * 256) + threadIdx.x;
     uint32_t b0 = 0, b1 = 0, b2 = 0, u0 = 0, u1 = 0;
-    if (j < sg.n_c) {
+    if (j < sg.n_c && w * 256 + (int)threadIdx.x < words_per_block) {
       const uint32_t s1 = sg.cls[1][j], s0 = sg.cls[0][j];
       uint32_t a[6];
       msc_anti(sg, 1, j, s1, sg.cls[0], a);
@@ -449,6 +458,7 @@ struct GroupHost {
 
 struct vg_batch {
   int device = 0;
+  vg_batch_tuning tune{256, 4, 1};
   cudaStream_t own_stream = nullptr, stream = nullptr;
   double J = 1.0;
   uint64_t seed = 0;
@@ -543,19 +553,58 @@ cudaError_t launch_pdl(void (*kern)(P...), dim3 grid, dim3 block, size_t smem, c
   return cudaLaunchKernelEx(&cfg, kern, std::forward<A>(args)...);
 }
 
+using MscPassFn = void (*)(const MscSeg*, const int2*, const uint32_t*, const MscDev*, uint32_t, KeySchedule, int);
+
+template <int C, int TPB>
+MscPassFn msc_pass_wpt(int wpt, int wif) {
+  if (wpt == 2) return wif == 2 ? msc_pass<C, TPB, 2, 2> : msc_pass<C, TPB, 2, 1>;
+  if (wpt == 4) return wif == 2 ? msc_pass<C, TPB, 4, 2> : msc_pass<C, TPB, 4, 1>;
+  return wif == 2 ? msc_pass<C, TPB, 8, 2> : msc_pass<C, TPB, 8, 1>;
+}
+
+template <int C>
+MscPassFn msc_pass_fn(const vg_batch_tuning& t) {
+  return t.threads_per_block == 128 ? msc_pass_wpt<C, 128>(t.words_per_thread, t.words_in_flight)
+                                    : msc_pass_wpt<C, 256>(t.words_per_thread, t.words_in_flight);
+}
+
+bool tuning_supported(const vg_batch_tuning& t) {
+  return (t.threads_per_block == 128 || t.threads_per_block == 256) &&
+         (t.words_per_thread == 2 || t.words_per_thread == 4 || t.words_per_thread == 8) &&
+         (t.words_in_flight == 1 || t.words_in_flight == 2);
+}
+
+// Block table for the current launch shape: (segment, first word) per block.
+int build_blocks(vg_batch* b) {
+  const int per = b->tune.threads_per_block * b->tune.words_per_thread;
+  b->blocks.clear();
+  for (size_t k = 0; k < b->segs.size(); ++k) {
+    const int nbl = (int)((b->segs[k].n_c + per - 1) / per);
+    for (int i = 0; i < nbl; ++i) b->blocks.push_back(make_int2((int)k, i * per));
+  }
+  cudaFree(b->d_blocks);
+  b->d_blocks = nullptr;
+  int rc = balloc(b, &b->d_blocks, b->blocks.size());
+  if (rc) return rc;
+  VG_BCUDA(b, cudaMemcpy(b->d_blocks, b->blocks.data(), sizeof(int2) * b->blocks.size(), cudaMemcpyHostToDevice));
+  return VG_OK;
+}
+
 // One round on the stream: sweeps, measurement, exchange, advance.
 int enqueue_round(vg_batch* b) {
   const int nb = (int)b->blocks.size();
+  const MscPassFn p0 = msc_pass_fn<0>(b->tune), p1 = msc_pass_fn<1>(b->tune);
+  const dim3 tpb((unsigned)b->tune.threads_per_block);
   for (int t = 0; t < b->every; ++t) {
     const int jsign = b->J > 0.0 ? 1 : b->J < 0.0 ? -1 : 0;
-    VG_BCUDA(b, launch_pdl(msc_pass<0>, dim3(nb), dim3(256), 0, b->stream, (const MscSeg*)b->d_segs,
-                           (const int2*)b->d_blocks, (const uint32_t*)b->d_tabs, (const MscDev*)b->d_dev,
-                           (uint32_t)t, b->ks, jsign));
-    VG_BCUDA(b, launch_pdl(msc_pass<1>, dim3(nb), dim3(256), 0, b->stream, (const MscSeg*)b->d_segs,
-                           (const int2*)b->d_blocks, (const uint32_t*)b->d_tabs, (const MscDev*)b->d_dev,
-                           (uint32_t)t, b->ks, jsign));
+    VG_BCUDA(b, launch_pdl(p0, dim3(nb), tpb, 0, b->stream, (const MscSeg*)b->d_segs, (const int2*)b->d_blocks,
+                           (const uint32_t*)b->d_tabs, (const MscDev*)b->d_dev, (uint32_t)t, b->ks, jsign));
+    VG_BCUDA(b, launch_pdl(p1, dim3(nb), tpb, 0, b->stream, (const MscSeg*)b->d_segs, (const int2*)b->d_blocks,
+                           (const uint32_t*)b->d_tabs, (const MscDev*)b->d_dev, (uint32_t)t, b->ks, jsign));
   }
-  msc_measure<<<nb, 256, 0, b->stream>>>(b->d_segs, b->d_blocks, b->d_dev, b->total_rep, b->d_obs);
+  msc_measure<<<nb, 256, 0, b->stream>>>(b->d_segs, b->d_blocks,
+                                         b->tune.threads_per_block * b->tune.words_per_thread, b->d_dev,
+                                         b->total_rep, b->d_obs);
   VG_BCUDA(b, cudaGetLastError());
   int maxrep = 0;
   for (auto& g : b->groups) maxrep = std::max(maxrep, g.n_rep);
@@ -703,14 +752,11 @@ int vg_batch_create(const vg_replica_group* groups, int32_t n_groups, double J, 
       s.nd = G.nd;
       for (int q = 0; q < 4; ++q) s.dn[q] = q < G.nd ? G.dn[q] : 0;
       s.rep0 = G.rep_off + 32 * w;
-      const int per = 256 * kWordsPerThread;
-      const int nbl = (int)((nc + per - 1) / per);
-      for (int k = 0; k < nbl; ++k) b->blocks.push_back(make_int2((int)b->segs.size(), k * per));
       b->segs.push_back(s);
     }
   }
   if (!rc) rc = balloc(b, &b->d_segs, b->segs.size());
-  if (!rc) rc = balloc(b, &b->d_blocks, b->blocks.size());
+  if (!rc) rc = build_blocks(b);
   if (!rc) rc = balloc(b, &b->d_tabs, b->segs.size() * kTabWords);
   if (!rc) rc = balloc(b, &b->d_groups, b->groups.size());
   if (!rc) rc = balloc(b, &b->d_dev, 1);
@@ -771,7 +817,6 @@ int vg_batch_create(const vg_replica_group* groups, int32_t n_groups, double J, 
     return bfail(nullptr, rc, e);
   }
   cudaMemcpy(b->d_segs, b->segs.data(), sizeof(MscSeg) * b->segs.size(), cudaMemcpyHostToDevice);
-  cudaMemcpy(b->d_blocks, b->blocks.data(), sizeof(int2) * b->blocks.size(), cudaMemcpyHostToDevice);
   cudaMemcpy(b->d_groups, gdev.data(), sizeof(MscGroupDev) * gdev.size(), cudaMemcpyHostToDevice);
   MscDev d0{0, 0, 0, 0};
   cudaMemcpy(b->d_dev, &d0, sizeof(d0), cudaMemcpyHostToDevice);
@@ -896,6 +941,157 @@ int vg_batch_swap_stats(vg_batch* b, int32_t group, int64_t* accepted, int64_t* 
   const GroupHost& G = b->groups[group];
   if (accepted) VG_BCUDA(b, cudaMemcpy(accepted, G.d_acc, sizeof(int64_t) * G.n_rep, cudaMemcpyDeviceToHost));
   if (attempted) VG_BCUDA(b, cudaMemcpy(attempted, G.d_att, sizeof(int64_t) * G.n_rep, cudaMemcpyDeviceToHost));
+  return VG_OK;
+}
+
+int vg_batch_get_tuning(const vg_batch* b, vg_batch_tuning* t) {
+  if (!b || !t) return VG_ERR_INVALID_ARG;
+  *t = b->tune;
+  return VG_OK;
+}
+
+int vg_batch_set_tuning(vg_batch* b, const vg_batch_tuning* t) {
+  if (!b || !t) return VG_ERR_INVALID_ARG;
+  if (!tuning_supported(*t))
+    return bfail(b, VG_ERR_UNSUPPORTED, "tuning: threads_per_block 128 or 256, words_per_thread 2, 4 or 8, "
+                                        "words_in_flight 1 or 2");
+  VG_BCUDA(b, cudaSetDevice(b->device));
+  VG_BCUDA(b, cudaStreamSynchronize(b->stream));
+  if (b->graph) {  // the captured round holds the old launch shape
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  b->tune = *t;
+  return build_blocks(b);
+}
+
+int vg_batch_autotune(vg_batch* b, uint32_t rounds, vg_batch_tuning* best, double* best_ms) {
+  if (!b || rounds == 0) return VG_ERR_INVALID_ARG;
+  VG_BCUDA(b, cudaSetDevice(b->device));
+  VG_BCUDA(b, cudaStreamSynchronize(b->stream));
+  int rc;
+  // The candidates run real rounds; everything they change is saved first
+  // and restored afterwards, so the batch continues as if never tuned.
+  size_t words = 0;
+  for (const auto& sg : b->segs) words += 2 * (size_t)sg.n_c;
+  const size_t tabs = b->segs.size() * kTabWords;
+  const size_t ring_obs = (size_t)b->last_rounds * b->total_rep * 2, ring_tau = (size_t)b->last_rounds * b->total_rep;
+  uint32_t* sv_spins = nullptr;
+  uint32_t* sv_tabs = nullptr;
+  unsigned long long* sv_obs = nullptr;
+  int* sv_ring = nullptr;
+  std::vector<int*> sv_int;
+  std::vector<unsigned long long*> sv_cnt;
+  auto release = [&]() {
+    cudaFree(sv_spins);
+    cudaFree(sv_tabs);
+    cudaFree(sv_obs);
+    cudaFree(sv_ring);
+    for (auto* p : sv_int) cudaFree(p);
+    for (auto* p : sv_cnt) cudaFree(p);
+  };
+  bool ok = cudaMalloc((void**)&sv_spins, words * 4) == cudaSuccess &&
+            cudaMalloc((void**)&sv_tabs, tabs * 4) == cudaSuccess &&
+            cudaMalloc((void**)&sv_obs, std::max<size_t>(ring_obs, 1) * 8) == cudaSuccess &&
+            cudaMalloc((void**)&sv_ring, std::max<size_t>(ring_tau, 1) * 4) == cudaSuccess;
+  for (auto& G : b->groups) {
+    int* a = nullptr;
+    unsigned long long* c = nullptr;
+    ok = ok && cudaMalloc((void**)&a, sizeof(int) * 2 * G.n_rep) == cudaSuccess;
+    sv_int.push_back(a);
+    ok = ok && cudaMalloc((void**)&c, sizeof(unsigned long long) * 2 * G.n_rep) == cudaSuccess;
+    sv_cnt.push_back(c);
+  }
+  if (!ok) {
+    release();
+    cudaGetLastError();
+    return bfail(b, VG_ERR_OOM, "autotune: no device memory for the saved state");
+  }
+  auto copy_state = [&](bool save) -> cudaError_t {
+    const cudaMemcpyKind k = cudaMemcpyDeviceToDevice;
+    cudaError_t e = save ? cudaMemcpyAsync(sv_spins, b->d_spins, words * 4, k, b->stream)
+                         : cudaMemcpyAsync(b->d_spins, sv_spins, words * 4, k, b->stream);
+    if (e == cudaSuccess)
+      e = save ? cudaMemcpyAsync(sv_tabs, b->d_tabs, tabs * 4, k, b->stream)
+               : cudaMemcpyAsync(b->d_tabs, sv_tabs, tabs * 4, k, b->stream);
+    if (e == cudaSuccess && ring_obs)
+      e = save ? cudaMemcpyAsync(sv_obs, b->d_obs, ring_obs * 8, k, b->stream)
+               : cudaMemcpyAsync(b->d_obs, sv_obs, ring_obs * 8, k, b->stream);
+    if (e == cudaSuccess && ring_tau)
+      e = save ? cudaMemcpyAsync(sv_ring, b->d_tau_ring, ring_tau * 4, k, b->stream)
+               : cudaMemcpyAsync(b->d_tau_ring, sv_ring, ring_tau * 4, k, b->stream);
+    for (size_t g = 0; g < b->groups.size() && e == cudaSuccess; ++g) {
+      GroupHost& G = b->groups[g];
+      const size_t n = (size_t)G.n_rep;
+      int* a = sv_int[g];
+      unsigned long long* c = sv_cnt[g];
+      if (save) {
+        e = cudaMemcpyAsync(a, G.d_tau, n * 4, k, b->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(a + n, G.d_rep_at, n * 4, k, b->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(c, G.d_acc, n * 8, k, b->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(c + n, G.d_att, n * 8, k, b->stream);
+      } else {
+        e = cudaMemcpyAsync(G.d_tau, a, n * 4, k, b->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(G.d_rep_at, a + n, n * 4, k, b->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(G.d_acc, c, n * 8, k, b->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(G.d_att, c + n, n * 8, k, b->stream);
+      }
+    }
+    return e;
+  };
+  cudaError_t e = copy_state(true);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+  if (e == cudaSuccess && (rc = ensure_ring(b, rounds + 1))) {  // after the saved copy: growing drops the ring
+    release();
+    return rc;
+  }
+  const vg_batch_tuning keep = b->tune;
+  vg_batch_tuning top = keep;
+  double top_ms = 1e300;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  if (b->graph) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  static const int kTpb[2] = {128, 256}, kWpt[3] = {2, 4, 8}, kWif[2] = {1, 2};
+  for (int it = 0; it < 2 && e == cudaSuccess && !rc; ++it)
+    for (int iw = 0; iw < 3 && e == cudaSuccess && !rc; ++iw)
+      for (int ii = 0; ii < 2 && e == cudaSuccess && !rc; ++ii) {
+        b->tune = vg_batch_tuning{kTpb[it], kWpt[iw], kWif[ii]};
+        if ((rc = build_blocks(b))) break;
+        const MscDev d{(uint32_t)b->sweep, b->round, b->round, 0};
+        e = cudaMemcpyAsync(b->d_dev, &d, sizeof(d), cudaMemcpyHostToDevice, b->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+        if (e == cudaSuccess && (rc = enqueue_round(b))) break;  // warm-up round
+        if (e == cudaSuccess) e = cudaEventRecord(e0, b->stream);
+        for (uint32_t r = 0; r < rounds && e == cudaSuccess && !rc; ++r) rc = enqueue_round(b);
+        if (e == cudaSuccess) e = cudaEventRecord(e1, b->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+        float ms = 0.f;
+        if (e == cudaSuccess && !rc) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (e == cudaSuccess && !rc && ms / rounds < top_ms) {
+          top_ms = ms / rounds;
+          top = b->tune;
+        }
+      }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  // restore the state and the counters, keep the fastest shape
+  b->tune = (e == cudaSuccess && !rc) ? top : keep;
+  int rc2 = build_blocks(b);
+  const MscDev d{(uint32_t)b->sweep, b->round, b->round - (uint32_t)b->last_rounds, 0};
+  cudaError_t e2 = copy_state(false);
+  if (e2 == cudaSuccess) e2 = cudaMemcpyAsync(b->d_dev, &d, sizeof(d), cudaMemcpyHostToDevice, b->stream);
+  if (e2 == cudaSuccess) e2 = cudaStreamSynchronize(b->stream);
+  release();
+  if (rc) return rc;
+  if (e != cudaSuccess) return bfail(b, VG_ERR_CUDA, std::string("autotune: ") + cudaGetErrorString(e));
+  if (rc2) return rc2;
+  if (e2 != cudaSuccess) return bfail(b, VG_ERR_CUDA, std::string("autotune restore: ") + cudaGetErrorString(e2));
+  if (best) *best = top;
+  if (best_ms) *best_ms = top_ms;
   return VG_OK;
 }
 

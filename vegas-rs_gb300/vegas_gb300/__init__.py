@@ -16,6 +16,7 @@ All compute runs in the CUDA library; this module only marshals arguments.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from dataclasses import dataclass, field
 from typing import Optional, Sequence, Tuple
 
@@ -403,6 +404,59 @@ class Batch:
                                             att.ctypes.data_as(C.POINTER(C.c_int64))))
         return acc, att
 
+    # launch shape of the multi-spin-coded passes (results do not depend on it)
+    def tuning(self) -> Tuple[int, int, int]:
+        t = _abi.BatchTuning()
+        self._chk(lib().vg_batch_get_tuning(self._h, C.byref(t)))
+        return (t.threads_per_block, t.words_per_thread, t.words_in_flight)
+
+    def set_tuning(self, threads_per_block: int, words_per_thread: int, words_in_flight: int):
+        t = _abi.BatchTuning(threads_per_block, words_per_thread, words_in_flight)
+        self._chk(lib().vg_batch_set_tuning(self._h, C.byref(t)))
+
+    def signature(self) -> str:
+        """Shape of the batch as a tuning-cache key: per group the lattice
+        extents, periodicity and replica count."""
+        parts = []
+        for lat, temps in zip(self.lattices, self._temps):
+            d = lat.desc()
+            parts.append(f"sc{d.nx}x{d.ny}x{d.nz}p{d.pbc_x}{d.pbc_y}{d.pbc_z}r{temps.size}")
+        return "+".join(parts)
+
+    def autotune(self, rounds: int = 3, cache: Optional[str] = None):
+        """Pick the fastest launch shape for this batch on this device.
+
+        With `cache` (a JSON file), a shape stored for the same device name and
+        batch signature is applied without timing; otherwise every shape is
+        timed (vg_batch_autotune, which restores the batch's state afterwards)
+        and the winner is stored.  Returns (shape, ms per round or None)."""
+        import json
+
+        key = f"{device_name()}|{self.signature()}"
+        table = {}
+        if cache and os.path.exists(cache):
+            try:
+                with open(cache) as f:
+                    table = json.load(f)
+            except (OSError, ValueError):
+                table = {}
+        if key in table:
+            self.set_tuning(*table[key]["shape"])
+            return tuple(table[key]["shape"]), None
+        best = _abi.BatchTuning()
+        ms = C.c_double()
+        self._chk(lib().vg_batch_autotune(self._h, rounds, C.byref(best), C.byref(ms)))
+        shape = (best.threads_per_block, best.words_per_thread, best.words_in_flight)
+        if cache:
+            table[key] = {"shape": list(shape), "ms_per_round": ms.value}
+            d = os.path.dirname(os.path.abspath(cache))
+            os.makedirs(d, exist_ok=True)
+            tmp = cache + ".tmp"
+            with open(tmp, "w") as f:
+                json.dump(table, f, indent=1, sort_keys=True)
+            os.replace(tmp, cache)
+        return shape, ms.value
+
     def get_replica(self, group: int, replica: int) -> np.ndarray:
         out = np.empty(self.lattices[group].n_sites, dtype=np.int8)
         self._chk(lib().vg_batch_get_replica(self._h, group, replica, out.ctypes.data_as(C.POINTER(C.c_int8))))
@@ -562,6 +616,12 @@ def coercive_fields(fields: np.ndarray, m: np.ndarray):
                 break
         res.append(hc)
     return tuple(res)
+
+
+def device_name(device: int = 0) -> str:
+    buf = C.create_string_buffer(256)
+    _check(lib().vg_device_name(device, buf, 256))
+    return buf.value.decode()
 
 
 def device_count() -> int:

@@ -62,6 +62,10 @@ class BatchInfo(C.Structure):
                 ("round_index", C.c_uint32), ("graph", C.c_int32)]
 
 
+class BatchTuning(C.Structure):
+    _fields_ = [("threads_per_block", C.c_int32), ("words_per_thread", C.c_int32), ("words_in_flight", C.c_int32)]
+
+
 class HeisReplica(C.Structure):
     _fields_ = [("seed", C.c_uint64), ("replica", C.c_uint32), ("reserved", C.c_uint32),
                 ("temperature", C.c_double), ("exchange", C.c_double), ("anisotropy", C.c_double),
@@ -87,6 +91,7 @@ SIGNATURES = {
     "vg_status_string": (C.c_char_p, [C.c_int]),
     "vg_abi_version": (C.c_int, []),
     "vg_device_count": (C.c_int, [P(C.c_int32)]),
+    "vg_device_name": (C.c_int, [C.c_int32, C.c_char_p, C.c_int32]),
     "vg_options_default": (C.c_int, [C.c_int32, P(Options)]),
     "vg_ctx_create": (C.c_int, [P(LatticeDesc), P(HamiltonianDesc), C.c_int32, C.c_uint64, P(C.c_void_p)]),
     "vg_ctx_create_ex": (C.c_int, [P(LatticeDesc), P(HamiltonianDesc), P(Options), C.c_uint64, P(C.c_void_p)]),
@@ -124,6 +129,9 @@ SIGNATURES = {
     "vg_batch_observables": (C.c_int, [C.c_void_p, C.c_uint64, P(C.c_int64), P(C.c_int32)]),
     "vg_batch_ladder": (C.c_int, [C.c_void_p, C.c_int32, P(C.c_int32)]),
     "vg_batch_swap_stats": (C.c_int, [C.c_void_p, C.c_int32, P(C.c_int64), P(C.c_int64)]),
+    "vg_batch_get_tuning": (C.c_int, [C.c_void_p, P(BatchTuning)]),
+    "vg_batch_set_tuning": (C.c_int, [C.c_void_p, P(BatchTuning)]),
+    "vg_batch_autotune": (C.c_int, [C.c_void_p, C.c_uint32, P(BatchTuning), P(C.c_double)]),
     "vg_batch_get_replica": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, P(C.c_int8)]),
     "vg_batch_set_replica": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, P(C.c_int8)]),
     "vg_hbatch_create": (C.c_int, [P(HBatchDesc), P(HeisReplica), C.c_int32, P(C.c_void_p)]),
