@@ -231,6 +231,58 @@ def run_batched(V, torch, args):
             "swap_acceptance_3d128": float(acc[:-1].sum() / max(att[:-1].sum(), 1))}
 
 
+def run_cooldown_2d(V, torch, args):
+    """The reference's own CPU-sized case: sc 32x32x1 (PBC x, y; open z),
+    J=1, random start, Relax 1000 sweeps at T=4 then CoolDown(4.0, 0.1, 0.1)
+    with 1000 relax + 20000 measured sweeps per temperature (39 temperatures
+    by the reference's loop).  Timed on a bounded sample: the relax and the
+    first 5 temperatures (106,000 sweeps), on the resident kernel (all sweeps
+    of a call in one launch); the reference restatement runs 20,000 measured
+    sweeps of the same lattice on one host core beside it."""
+    import oracle as O
+
+    lat = V.Lattice.sc(32, 32, 1, pbc=(True, True, False))
+    H = V.hamiltonian(V.Exchange(1.0))
+    temps, t = [], 4.0
+    while True:  # CoolDown::run (src/program.rs:202-211)
+        temps.append(t)
+        t -= 0.1
+        if t < 0.1:
+            break
+    k = 5
+    with V.Engine(lat, H, spin=V.SPIN_ISING, seed=1) as eng:
+        eng.init_random()
+        path = eng.info().path
+        s = torch.cuda.ExternalStream(eng.stream())
+        a, c = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        eng.set_thermostat(4.0)
+        eng.sweeps(100)  # warm-up
+        a.record(s)
+        eng.set_thermostat(4.0)
+        eng.sweeps_async(1000, measure=False)
+        for T in temps[:k]:
+            eng.set_thermostat(T)
+            eng.sweeps_async(1000, measure=False)
+            eng.sweeps_async(20000, measure=True)
+        c.record(s)
+        eng.synchronize()
+        ms = a.elapsed_time(c)
+    sweeps = 1000 + k * 21000
+    full = 1000 + len(temps) * 21000
+    n = lat.n_sites
+    cpu = None
+    if not args.no_cpu_baseline:
+        olat = O.lattice("sc", 32, 32, 1, (1, 1, 0))
+        flips, dt = O.ref_parallel(olat, 0, O.Hamiltonian(has_exchange=1, J=1.0, compound=0), 2.0, 20000, 1,
+                                   seed=1, measure=True)
+        cpu = {"value": flips / (dt * 1e9), "unit": "flips/ns", "cores": 1, "kind": "port",
+               "sample": "20,000 measured reference sweeps of the 32x32x1 lattice at T=2.0 on one core"}
+    return {"workload": "sc 32x32x1 (open z) Ising, Relax 1000 @ T=4 + CoolDown(4.0, 0.1, 0.1) x (1000 + 20000)",
+            "value": n * sweeps / (ms * 1e6), "unit": "flips/ns", "sample_sweeps": sweeps,
+            "sample_ms": ms, "full_schedule_s_projected": ms * full / sweeps / 1e3, "temperatures": len(temps),
+            "path": {1: "generic", 2: "structured", 3: "resident"}.get(path, "?"), "cpu_baseline": cpu}
+
+
 def run_heisenberg(V, torch, args):
     """Heisenberg sc 128^3, J=1, K=0.1 along z, B=0.05 along z, uniform-on-sphere
     proposals, FP32 updates with FP64 sums; a step is 100 measured sweeps at the
@@ -464,6 +516,7 @@ def main():
     if not args.no_batched:
         batched = run_batched(V, torch, args)
 
+    cool = run_cooldown_2d(V, torch, args) if not args.no_heisenberg else None
     heis = hyst = None
     if not args.no_heisenberg:
         heis = run_heisenberg(V, torch, args)
@@ -500,6 +553,7 @@ def main():
             "cpu_baseline": cpu,
             "batched": batched,
             "batched_vs_plain": (batched["value"] / value) if batched else None,
+            "cooldown_2d": cool,
             "heisenberg": heis,
             "hysteresis_batch": hyst,
             "clocks": clk.summary(),

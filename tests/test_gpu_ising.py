@@ -12,6 +12,8 @@ CASES = [
     ("sc", (32, 5, 4), (0, 0, 1), "resident"),      # open x and y boundaries
     ("sc", (64, 16, 10), (1, 1, 1), "structured"),
     ("sc", (96, 18, 6), (1, 0, 1), "structured"),
+    ("sc", (128, 8, 10), (1, 1, 1), "structured"),  # pairs of groups per thread
+    ("sc", (256, 64, 1), (1, 1, 0), "structured"),  # pairs, 2D (open z of extent 1)
     ("sc", (16, 4, 4), (1, 1, 1), "generic"),       # x/2 not a multiple of 16
     ("sc", (33, 4, 4), (1, 1, 1), "generic"),       # odd periodic cycle: greedy colouring
     ("bcc", (4, 4, 4), (1, 1, 1), "generic"),
@@ -168,3 +170,23 @@ def test_device_memory_cap_reports_oom(V):
     with _engine(V, "sc", (64, 16, 16), (1, 1, 1), H, 1, max_device_bytes=1 << 26) as eng:
         eng.init_random()
         eng.sweeps(2)  # within the cap the context works
+
+
+@pytest.mark.parametrize("ext,pbc,proposal", [((128, 8, 10), (1, 1, 1), 0), ((128, 8, 10), (1, 1, 1), 1),
+                                              ((256, 64, 1), (1, 1, 0), 0)])
+def test_one_call_equals_single_sweep_calls(V, ext, pbc, proposal):
+    """70 sweeps in one call (two reduction chunks) give the state and the
+    per-sweep sums of 70 one-sweep calls."""
+    H = V.hamiltonian(V.Exchange(1.0), V.Zeeman())
+    out = []
+    for split in (False, True):
+        with _engine(V, "sc", ext, pbc, H, 99, path=V.PATH_STRUCTURED, proposal=proposal) as eng:
+            eng.init_random()
+            eng.set_thermostat(3.1, (0, 0, 1), 0.2)
+            if split:
+                sums = np.concatenate([eng.sweeps_sums(1) for _ in range(70)])
+            else:
+                sums = eng.sweeps_sums(70)   # one chunk of 64 sweeps and one of 6
+            out.append((eng.get_state(), sums))
+    assert np.array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])

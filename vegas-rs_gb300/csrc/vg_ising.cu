@@ -390,18 +390,14 @@ __global__ void __launch_bounds__(256, UNIFORM ? 4 : 2) ising_sc_kernel(const Is
 // blocks, same tie resolution), so results are identical.  ALLPER: all axes
 // periodic, no missing rows.
 constexpr int kSc2MinBlocks = 3;  // 80 registers: the pair state stays in registers
-template <int C, bool MEASURE, bool UPDATE, int PROP, bool ALLPER>
-__global__ void __launch_bounds__(256, kSc2MinBlocks) ising_sc2_kernel(const IsingScArgs a, const FastDiv fG2, const IsingTable tab,
-                                                           const RngKey key, long long* __restrict__ part) {
-  constexpr int Z = 6, W = 2 * Z + 1;
-  constexpr int kQ = 64;  // per-warp tie queue
-  __shared__ unsigned long long s_thr[2 * W];
-  __shared__ uint2 s_q[8][kQ];
-  pdl_launch_dependents();
-  for (int i = threadIdx.x; i < 2 * W; i += blockDim.x) s_thr[i] = tab.thr[i];
-  __syncthreads();
-  pdl_wait();
+constexpr int kSc2Queue = 64;      // per-warp tie queue
 
+template <int C, bool MEASURE, bool UPDATE, int PROP, bool ALLPER>
+__device__ __forceinline__ void sc2_pass(const IsingScArgs& a, const FastDiv& fG2, const IsingTable& tab,
+                                         const RngKey& key, const unsigned long long* s_thr,
+                                         uint2 (*s_q)[kSc2Queue], long long* __restrict__ part) {
+  constexpr int Z = 6;
+  constexpr int kQ = kSc2Queue;
   uint8_t* __restrict__ own = a.cls[C];
   const uint8_t* __restrict__ oth = a.cls[C ^ 1];
   const uint32_t zoff = (uint32_t)(Z - tab.zeff) * 0x01010101u;
@@ -591,6 +587,20 @@ __global__ void __launch_bounds__(256, kSc2MinBlocks) ising_sc2_kernel(const Isi
   }
   if (UPDATE && qn > 0) drain(qn);
   if (MEASURE) block_sum3_store(bond, ups, nacc, part + (size_t)blockIdx.x * kNumSums);
+}
+
+template <int C, bool MEASURE, bool UPDATE, int PROP, bool ALLPER>
+__global__ void __launch_bounds__(256, kSc2MinBlocks) ising_sc2_kernel(const IsingScArgs a, const FastDiv fG2,
+                                                                       const IsingTable tab, const RngKey key,
+                                                                       long long* __restrict__ part) {
+  constexpr int W = 13;
+  __shared__ unsigned long long s_thr[2 * W];
+  __shared__ uint2 s_q[8][kSc2Queue];
+  pdl_launch_dependents();
+  for (int i = threadIdx.x; i < 2 * W; i += blockDim.x) s_thr[i] = tab.thr[i];
+  __syncthreads();
+  pdl_wait();
+  sc2_pass<C, MEASURE, UPDATE, PROP, ALLPER>(a, fG2, tab, key, s_thr, s_q, part);
 }
 
 // ------------------------------------------------------------- generic
