@@ -30,10 +30,48 @@ def test_cli_prints_default_input_and_fails_loudly_without_args():
     assert r.returncode == 1 and r.stderr.startswith("Error:")
 
 
+def test_parquet_writer_is_read_by_arrow(tmp_path):
+    """The host's Parquet files (the reference's ObservableParquetOutput
+    schema, src/output.rs:37-46) read back with an independent reader."""
+    pq = pytest.importorskip("pyarrow.parquet")
+    import pyarrow as pa
+
+    r = subprocess.run([_bin("host_selftest"), "--parquet-demo", str(tmp_path)], capture_output=True, text=True,
+                       timeout=60)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert not (tmp_path / "demo.parquet.tmp").exists()
+    f = pq.ParquetFile(str(tmp_path / "demo.parquet"))
+    assert f.metadata.num_rows == 2500 and f.metadata.num_row_groups == 3
+    t = f.read()
+    assert t.schema.names == ["relax", "stage", "step", "n", "temperature", "field", "energy", "magnetization"]
+    assert [t.schema.field(k).type for k in range(8)] == [pa.bool_(), pa.uint64(), pa.uint64(), pa.uint64(),
+                                                          pa.float64(), pa.float64(), pa.float64(), pa.float64()]
+    assert all(not t.schema.field(k).nullable for k in range(8))
+    i = list(range(2500))
+    assert t.column("relax").to_pylist() == [k % 3 == 0 for k in i]
+    assert t.column("stage").to_pylist() == [k // 100 for k in i]
+    assert t.column("step").to_pylist() == [k % 100 for k in i]
+    assert t.column("n").to_pylist() == [100] * 2500
+    assert t.column("temperature").to_pylist() == [1.0 + k / 1000.0 for k in i]
+    assert t.column("energy").to_pylist() == [-k / 7.0 for k in i]
+    assert t.column("magnetization").to_pylist() == [k * 1e-3 for k in i]
+
+
 @pytest.mark.gpu
 def test_host_selftest_gpu(tmp_path):
-    r = subprocess.run([_bin("host_selftest"), "--gpu"], capture_output=True, text=True, timeout=600, cwd=tmp_path)
+    r = subprocess.run([_bin("host_selftest"), "--gpu", str(tmp_path)], capture_output=True, text=True, timeout=600,
+                       cwd=tmp_path)
     assert r.returncode == 0, r.stdout + r.stderr
+    try:
+        import pyarrow.parquet as pq
+    except ImportError:  # the GPU host has no pyarrow: the C++ side checked the file structure
+        return
+    obs = pq.read_table(str(tmp_path / "host_obs.parquet"))
+    assert obs.num_rows == 20 + 7 * 40
+    assert obs.column("relax").to_pylist()[:20] == [True] * 20
+    assert obs.column("stage").to_pylist()[-1] == 14
+    st = pq.read_table(str(tmp_path / "host_state.parquet"))
+    assert st.num_rows == 1024 * (3 + 7 * (2 + 5))
 
 
 @pytest.mark.gpu
@@ -45,7 +83,7 @@ def test_cli_run_and_bench(tmp_path):
         '[[stages]]\nprogram = "Relax"\nsteps = 100\ntemperature = 4.0\n'
         '[[stages]]\nprogram = "CoolDown"\nmax_temperature = 4.0\nmin_temperature = 0.1\ncool_rate = 0.1\n'
         "relax = 20\nsteps = 100\n"
-        f'[output]\nobservables = "{tmp_path}/obs.csv"\n')
+        f'[output]\nobservables = "{tmp_path}/obs.parquet"\n')
     r = subprocess.run([_bin("vegas_gpu_cli"), "run", str(toml), "-s", "1"], capture_output=True, text=True,
                        timeout=600)
     assert r.returncode == 0, r.stderr
@@ -55,6 +93,6 @@ def test_cli_run_and_bench(tmp_path):
     assert all(len(c) == 7 for c in cols)
     # energy per spin at the lowest temperature is near the ground state -2 (bond) x 2 (Compound total)
     assert cols[-1][2] / 1024 < -3.9
-    assert (tmp_path / "obs.csv").exists() and not (tmp_path / "obs.csv.tmp").exists()
+    assert (tmp_path / "obs.parquet").exists() and not (tmp_path / "obs.parquet.tmp").exists()
     r = subprocess.run([_bin("vegas_gpu_cli"), "bench", "potts", "8"], capture_output=True, text=True, timeout=60)
     assert r.returncode == 1 and "unknown model" in r.stderr

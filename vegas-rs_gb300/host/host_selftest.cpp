@@ -3,7 +3,10 @@
 //   host_selftest --cpu   logic that needs no GPU: schedules, accumulator,
 //                         StatSensor format, TOML input, program errors,
 //                         hamiltonian descriptors
-//   host_selftest --gpu   Machine + programs + instruments on the engine
+//   host_selftest --gpu DIR   Machine + programs + instruments on the engine
+//                             (instrument files under DIR)
+//   host_selftest --parquet-demo DIR   writes DIR/demo.parquet (3 row groups
+//                             of the observables schema) for a reader check
 //
 // Prints one line per check and exits non-zero on the first failure.
 #include <cmath>
@@ -127,7 +130,7 @@ static void cpu_checks() {
   CHECK(wolff);
 }
 
-static void gpu_checks() {
+static void gpu_checks(const std::string& dir) {
   int32_t ndev = 0;
   vg_device_count(&ndev);
   CHECK(ndev > 0);
@@ -138,8 +141,8 @@ static void gpu_checks() {
     FILE* out = std::tmpfile();
     Machine<decltype(H), GpuIntegrator, IsingSpin>::Instruments ins;
     ins.push_back(std::make_unique<StatSensor<IsingSpin>>(out));
-    ins.push_back(std::make_unique<ObservableSensor<IsingSpin>>("_host_obs.csv"));
-    ins.push_back(std::make_unique<StateSensor<IsingSpin>>("_host_state.csv", 7));
+    ins.push_back(std::make_unique<ObservableSensor<IsingSpin>>(dir + "/host_obs.parquet"));
+    ins.push_back(std::make_unique<StateSensor<IsingSpin>>(dir + "/host_state.parquet", 7));
     {
       Machine<decltype(H), GpuIntegrator, IsingSpin> m(Thermostat<IsingSpin>(2.8, Field<IsingSpin>::zero()), H,
                                                        MetropolisFlipIntegrator(5), std::move(ins),
@@ -155,21 +158,18 @@ static void gpu_checks() {
     const std::string stats = slurp(out);
     std::fclose(out);
     CHECK(count_lines(stats) == (int)CoolDown(4.0, 1.0, 0.5).temperatures().size());
-    FILE* o = std::fopen("_host_obs.csv", "r");
-    CHECK(o != nullptr);
-    const std::string obs = slurp(o);
-    std::fclose(o);
-    // header + relax 20 + 7 temperatures x (10 relax + 30 measured)
-    CHECK(count_lines(obs) == 1 + 20 + 7 * 40);
-    FILE* st = std::fopen("_host_state.csv", "r");
-    CHECK(st != nullptr);
-    const std::string states = slurp(st);
-    std::fclose(st);
-    // snapshots at steps 0, 7, 14 of the relax run (3) and per temperature
-    // 0, 7 of the relax run (2) and 0, 7, 14, 21, 28 of the measure run (5)
-    CHECK(count_lines(states) == 1 + 1024 * (3 + 7 * (2 + 5)));
-    std::remove("_host_obs.csv");
-    std::remove("_host_state.csv");
+    // Parquet files in place of their .parquet.tmp (row counts are checked by
+    // the Python test that reads them: relax 20 + 7 x (10 + 30) observable
+    // rows; 1024 x (3 + 7 x (2 + 5)) state rows)
+    for (const char* f : {"/host_obs.parquet", "/host_state.parquet"}) {
+      FILE* p = std::fopen((dir + f).c_str(), "rb");
+      CHECK(p != nullptr);
+      if (p) {
+        const std::string b = slurp(p);
+        std::fclose(p);
+        CHECK(b.size() > 12 && b.compare(0, 4, "PAR1") == 0 && b.compare(b.size() - 4, 4, "PAR1") == 0);
+      }
+    }
   }
   // Heisenberg hysteresis with Exchange + Anisotropy + Zeeman
   {
@@ -214,20 +214,54 @@ static void gpu_checks() {
   }
 }
 
+// Rows i = 0..2499 of the observables schema in row groups of 1000:
+// relax = i % 3 == 0, stage = i / 100, step = i % 100, n = 100,
+// temperature = 1 + i / 1000, field = -0.5 (stored as given), energy = -i / 7,
+// magnetization = i * 1e-3.
+static void parquet_demo(const std::string& dir) {
+  parquet::Writer w(dir + "/demo.parquet", parquet::with_extension(dir + "/demo.parquet", "parquet.tmp"),
+                    {{"relax", parquet::Type::Bool},
+                     {"stage", parquet::Type::UInt64},
+                     {"step", parquet::Type::UInt64},
+                     {"n", parquet::Type::UInt64},
+                     {"temperature", parquet::Type::Float64},
+                     {"field", parquet::Type::Float64},
+                     {"energy", parquet::Type::Float64},
+                     {"magnetization", parquet::Type::Float64}},
+                    1000);
+  for (int i = 0; i < 2500; ++i) {
+    w.add_bool(0, i % 3 == 0);
+    w.add_u64(1, (uint64_t)(i / 100));
+    w.add_u64(2, (uint64_t)(i % 100));
+    w.add_u64(3, 100);
+    w.add_f64(4, 1.0 + i / 1000.0);
+    w.add_f64(5, -0.5);
+    w.add_f64(6, -i / 7.0);
+    w.add_f64(7, i * 1e-3);
+    w.end_row();
+  }
+  w.close();
+  CHECK(parquet::with_extension("a/b.parquet", "parquet.tmp") == "a/b.parquet.tmp");
+  CHECK(parquet::with_extension("a.d/obs", "parquet.tmp") == "a.d/obs.parquet.tmp");
+  CHECK(parquet::with_extension("obs.csv", "parquet.tmp") == "obs.parquet.tmp");
+}
+
 int main(int argc, char** argv) {
   const bool cpu = argc > 1 && !std::strcmp(argv[1], "--cpu");
   const bool gpu = argc > 1 && !std::strcmp(argv[1], "--gpu");
-  if (!cpu && !gpu) {
-    std::fprintf(stderr, "usage: %s --cpu | --gpu\n", argv[0]);
+  const bool demo = argc > 2 && !std::strcmp(argv[1], "--parquet-demo");
+  if (!cpu && !gpu && !demo) {
+    std::fprintf(stderr, "usage: %s --cpu | --gpu [DIR] | --parquet-demo DIR\n", argv[0]);
     return 2;
   }
   try {
     if (cpu) cpu_checks();
-    if (gpu) gpu_checks();
+    if (gpu) gpu_checks(argc > 2 ? argv[2] : ".");
+    if (demo) parquet_demo(argv[2]);
   } catch (const std::exception& e) {
     std::fprintf(stderr, "FAIL exception: %s\n", e.what());
     return 1;
   }
-  std::printf("host_selftest %s: %d checks passed\n", cpu ? "cpu" : "gpu", g_checks);
+  std::printf("host_selftest %s: %d checks passed\n", cpu ? "cpu" : gpu ? "gpu" : "parquet-demo", g_checks);
   return 0;
 }

@@ -7,9 +7,9 @@
 // src/instrument.rs:133-141, :254-262) and a callback that copies the state
 // back when an instrument needs the spins (StateSensor).
 //
-// Output files: the reference writes parquet (src/output.rs); this host writes
-// the same columns as CSV, through a ".tmp" file renamed on close as the
-// reference does (src/output.rs:101-112, :189-200).
+// Output files: Parquet with the reference's schemas (src/output.rs:37-46,
+// :126-136), through "<path>.parquet.tmp" renamed on close as the reference
+// does (src/output.rs:101-112, :189-200); see parquet.hpp.
 #pragma once
 
 #include <cstdio>
@@ -19,6 +19,7 @@
 
 #include "accumulator.hpp"
 #include "error.hpp"
+#include "parquet.hpp"
 #include "state.hpp"
 #include "thermostat.hpp"
 
@@ -85,43 +86,36 @@ class StatSensor : public Instrument<S> {
   Accumulator energy_, magnetization_;
 };
 
-// Atomic CSV file: writes path + ".tmp", renames to path on close.
-class CsvOutput {
- public:
-  CsvOutput(const std::string& path, const char* header) : path_(path), tmp_(path + ".tmp") {
-    f_ = std::fopen(tmp_.c_str(), "w");
-    if (!f_) throw IoError("std io error: cannot create " + tmp_);
-    std::fprintf(f_, "%s\n", header);
-  }
-  ~CsvOutput() { close(); }
-  FILE* file() { return f_; }
-  void close() {
-    if (!f_) return;
-    std::fclose(f_);
-    f_ = nullptr;
-    if (std::rename(tmp_.c_str(), path_.c_str()) != 0) std::fprintf(stderr, "Failed to rename %s\n", tmp_.c_str());
-  }
-
- private:
-  std::string path_, tmp_;
-  FILE* f_ = nullptr;
-};
-
 // ObservableSensor (src/instrument.rs:144-263): per-sweep rows during relax
 // and measure runs; schema of src/output.rs:37-46.
 template <typename S>
 class ObservableSensor : public Instrument<S> {
  public:
   explicit ObservableSensor(const std::string& path)
-      : io_(path, "relax,stage,step,n,temperature,field,energy,magnetization") {}
+      : io_(path, parquet::with_extension(path, "parquet.tmp"),
+            {{"relax", parquet::Type::Bool},
+             {"stage", parquet::Type::UInt64},
+             {"step", parquet::Type::UInt64},
+             {"n", parquet::Type::UInt64},
+             {"temperature", parquet::Type::Float64},
+             {"field", parquet::Type::Float64},
+             {"energy", parquet::Type::Float64},
+             {"magnetization", parquet::Type::Float64}}) {}
   void on_relax_start(const Thermostat<S>& t, size_t n) override { start(t, n, true); }
   void on_relax_end() override { finish(); }
   void on_measure_start(const Thermostat<S>& t, size_t n) override { start(t, n, false); }
   void on_measure_end() override { finish(); }
   void after_step(const StepView<S>& v) override {
     if (!thermostat_) return;
-    std::fprintf(io_.file(), "%s,%zu,%zu,%zu,%.17g,%.17g,%.17g,%.17g\n", relax_ ? "true" : "false", stage_, step_++,
-                 n_, thermostat_->temperature(), thermostat_->field().magnitude(), v.energy, v.magnetization);
+    io_.add_bool(0, relax_);
+    io_.add_u64(1, stage_);
+    io_.add_u64(2, step_++);
+    io_.add_u64(3, n_);
+    io_.add_f64(4, thermostat_->temperature());
+    io_.add_f64(5, thermostat_->field().magnitude());
+    io_.add_f64(6, v.energy);
+    io_.add_f64(7, v.magnetization);
+    io_.end_row();
   }
   bool wants_observables() const override { return thermostat_ != nullptr; }
 
@@ -136,7 +130,7 @@ class ObservableSensor : public Instrument<S> {
     ++stage_;
     thermostat_.reset();
   }
-  CsvOutput io_;
+  parquet::Writer io_;
   std::unique_ptr<Thermostat<S>> thermostat_;
   size_t n_ = 0, stage_ = 0, step_ = 0;
   bool relax_ = false;
@@ -148,7 +142,17 @@ template <typename S>
 class StateSensor : public Instrument<S> {
  public:
   StateSensor(const std::string& path, size_t frequency)
-      : io_(path, "relax,stage,step,temperature,field,id,sx,sy,sz"), frequency_(frequency ? frequency : 1) {}
+      : io_(path, parquet::with_extension(path, "parquet.tmp"),
+            {{"relax", parquet::Type::Bool},
+             {"stage", parquet::Type::UInt64},
+             {"step", parquet::Type::UInt64},
+             {"temperature", parquet::Type::Float64},
+             {"field", parquet::Type::Float64},
+             {"id", parquet::Type::UInt64},
+             {"sx", parquet::Type::Float64},
+             {"sy", parquet::Type::Float64},
+             {"sz", parquet::Type::Float64}}),
+        frequency_(frequency ? frequency : 1) {}
   void on_relax_start(const Thermostat<S>& t, size_t) override {
     relax_ = 1;
     thermostat_ = std::make_unique<Thermostat<S>>(t);
@@ -164,8 +168,16 @@ class StateSensor : public Instrument<S> {
       const State<S> st = v.state();
       for (size_t i = 0; i < st.len(); ++i) {
         const S& s = st.at(i);
-        std::fprintf(io_.file(), "%s,%zu,%zu,%.17g,%.17g,%zu,%.17g,%.17g,%.17g\n", relax_ ? "true" : "false", stage_,
-                     step_, thermostat_->temperature(), thermostat_->field().magnitude(), i, s.sx(), s.sy(), s.sz());
+        io_.add_bool(0, relax_ == 1);
+        io_.add_u64(1, stage_);
+        io_.add_u64(2, step_);
+        io_.add_f64(3, thermostat_->temperature());
+        io_.add_f64(4, thermostat_->field().magnitude());
+        io_.add_u64(5, i);
+        io_.add_f64(6, s.sx());
+        io_.add_f64(7, s.sy());
+        io_.add_f64(8, s.sz());
+        io_.end_row();
       }
     }
     ++step_;
@@ -179,7 +191,7 @@ class StateSensor : public Instrument<S> {
     ++stage_;
     thermostat_.reset();
   }
-  CsvOutput io_;
+  parquet::Writer io_;
   size_t frequency_;
   int relax_ = -1;
   size_t step_ = 0, stage_ = 0;
