@@ -40,7 +40,7 @@ def _worker(rank, world, port, out):
 
 def test_two_rank_replica_aggregation():
     world = 2
-    mgr = mp.Manager()
+    mgr = mp.get_context("spawn").Manager()
     out = mgr.dict()
     mp.start_processes(_worker, args=(world, _free_port(), out), nprocs=world, join=True, start_method="spawn")
     assert out[0] == out[1]

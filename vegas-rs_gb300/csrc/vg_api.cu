@@ -703,11 +703,16 @@ void energy_of(const vg_ctx* c, const vg_sums* s, double* E, double* M) {
   }
 }
 
+int sync_stream(vg_ctx* c) {
+  VG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return VG_OK;
+}
+
 int read_raw(vg_ctx* c, uint64_t count, double** host) {
   int rc;
   if ((rc = ensure_pinned(c, (size_t)count * kNumSums))) return rc;
   if (count) VG_CUDA(c, cudaMemcpyAsync(c->h_pin, c->d_sums, count * kNumSums * 8, cudaMemcpyDeviceToHost, c->stream));
-  VG_CUDA(c, cudaStreamSynchronize(c->stream));
+  if ((rc = sync_stream(c))) return rc;
   *host = c->h_pin;
   return VG_OK;
 }
@@ -1197,8 +1202,7 @@ int vg_read_sums(vg_ctx* c, uint64_t count, vg_sums* out) {
 
 int vg_synchronize(vg_ctx* c) {
   if (!c) return VG_ERR_INVALID_ARG;
-  VG_CUDA(c, cudaStreamSynchronize(c->stream));
-  return VG_OK;
+  return sync_stream(c);
 }
 
 int vg_sweeps_sums(vg_ctx* c, uint64_t n, vg_sums* out) {
@@ -1206,10 +1210,7 @@ int vg_sweeps_sums(vg_ctx* c, uint64_t n, vg_sums* out) {
   VG_CUDA(c, cudaSetDevice(c->device));
   int rc = enqueue(c, n, out != nullptr);
   if (rc) return rc;
-  if (!out) {
-    VG_CUDA(c, cudaStreamSynchronize(c->stream));
-    return VG_OK;
-  }
+  if (!out) return sync_stream(c);
   return vg_read_sums(c, n, out);
 }
 
@@ -1218,10 +1219,7 @@ int vg_sweeps(vg_ctx* c, uint64_t n, int32_t measure, double* E, double* M) {
   VG_CUDA(c, cudaSetDevice(c->device));
   int rc = enqueue(c, n, measure != 0);
   if (rc) return rc;
-  if (!measure) {
-    VG_CUDA(c, cudaStreamSynchronize(c->stream));
-    return VG_OK;
-  }
+  if (!measure) return sync_stream(c);
   double* raw = nullptr;
   if ((rc = read_raw(c, n, &raw))) return rc;
   for (uint64_t t = 0; t < n; ++t) {

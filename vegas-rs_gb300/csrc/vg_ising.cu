@@ -392,10 +392,14 @@ __global__ void __launch_bounds__(256, UNIFORM ? 4 : 2) ising_sc_kernel(const Is
 constexpr int kSc2MinBlocks = 3;  // 80 registers: the pair state stays in registers
 constexpr int kSc2Queue = 64;      // per-warp tie queue
 
+// The pairs base + lane for base in [first, end) step `step` (base a
+// multiple of 32 apart from `first`), adding the pass's sums to bond / ups /
+// nacc.  Every tie is resolved before returning.
 template <int C, bool MEASURE, bool UPDATE, int PROP, bool ALLPER>
-__device__ __forceinline__ void sc2_pass(const IsingScArgs& a, const FastDiv& fG2, const IsingTable& tab,
-                                         const RngKey& key, const unsigned long long* s_thr,
-                                         uint2 (*s_q)[kSc2Queue], long long* __restrict__ part) {
+__device__ __forceinline__ void sc2_range(const IsingScArgs& a, const FastDiv& fG2, const IsingTable& tab,
+                                          const RngKey& key, const unsigned long long* s_thr,
+                                          uint2 (*s_q)[kSc2Queue], uint32_t first, uint32_t end, uint32_t step,
+                                          int& bond, int& ups, int& nacc) {
   constexpr int Z = 6;
   constexpr int kQ = kSc2Queue;
   uint8_t* __restrict__ own = a.cls[C];
@@ -403,8 +407,7 @@ __device__ __forceinline__ void sc2_pass(const IsingScArgs& a, const FastDiv& fG
   const uint32_t zoff = (uint32_t)(Z - tab.zeff) * 0x01010101u;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int G2 = a.G >> 1;
-  const uint32_t pairs = a.groups >> 1;
-  int bond = 0, ups = 0, nacc = 0;
+  const uint32_t pairs = end;
   int qn = 0;  // warp-uniform queue length
 
   auto drain = [&](int n) {
@@ -430,8 +433,7 @@ __device__ __forceinline__ void sc2_pass(const IsingScArgs& a, const FastDiv& fG
     qn = rest;
   };
 
-  const uint32_t stride = gridDim.x * blockDim.x;
-  for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < pairs; base += stride) {
+  for (uint32_t base = first; base < pairs; base += step) {
     const uint32_t q = base + lane;
     const bool active = q < pairs;
     uint32_t tm = 0;  // tied sites: bit k -> group 2q + (k >> 4), site k & 15
@@ -575,8 +577,14 @@ __device__ __forceinline__ void sc2_pass(const IsingScArgs& a, const FastDiv& fG
           const int k = __ffs(tm) - 1;
           tm &= tm - 1u;
           const int wi = k >> 2;
-          const uint32_t sk = (S[wi] >> (8 * (k & 3))) & 0xFFu;
-          const uint32_t nk = (A[wi] >> (8 * (k & 3))) & 0xFFu;
+          uint32_t sw = 0, aw = 0;  // S[wi], A[wi] by selects: a dynamic index would put S, A on the stack
+#pragma unroll
+          for (int i = 0; i < 8; ++i) {
+            sw = i == wi ? S[i] : sw;
+            aw = i == wi ? A[i] : aw;
+          }
+          const uint32_t sk = (sw >> (8 * (k & 3))) & 0xFFu;
+          const uint32_t nk = (aw >> (8 * (k & 3))) & 0xFFu;
           s_q[warp][pos] = make_uint2(2u * q + (uint32_t)(k >> 4), (uint32_t)(k & 15) | (sk << 4) | (nk << 5));
         }
         qn += __popc(lanes);
@@ -586,7 +594,6 @@ __device__ __forceinline__ void sc2_pass(const IsingScArgs& a, const FastDiv& fG
     }
   }
   if (UPDATE && qn > 0) drain(qn);
-  if (MEASURE) block_sum3_store(bond, ups, nacc, part + (size_t)blockIdx.x * kNumSums);
 }
 
 template <int C, bool MEASURE, bool UPDATE, int PROP, bool ALLPER>
@@ -600,7 +607,11 @@ __global__ void __launch_bounds__(256, kSc2MinBlocks) ising_sc2_kernel(const Isi
   for (int i = threadIdx.x; i < 2 * W; i += blockDim.x) s_thr[i] = tab.thr[i];
   __syncthreads();
   pdl_wait();
-  sc2_pass<C, MEASURE, UPDATE, PROP, ALLPER>(a, fG2, tab, key, s_thr, s_q, part);
+  int bond = 0, ups = 0, nacc = 0;
+  sc2_range<C, MEASURE, UPDATE, PROP, ALLPER>(a, fG2, tab, key, s_thr, s_q,
+                                                     blockIdx.x * blockDim.x + (threadIdx.x & ~31u), a.groups >> 1,
+                                                     gridDim.x * blockDim.x, bond, ups, nacc);
+  if (MEASURE) block_sum3_store(bond, ups, nacc, part + (size_t)blockIdx.x * kNumSums);
 }
 
 // ------------------------------------------------------------- generic
