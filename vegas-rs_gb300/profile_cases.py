@@ -5,6 +5,7 @@ profiles/*.md run these under ncu (one kernel filtered with -k, a few
 launches with -c), after the same command has run without the profiler.
 
     python vegas-rs_gb300/profile_cases.py ising L SWEEPS      # sc L^3 Ising, checkerboard passes
+    python vegas-rs_gb300/profile_cases.py ising_sizes N       # pass time for sc 64^3 .. 512^3
     python vegas-rs_gb300/profile_cases.py heis L SWEEPS       # sc L^3 Heisenberg, FP32
     python vegas-rs_gb300/profile_cases.py hbatch L REPLICAS   # fcc L^3 cells x replicas, field points
     python vegas-rs_gb300/profile_cases.py msc ROUNDS          # the 256-replica multi-spin-coded batch
@@ -26,6 +27,23 @@ def ising(L, sweeps):
         eng.sweeps(sweeps)
         dt = time.perf_counter() - t0
         print(f"ising sc {L}^3: {sweeps} measured sweeps, {L ** 3 * sweeps / (dt * 1e9):.1f} flips/ns (wall)")
+
+
+def ising_sizes(sweeps_at_256):
+    """Pass time against lattice size (unmeasured sweeps): the intercept is
+    the fixed cost of a colour-pass launch boundary."""
+    for L in (64, 128, 192, 256, 320, 384, 512):
+        with V.Engine(V.Lattice.sc(L, L, L), V.hamiltonian(V.Exchange(1.0)), seed=1, path=V.PATH_STRUCTURED) as eng:
+            eng.init_random()
+            eng.set_thermostat(4.5)
+            n = max(20, int(sweeps_at_256 * (256 / L) ** 3)) if L >= 128 else 10 * sweeps_at_256
+            eng.sweeps_async(n, measure=False)
+            eng.synchronize()
+            t0 = time.perf_counter()
+            eng.sweeps_async(n, measure=False)
+            eng.synchronize()
+            us = (time.perf_counter() - t0) / n * 1e6
+            print(f"sc {L}^3: pass {us / 2:.2f} us, {L ** 3 / (us * 1e3):.1f} flips/ns, grid {eng.info().grid_blocks}")
 
 
 def heis(L, sweeps):
@@ -69,4 +87,4 @@ def msc(rounds):
 
 if __name__ == "__main__":
     case, args = sys.argv[1], [int(a) for a in sys.argv[2:]]
-    {"ising": ising, "heis": heis, "hbatch": hbatch, "msc": msc}[case](*args)
+    {"ising": ising, "ising_sizes": ising_sizes, "heis": heis, "hbatch": hbatch, "msc": msc}[case](*args)
