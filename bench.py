@@ -220,7 +220,16 @@ def run_batched(V, torch, args):
         info = b.info()
         flips = float(info.replica_sites) * 10 * rounds * args.steps
         acc, att = b.swap_stats(3)
-    return {"value": flips / (ms * 1e6), "unit": "flips/ns", "ms_per_step": ms / args.steps,
+    cpu = None
+    if not args.no_cpu_baseline:
+        import oracle as O
+
+        cores = os.cpu_count() or 1
+        fl, dt = O.ref_parallel(O.lattice("sc", 128, 128, 128), 0, O.Hamiltonian(has_exchange=1, J=1.0, compound=0),
+                                4.5, 1, cores, seed=SEED, measure=True)
+        cpu = {"value": fl / (dt * 1e9), "unit": "flips/ns", "cores": cores, "kind": "port",
+               "sample": f"one measured reference sweep of an independent 128^3 replica on each of {cores} cores"}
+    return {"value": flips / (ms * 1e6), "unit": "flips/ns", "ms_per_step": ms / args.steps, "cpu_baseline": cpu,
             "replicas": int(info.total_replicas), "replica_sites": int(info.replica_sites),
             "sweeps_per_step": 10 * rounds, "graph": bool(info.graph),
             "workload": "256 replicas: 64 x 2D 64^2, 64 x 2D 512^2 (T 2.0-2.6), 64 x 3D 32^3, 64 x 3D 128^3 "
@@ -323,7 +332,18 @@ def run_heisenberg(V, torch, args):
     alg = 18.0 * lat.n_sites  # per pass: read both classes (12 B each), write one class
     peak, _ = peaks()
     ach = alg / (out["fp32"]["pass_ms"] * 1e-3) / 1e9
-    return {"workload": "heisenberg-sc-128^3-pbc J=1 K=0.1 z B=0.05 z, random proposals, FP32 update / FP64 sums",
+    cpu = None
+    if not args.no_cpu_baseline:
+        import oracle as O
+
+        OH = O.Hamiltonian(has_exchange=1, J=1.0, has_anisotropy=1, K=0.1, has_zeeman=1, zeeman_sign=1.0, compound=1)
+        OH.axis[:] = (0.0, 0.0, 1.0)
+        flips, dt = O.ref_parallel(O.lattice("sc", n_l, n_l, n_l), 1, OH, 1.0, 2, 1, seed=SEED,
+                                   proposal=O.PROPOSE_RANDOM, measure=True, bmag=0.05)
+        cpu = {"value": flips / (dt * 1e9), "unit": "flips/ns", "cores": 1, "kind": "port",
+               "sample": f"2 measured reference sweeps of the {n_l}^3 Heisenberg lattice on one core"}
+    return {"cpu_baseline": cpu,
+            "workload": "heisenberg-sc-128^3-pbc J=1 K=0.1 z B=0.05 z, random proposals, FP32 update / FP64 sums",
             "value": out["fp32"]["value"], "unit": "flips/ns", "sweeps_per_step": sweeps,
             "fp64_value": out["fp64"]["value"], "bytes_per_flip": 36.0,
             "roofline": {"achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
@@ -375,11 +395,22 @@ def run_hysteresis(V, torch, args):
         m = sums[:, :, 6] / (30 * small.n_sites)
         loops[prec] = ([V.loop_area(fields, m[:, r]) for r in range(64)],
                        [V.coercive_fields(fields, m[:, r]) for r in range(64)])
+    cpu = None
+    if not args.no_cpu_baseline:
+        import oracle as O
+
+        cores = os.cpu_count() or 1
+        OH = O.Hamiltonian(has_exchange=1, J=1.0, has_zeeman=1, zeeman_sign=-1.0, compound=1)
+        fl, dt = O.ref_parallel(O.lattice("fcc", 64, 64, 64), 1, OH, 0.5, 1, cores, seed=SEED,
+                                proposal=O.PROPOSE_RANDOM, measure=True, bmag=1.0)
+        cpu = {"value": fl / (dt * 1e9), "unit": "flips/ns", "cores": cores, "kind": "port",
+               "sample": f"one measured reference sweep of an independent fcc 64^3-cell replica on each of {cores} "
+                         "cores (exchange + Zeeman: the reference has no cubic term)"}
     a32, a64 = np.array(loops[V.FP32][0]), np.array(loops[V.FP64][0])
     h32, h64 = np.array(loops[V.FP32][1]), np.array(loops[V.FP64][1])
     return {"workload": "fcc 64^3 cells x 64 replicas (8 seeds x 8 Kc in 0-0.1), T=0.5, B_z +5 -> -5 -> +5 "
                         "step 0.1, FP32 updates, FP64 sums",
-            "value": value, "unit": "flips/ns", "ms_per_step": ms / args.steps,
+            "value": value, "unit": "flips/ns", "ms_per_step": ms / args.steps, "cpu_baseline": cpu,
             "sample": f"{pts} field points x ({relax} relax + {measure} measured sweeps) per step",
             "graph": bool(info.graph), "sites_per_thread": int(info.sites_per_thread), "bytes_per_flip": 60.0,
             "roofline": {"achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,

@@ -633,7 +633,7 @@ typedef struct {
   const vo_lattice* lat;
   int32_t kind, proposal, nsweeps, measure;
   const vo_hamiltonian* H;
-  double T;
+  double T, bmag;
   uint64_t seed;
   int64_t flips;
   pthread_barrier_t* start;
@@ -667,7 +667,8 @@ static void* par_worker(void* arg) {
   double b[3] = {0, 0, 1};
   pthread_barrier_wait(J->start); /* all chains set up: time the sweeps only */
   double t0 = now_s();
-  vo_ref_sweeps(n, z, nbr, J->kind, J->proposal, si, sf, J->H, J->T, b, 0.0, &rng, J->nsweeps, J->measure, 1, obs);
+  vo_ref_sweeps(n, z, nbr, J->kind, J->proposal, si, sf, J->H, J->T, b, J->bmag, &rng, J->nsweeps, J->measure, 1,
+                obs);
   J->seconds = now_s() - t0;
   J->flips = n * (int64_t)J->nsweeps;
   free(obs);
@@ -678,7 +679,7 @@ static void* par_worker(void* arg) {
 }
 
 int64_t vo_ref_parallel(const vo_lattice* lat, int32_t kind, int32_t proposal, const vo_hamiltonian* H,
-                        double T, int32_t nsweeps, int32_t measure, int32_t nthreads, uint64_t seed,
+                        double T, double bmag, int32_t nsweeps, int32_t measure, int32_t nthreads, uint64_t seed,
                         double* seconds) {
   if (nthreads < 1) nthreads = 1;
   pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)nthreads);
@@ -686,7 +687,7 @@ int64_t vo_ref_parallel(const vo_lattice* lat, int32_t kind, int32_t proposal, c
   pthread_barrier_t start;
   pthread_barrier_init(&start, NULL, (unsigned)nthreads);
   for (int k = 0; k < nthreads; ++k) {
-    par_job j = {lat, kind, proposal, nsweeps, measure, H, T, seed + 7919ull * (uint64_t)k, 0, &start, 0.0};
+    par_job j = {lat, kind, proposal, nsweeps, measure, H, T, bmag, seed + 7919ull * (uint64_t)k, 0, &start, 0.0};
     jobs[k] = j;
     pthread_create(&th[k], NULL, par_worker, &jobs[k]);
   }

@@ -146,7 +146,7 @@ double vo_ref_magnetization(int64_t n, int32_t spin_kind, const int8_t* spin_i8,
  * for the multi-core CPU baseline.  Returns total attempted flips; *seconds
  * receives the slowest chain's sweep time (setup excluded). */
 int64_t vo_ref_parallel(const vo_lattice* lat, int32_t spin_kind, int32_t proposal,
-                        const vo_hamiltonian* H, double T, int32_t nsweeps, int32_t measure,
+                        const vo_hamiltonian* H, double T, double bmag, int32_t nsweeps, int32_t measure,
                         int32_t nthreads, uint64_t seed, double* seconds);
 
 /* --------------------------------- (a) colour_cpu: batched multi-spin coding */
