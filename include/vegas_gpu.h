@@ -180,6 +180,20 @@ int vg_synchronize(vg_ctx* ctx);
  * duration (ms).  The sweeps are real work (the sweep index advances). */
 int vg_time_passes(vg_ctx* ctx, uint64_t n, int32_t measure, double* mean_pass_ms, double* mean_sweep_ms);
 
+/* Per-bond exchange constants: Exchange's CSR with arbitrary J_ij
+ * (src/energy.rs:169-206) instead of one constant for every bond.
+ * J[i * z + k] is the constant of the bond from site i to its k-th
+ * neighbour in vg_lattice_neighbours order (n_entries = n_sites x z; entries
+ * of absent neighbours are ignored).  The table must be symmetric (per pair
+ * of sites, the constants of its repeated bonds summed, J_ij == J_ji).  It
+ * replaces the Hamiltonian's uniform exchange constant; the bond sum then
+ * carries the constants (vg_sums.bond = sum over bonds of J_ij s_i.s_j) and
+ * the totals use J = 1.  Needs a context on the generic path
+ * (vg_options.path = VG_PATH_GENERIC) with an exchange term; Ising
+ * thresholds are then formed per site in FP64.  J = NULL restores the
+ * uniform constant. */
+int vg_set_exchange_bonds(vg_ctx* ctx, const double* J, int64_t n_entries);
+
 /* ---------------------------------------------------------- observables */
 int vg_current_sums(vg_ctx* ctx, vg_sums* out);
 int vg_total_energy(vg_ctx* ctx, double* energy);

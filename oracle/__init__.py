@@ -95,6 +95,13 @@ def lib():
         L.vo_heis_colour_sweeps.argtypes = [C.c_int64, C.c_int32, P(C.c_int32), P(C.c_int32), C.c_int32,
                                             P(C.c_double), P(HeisParams), C.c_int, C.c_uint64, C.c_uint32,
                                             C.c_uint32, C.c_int32, P(C.c_double)]
+        L.vo_ising_colour_sweeps_bonds.argtypes = [C.c_int64, C.c_int32, P(C.c_int32), P(C.c_double),
+                                                   P(C.c_int32), C.c_int32, P(C.c_int8), C.c_double, C.c_double,
+                                                   C.c_int, C.c_uint64, C.c_uint32, C.c_uint32, C.c_int32,
+                                                   P(C.c_double)]
+        L.vo_heis_colour_sweeps_bonds.argtypes = [C.c_int64, C.c_int32, P(C.c_int32), P(C.c_double),
+                                                  P(C.c_int32), C.c_int32, P(C.c_double), P(HeisParams), C.c_int,
+                                                  C.c_uint64, C.c_uint32, C.c_uint32, C.c_int32, P(C.c_double)]
         L.vo_pcg64_seed.argtypes = [P(Pcg64), C.c_uint64]
         L.vo_pcg64_next.argtypes = [P(Pcg64)]
         L.vo_pcg64_next.restype = C.c_uint64
@@ -186,6 +193,46 @@ class Graph:
                                     self.ncolours, _p(spin, C.c_double), C.byref(params), proposal, seed,
                                     replica, sweep0, nsweeps, _p(obs, C.c_double))
         return spin, obs[:nsweeps]
+
+    # ---- per-bond exchange constants (jb: n x zmax, entries of absent neighbours ignored)
+    def ising_sweeps_bonds(self, spin, jb, hz, T, seed, sweep0, nsweeps, replica=0, proposal=PROPOSE_FLIP):
+        spin = np.ascontiguousarray(spin, dtype=np.int8).copy()
+        jb = np.ascontiguousarray(jb, dtype=np.float64).reshape(self.n, self.zmax)
+        obs = np.zeros((max(nsweeps, 1), 2), dtype=np.float64)
+        lib().vo_ising_colour_sweeps_bonds(self.n, self.zmax, _p(self.nbr, C.c_int32), _p(jb, C.c_double),
+                                           _p(self.colour, C.c_int32), self.ncolours, _p(spin, C.c_int8), hz, T,
+                                           proposal, seed, replica, sweep0, nsweeps, _p(obs, C.c_double))
+        return spin, obs[:nsweeps]
+
+    def heis_sweeps_bonds(self, spin, jb, params: HeisParams, seed, sweep0, nsweeps, replica=0,
+                          proposal=PROPOSE_RANDOM):
+        spin = np.ascontiguousarray(spin, dtype=np.float64).copy()
+        jb = np.ascontiguousarray(jb, dtype=np.float64).reshape(self.n, self.zmax)
+        obs = np.zeros((max(nsweeps, 1), 8), dtype=np.float64)
+        lib().vo_heis_colour_sweeps_bonds(self.n, self.zmax, _p(self.nbr, C.c_int32), _p(jb, C.c_double),
+                                          _p(self.colour, C.c_int32), self.ncolours, _p(spin, C.c_double),
+                                          C.byref(params), proposal, seed, replica, sweep0, nsweeps,
+                                          _p(obs, C.c_double))
+        return spin, obs[:nsweeps]
+
+    def symmetric_bonds(self, rng, values=(0.5, 1.0, 1.5)):
+        """Random symmetric per-bond constants drawn from `values`
+        (J_ij = J_ji for every bond, duplicates of a pair share one value)."""
+        nb = self.neighbours()
+        jb = np.zeros((self.n, self.zmax))
+        for i in range(self.n):
+            for k in range(self.zmax):
+                t = int(nb[i, k])
+                if t < 0 or jb[i, k] != 0.0:
+                    continue
+                v = float(rng.choice(values))
+                for kk in range(self.zmax):
+                    if nb[i, kk] == t:
+                        jb[i, kk] = v
+                for kk in range(self.zmax):
+                    if nb[t, kk] == i:
+                        jb[t, kk] = v
+        return jb
 
     # ---- ref_cpu (faithful restatement of the reference)
     def ref_sweeps(self, kind, spin, H: Hamiltonian, T, nsweeps, rng: Pcg64, b=(0.0, 0.0, 1.0), bmag=0.0,

@@ -258,6 +258,75 @@ int vo_ising_colour_sweeps(int64_t n, int32_t zmax, const int32_t* nbr, const in
   return 0;
 }
 
+/* Per-bond exchange constants (Exchange's CSR with arbitrary J_ij,
+ * src/energy.rs:169-206): jb[i * zmax + k] is the constant of the bond to
+ * neighbour k of site i.  hJ = sum_k jb s_k in k order; dE of s -> -s is
+ * (-(-s) hJ + hz (-s)) - (-s hJ + hz s), thr = ceil(exp(-dE / T) 2^32) as in
+ * vo_ising_threshold; obs[2 t] = sum over bonds of J_ij s_i s_j (each bond
+ * once, from its higher-colour end), obs[2 t + 1] = magnetisation. */
+static uint64_t thr_of(double de, double T) {
+  if (de <= 0.0) return 1ull << 32;
+  double x = ceil(exp(-de / T) * 4294967296.0);
+  if (x >= 4294967296.0) return 1ull << 32;
+  if (x <= 0.0) return 0;
+  return (uint64_t)x;
+}
+
+int vo_ising_colour_sweeps_bonds(int64_t n, int32_t zmax, const int32_t* nbr, const double* jb,
+                                 const int32_t* colour, int32_t ncol, int8_t* spin, double hz, double T,
+                                 int proposal, uint64_t seed, uint32_t replica, uint32_t sweep0, int32_t nsweeps,
+                                 double* obs) {
+  if (T < 2.220446049250313e-16) T = 2.220446049250313e-16;
+  int64_t* rank = class_ranks(n, colour, ncol);
+  for (int32_t t = 0; t < nsweeps; ++t) {
+    uint32_t sweep = sweep0 + (uint32_t)t;
+    double bond = 0.0;
+    int64_t mag = 0;
+    for (int c = 0; c < ncol; ++c) {
+      for (int64_t i = 0; i < n; ++i) {
+        if (colour[i] != c) continue;
+        int64_t j = rank[i];
+        int s = spin[i];
+        double hj = 0.0;
+        for (int k = 0; k < zmax; ++k) {
+          int32_t q = nbr[i * zmax + k];
+          if (q >= 0) hj += jb[i * zmax + k] * (double)spin[q];
+        }
+        int propose_flip = 1;
+        if (proposal == VO_PROPOSE_RANDOM) {
+          uint32_t w[4];
+          draw(seed, (uint32_t)(j >> 4), sweep, ((uint32_t)VO_TAG_ISING_PROPOSE << 24) | ((uint32_t)c << 8),
+               replica, w);
+          int up = block_byte(w, (int)(j & 15)) < 128;
+          propose_flip = (up ? 1 : -1) != s;
+        }
+        if (propose_flip) {
+          const double sd = (double)s;
+          const double e_old = -sd * hj + hz * sd;
+          const double e_new = -(-sd) * hj + hz * (-sd);
+          uint64_t th = thr_of(e_new - e_old, T);
+          int accept = th >= (1ull << 32) ? 1 : (uint64_t)ising_uniform(seed, replica, sweep, c, j) < th;
+          if (accept) spin[i] = (int8_t)(-s);
+        }
+        int sn = spin[i];
+        mag += sn;
+        double low = 0.0;
+        for (int k = 0; k < zmax; ++k) {
+          int32_t q = nbr[i * zmax + k];
+          if (q >= 0 && colour[q] < c) low += jb[i * zmax + k] * (double)spin[q];
+        }
+        bond += (double)sn * low;
+      }
+    }
+    if (obs) {
+      obs[2 * t] = bond;
+      obs[2 * t + 1] = (double)mag;
+    }
+  }
+  free(rank);
+  return 0;
+}
+
 /* ===================================================== Heisenberg oracle */
 /* Uniform point on S^2 (Archimedes: z uniform in (-1,1), azimuth uniform):
  * z = (2k + 1 - 2^24) / 2^24 with k = w0 >> 8, azimuth = pi * (w1 >> 8) / 2^23.
@@ -296,10 +365,11 @@ double vo_heis_delta(const vo_heis_params* P, const double s[3], const double p[
   return de;
 }
 
-int vo_heis_colour_sweeps(int64_t n, int32_t zmax, const int32_t* nbr, const int32_t* colour,
-                          int32_t ncol, double* spin, const vo_heis_params* P, int proposal,
-                          uint64_t seed, uint32_t replica, uint32_t sweep0, int32_t nsweeps,
-                          double* obs) {
+/* jb = NULL: uniform exchange P->J; else per-bond constants jb[i * zmax + k]
+ * weigh the neighbour field and the bond sum, and P->J must be 1. */
+static int heis_sweeps(int64_t n, int32_t zmax, const int32_t* nbr, const double* jb, const int32_t* colour,
+                       int32_t ncol, double* spin, const vo_heis_params* P, int proposal, uint64_t seed,
+                       uint32_t replica, uint32_t sweep0, int32_t nsweeps, double* obs) {
   double T = P->T < 2.220446049250313e-16 ? 2.220446049250313e-16 : P->T;
   int64_t* rank = class_ranks(n, colour, ncol);
   for (int32_t t = 0; t < nsweeps; ++t) {
@@ -314,9 +384,10 @@ int vo_heis_colour_sweeps(int64_t n, int32_t zmax, const int32_t* nbr, const int
         for (int k = 0; k < zmax; ++k) {
           int32_t q = nbr[i * zmax + k];
           if (q >= 0) {
-            h[0] += spin[3 * q];
-            h[1] += spin[3 * q + 1];
-            h[2] += spin[3 * q + 2];
+            const double wq = jb ? jb[i * zmax + k] : 1.0;
+            h[0] += wq * spin[3 * q];
+            h[1] += wq * spin[3 * q + 1];
+            h[2] += wq * spin[3 * q + 2];
           }
         }
         uint32_t w[4];
@@ -337,9 +408,10 @@ int vo_heis_colour_sweeps(int64_t n, int32_t zmax, const int32_t* nbr, const int
         for (int k = 0; k < zmax; ++k) {
           int32_t q = nbr[i * zmax + k];
           if (q >= 0 && colour[q] < c) {
-            low[0] += spin[3 * q];
-            low[1] += spin[3 * q + 1];
-            low[2] += spin[3 * q + 2];
+            const double wq = jb ? jb[i * zmax + k] : 1.0;
+            low[0] += wq * spin[3 * q];
+            low[1] += wq * spin[3 * q + 1];
+            low[2] += wq * spin[3 * q + 2];
           }
         }
         double se = dot3(s, P->axis);
@@ -356,6 +428,20 @@ int vo_heis_colour_sweeps(int64_t n, int32_t zmax, const int32_t* nbr, const int
   }
   free(rank);
   return 0;
+}
+
+int vo_heis_colour_sweeps(int64_t n, int32_t zmax, const int32_t* nbr, const int32_t* colour,
+                          int32_t ncol, double* spin, const vo_heis_params* P, int proposal,
+                          uint64_t seed, uint32_t replica, uint32_t sweep0, int32_t nsweeps,
+                          double* obs) {
+  return heis_sweeps(n, zmax, nbr, NULL, colour, ncol, spin, P, proposal, seed, replica, sweep0, nsweeps, obs);
+}
+
+int vo_heis_colour_sweeps_bonds(int64_t n, int32_t zmax, const int32_t* nbr, const double* jb,
+                                const int32_t* colour, int32_t ncol, double* spin, const vo_heis_params* P,
+                                int proposal, uint64_t seed, uint32_t replica, uint32_t sweep0, int32_t nsweeps,
+                                double* obs) {
+  return heis_sweeps(n, zmax, nbr, jb, colour, ncol, spin, P, proposal, seed, replica, sweep0, nsweeps, obs);
 }
 
 /* ============================================================== ref_cpu */

@@ -110,6 +110,20 @@ int vo_heis_colour_sweeps(int64_t n, int32_t zmax, const int32_t* nbr, const int
                           uint64_t seed, uint32_t replica, uint32_t sweep0, int32_t nsweeps,
                           double* obs);
 
+/* Per-bond exchange constants (Exchange's CSR with arbitrary J_ij):
+ * jb[i * zmax + k] is the constant of the bond to neighbour k of site i.
+ * Ising: obs[2 t] = sum over bonds of J_ij s_i s_j, obs[2 t + 1] = M.
+ * Heisenberg: P->J must be 1 (the constants carry the exchange); obs as
+ * vo_heis_colour_sweeps with the bond sum weighted by J_ij. */
+int vo_ising_colour_sweeps_bonds(int64_t n, int32_t zmax, const int32_t* nbr, const double* jb,
+                                 const int32_t* colour, int32_t ncol, int8_t* spin, double hz, double T,
+                                 int proposal, uint64_t seed, uint32_t replica, uint32_t sweep0, int32_t nsweeps,
+                                 double* obs);
+int vo_heis_colour_sweeps_bonds(int64_t n, int32_t zmax, const int32_t* nbr, const double* jb,
+                                const int32_t* colour, int32_t ncol, double* spin, const vo_heis_params* P,
+                                int proposal, uint64_t seed, uint32_t replica, uint32_t sweep0, int32_t nsweeps,
+                                double* obs);
+
 /* ------------------------------------------------ (b) ref_cpu (faithful) */
 typedef struct {
   int32_t has_exchange; double J;

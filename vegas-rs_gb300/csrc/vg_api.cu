@@ -62,6 +62,9 @@ struct vg_ctx {
   double* h_pin = nullptr;  // pinned readback
   size_t h_pin_cap = 0;
   int64_t device_bytes = 0;
+  bool bonds = false;                    // per-bond exchange constants set (generic path)
+  double* d_jb[kMaxColours] = {};        // [z][n_c] per class, FP64
+  float* d_jbf[kMaxColours] = {};        // the same in FP32 (FP32 Heisenberg kernels)
   std::string err;
 };
 
@@ -465,7 +468,8 @@ template <typename R>
 HeisParams<R> heis_params(const vg_ctx* c) {
   HeisParams<R> p;
   const double T = clamp_temperature(c->T);
-  p.J = (R)(c->ham.has_exchange ? c->ham.exchange : 0.0);
+  // per-bond constants carry the exchange in the neighbour field
+  p.J = (R)(c->ham.has_exchange ? (c->bonds ? 1.0 : c->ham.exchange) : 0.0);
   p.K = (R)(c->ham.has_anisotropy ? c->ham.anisotropy : 0.0);
   p.ax = (R)c->ham.anisotropy_axis[0];
   p.ay = (R)c->ham.anisotropy_axis[1];
@@ -550,6 +554,9 @@ int launch_pass(vg_ctx* c, int colour, bool update, uint64_t sweep, void* part_r
       a.lowmask = c->d_low[colour];
       a.n_c = c->class_size[colour];
       a.z = c->z;
+      a.jb = c->bonds ? c->d_jb[colour] : nullptr;
+      a.hz = zeeman_coef(c) * (c->bhat[2] >= 0.0 ? 1.0 : -1.0);
+      a.T = clamp_temperature(c->T);
       e = launch_ising_gen(a, tab, key, colour, c->opt.proposal, update, part, c->grid, c->tpb, c->stream);
     }
   } else {
@@ -584,6 +591,8 @@ int launch_pass(vg_ctx* c, int colour, bool update, uint64_t sweep, void* part_r
       a.lowmask = c->d_low[colour];
       a.n_c = c->class_size[colour];
       a.zc = c->z;
+      a.jb = nullptr;
+      if (c->bonds) a.jb = sizeof(R) == 8 ? (const R*)c->d_jb[colour] : (const R*)c->d_jbf[colour];
       return launch_heis_gen<R>(a, P, key, colour, c->opt.proposal, update, part, c->grid, c->tpb, c->stream);
     };
     e = fp64(c) ? run(0.0) : run(0.0f);
@@ -596,8 +605,10 @@ size_t rows_per_sweep(const vg_ctx* c) { return (size_t)c->ncol * (size_t)c->gri
 
 int launch_reduce(vg_ctx* c, int sweeps, double* out) {
   const long long rows = (long long)rows_per_sweep(c);
-  if (is_ising(c)) reduce_rows<long long><<<sweeps, 256, 0, c->stream>>>((const long long*)c->d_part, rows, out);
-  else reduce_rows<double><<<sweeps, 256, 0, c->stream>>>((const double*)c->d_part, rows, out);
+  if (is_ising(c) && !c->bonds)
+    reduce_rows<long long><<<sweeps, 256, 0, c->stream>>>((const long long*)c->d_part, rows, out);
+  else
+    reduce_rows<double><<<sweeps, 256, 0, c->stream>>>((const double*)c->d_part, rows, out);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(c, e, "reduce launch");
   return VG_OK;
@@ -675,14 +686,15 @@ void energy_of(const vg_ctx* c, const vg_sums* s, double* E, double* M) {
   const double N = (double)c->n;
   const double B = std::fabs(c->bmag);
   double e = 0.0;
+  const double J = c->bonds ? 1.0 : h.exchange;  // per-bond constants are inside the bond sum
   if (h.compound) {
-    if (h.has_exchange) e += -2.0 * h.exchange * s->bond;
+    if (h.has_exchange) e += -2.0 * J * s->bond;
     if (h.has_anisotropy) e += h.anisotropy * s->anisotropy;
     if (h.has_zeeman) e += h.zeeman_sign * B * s->zeeman;
     if (h.has_gauge) e += N * h.gauge;
     if (h.has_cubic) e += -h.cubic * s->cubic;
   } else if (h.has_exchange) {
-    e = -h.exchange * s->bond;
+    e = -J * s->bond;
   } else if (h.has_anisotropy) {
     e = s->anisotropy;
   } else if (h.has_zeeman) {
@@ -775,6 +787,8 @@ void destroy(vg_ctx* c) {
     if (c->d_sites[k]) cudaFree(c->d_sites[k]);
     if (c->d_nbr[k]) cudaFree(c->d_nbr[k]);
     if (c->d_low[k]) cudaFree(c->d_low[k]);
+    if (c->d_jb[k]) cudaFree(c->d_jb[k]);
+    if (c->d_jbf[k]) cudaFree(c->d_jbf[k]);
   }
   if (c->d_stage) cudaFree(c->d_stage);
   if (c->d_part) cudaFree(c->d_part);
@@ -1312,6 +1326,70 @@ int vg_magnetization(vg_ctx* c, double m[3], double* mag) {
 int vg_energy_from_sums(const vg_ctx* c, const vg_sums* s, double* e, double* mag) {
   if (!c || !s) return VG_ERR_INVALID_ARG;
   energy_of(c, s, e, mag);
+  return VG_OK;
+}
+
+int vg_set_exchange_bonds(vg_ctx* c, const double* J, int64_t n_entries) {
+  if (!c) return VG_ERR_INVALID_ARG;
+  VG_CUDA(c, cudaSetDevice(c->device));
+  VG_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (!J) {  // back to the uniform constant
+    for (int k = 0; k < kMaxColours; ++k) {
+      if (c->d_jb[k]) cudaFree(c->d_jb[k]);
+      if (c->d_jbf[k]) cudaFree(c->d_jbf[k]);
+      c->d_jb[k] = nullptr;
+      c->d_jbf[k] = nullptr;
+    }
+    c->bonds = false;
+    return VG_OK;
+  }
+  if (c->path != VG_PATH_GENERIC)
+    return fail(c, VG_ERR_UNSUPPORTED, "per-bond exchange constants need the generic path (vg_options.path)");
+  if (!c->ham.has_exchange) return fail(c, VG_ERR_INVALID_ARG, "the Hamiltonian has no exchange term");
+  if (n_entries != c->n * (int64_t)c->z) return fail(c, VG_ERR_INVALID_ARG, "expected n_sites x coordination entries");
+  Geometry g;
+  std::string why;
+  int rc = geometry_init(&c->lat, &g, &why);
+  if (rc) return fail(c, rc, why);
+  std::vector<int32_t> nbr;
+  build_neighbours(g, nbr);
+  // symmetric (J_ij = J_ji, summed over repeated bonds of one pair) and finite
+  for (int64_t i = 0; i < c->n; ++i)
+    for (int k = 0; k < c->z; ++k) {
+      const int32_t t = nbr[(size_t)i * c->z + k];
+      const double v = J[(size_t)i * c->z + k];
+      if (t < 0) continue;
+      if (!std::isfinite(v)) return fail(c, VG_ERR_INVALID_ARG, "exchange constants must be finite");
+      double a = 0.0, b = 0.0;
+      for (int q = 0; q < c->z; ++q) {
+        if (nbr[(size_t)i * c->z + q] == t) a += J[(size_t)i * c->z + q];
+        if (nbr[(size_t)t * c->z + q] == i) b += J[(size_t)t * c->z + q];
+      }
+      if (std::fabs(a - b) > 1e-12 * std::max(1.0, std::fabs(a)))
+        return fail(c, VG_ERR_INVALID_ARG, "exchange constants must be symmetric (J_ij == J_ji)");
+    }
+  std::vector<int32_t> col;
+  greedy_colouring(g, nbr, col);
+  for (int k = 0; k < c->ncol; ++k) {
+    const int64_t nc = c->class_size[k];
+    std::vector<double> ell((size_t)c->z * nc, 0.0);
+    std::vector<float> ellf(ell.size(), 0.f);
+    int64_t j = 0;
+    for (int64_t i = 0; i < c->n; ++i) {  // class entries in ascending site order
+      if (col[i] != k) continue;
+      for (int q = 0; q < c->z; ++q) {
+        const double v = nbr[(size_t)i * c->z + q] >= 0 ? J[(size_t)i * c->z + q] : 0.0;
+        ell[(size_t)q * nc + j] = v;
+        ellf[(size_t)q * nc + j] = (float)v;
+      }
+      ++j;
+    }
+    if (!c->d_jb[k] && (rc = dalloc(c, (void**)&c->d_jb[k], sizeof(double) * ell.size()))) return rc;
+    if (!c->d_jbf[k] && (rc = dalloc(c, (void**)&c->d_jbf[k], sizeof(float) * ellf.size()))) return rc;
+    VG_CUDA(c, cudaMemcpy(c->d_jb[k], ell.data(), sizeof(double) * ell.size(), cudaMemcpyHostToDevice));
+    VG_CUDA(c, cudaMemcpy(c->d_jbf[k], ellf.data(), sizeof(float) * ellf.size(), cudaMemcpyHostToDevice));
+  }
+  c->bonds = true;
   return VG_OK;
 }
 

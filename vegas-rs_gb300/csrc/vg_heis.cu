@@ -212,7 +212,8 @@ __global__ void __launch_bounds__(256) heis_gen_kernel(const HeisGenArgs<R> a, c
       if (k < a.zc) {
         const int t = __ldg(a.nbr + (long long)k * a.n_c + j);
         if (t >= 0) {
-          const R vx = a.x[t], vy = a.y[t], vz = a.z[t];
+          const R wk = a.jb ? __ldg(a.jb + (long long)k * a.n_c + j) : (R)1;
+          const R vx = wk * a.x[t], vy = wk * a.y[t], vz = wk * a.z[t];
           hs.x += vx;
           hs.y += vy;
           hs.z += vz;

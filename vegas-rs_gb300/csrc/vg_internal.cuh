@@ -123,6 +123,9 @@ struct IsingGenArgs {         // any lattice: natural order uint8 0/1 + ELL
   const uint32_t* lowmask;    // bit k: neighbour k has a lower colour
   long long n_c;
   int z;
+  const double* jb;           // [z][n_c] per-bond exchange constants, or null (uniform J, table thresholds)
+  double hz;                  // per-bond path: per-site Zeeman coefficient (field orientation folded in)
+  double T;                   // per-bond path: temperature (clamped)
 };
 
 template <typename R>
@@ -146,6 +149,7 @@ struct HeisGenArgs {          // any lattice: natural order SoA + ELL
   const uint32_t* lowmask;
   long long n_c;
   int zc;
+  const R* jb;                // [zc][n_c] per-bond exchange constants (then P.J = 1), or null
 };
 
 template <typename R>

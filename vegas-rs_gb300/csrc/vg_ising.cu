@@ -686,6 +686,86 @@ __global__ void __launch_bounds__(256) ising_gen_kernel(const IsingGenArgs a, co
   }
 }
 
+// Per-bond exchange constants (Exchange's CSR with arbitrary J_ij,
+// src/energy.rs:169-206): the field of a site is hJ = sum_k J_k s_k (FP64,
+// k order) and its threshold is formed per site exactly as the host table
+// forms it for uniform J: dE = (-(-s) hJ + hz (-s)) - (-s hJ + hz s),
+// thr = ceil(exp(-dE / T) 2^32).  Same draws and tie digits as the table
+// kernel; partial rows are FP64 (the bond sum sum J_ij s_i s_j is not an
+// integer).
+template <int ZT, bool MEASURE, bool UPDATE, int PROP>
+__global__ void __launch_bounds__(256) ising_bond_kernel(const IsingGenArgs a, const RngKey key, const int colour,
+                                                         double* __restrict__ part) {
+  double bond = 0.0, ups = 0.0, nacc = 0.0;
+  const int z = a.z;
+  const long long ngroups = (a.n_c + 15) >> 4;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < ngroups; g += stride) {
+    const long long j0 = g << 4;
+    int site[16];
+    double hlow[16];
+    unsigned long long t[16];
+    uint32_t S[4] = {0, 0, 0, 0}, valid = 0;
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      const long long j = j0 + k;
+      site[k] = -1;
+      hlow[k] = 0.0;
+      t[k] = 0;
+      if (j < a.n_c) {
+        valid |= 1u << k;
+        const int i = __ldg(a.sites + j);
+        site[k] = i;
+        const uint32_t s01 = a.spin[i];
+        S[k >> 2] |= s01 << (8 * (k & 3));
+        const uint32_t lm = __ldg(a.lowmask + j);
+        double hj = 0.0;
+#pragma unroll
+        for (int q = 0; q < ZT; ++q) {
+          if (q < z) {
+            const int nb = __ldg(a.nbr + (long long)q * a.n_c + j);
+            if (nb >= 0) {
+              const double v = __ldg(a.jb + (long long)q * a.n_c + j) * (double)(2 * (int)a.spin[nb] - 1);
+              hj += v;
+              if ((lm >> q) & 1u) hlow[k] += v;
+            }
+          }
+        }
+        const double sd = s01 ? 1.0 : -1.0;
+        const double e_old = -sd * hj + a.hz * sd;
+        const double e_new = -(-sd) * hj + a.hz * (-sd);
+        const double de = e_new - e_old;
+        if (de <= 0.0) {
+          t[k] = 1ull << 32;
+        } else {
+          const double x = ceil(exp(-de / a.T) * 4294967296.0);
+          t[k] = x >= 4294967296.0 ? (1ull << 32) : x <= 0.0 ? 0ull : (unsigned long long)x;
+        }
+      }
+    }
+    uint32_t flip = 0;
+    if (UPDATE) {
+      const uint32_t cand = (PROP == VG_PROPOSE_FLIP ? 0xFFFFu : propose_random16(S, key, (uint32_t)g, colour)) & valid;
+      flip = decide16(t, cand, key, (uint32_t)g, colour) & cand;
+    }
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      const int s = (S[k >> 2] >> (8 * (k & 3))) & 1;
+      const int sn = s ^ (int)((flip >> k) & 1u);
+      if ((flip >> k) & 1u) a.spin[site[k]] = (uint8_t)sn;
+      if (MEASURE && ((valid >> k) & 1u)) {
+        ups += (double)sn;
+        bond += sn ? hlow[k] : -hlow[k];
+      }
+    }
+    if (MEASURE) nacc += (double)__popc(flip);
+  }
+  if (MEASURE) {
+    double v[kNumSums] = {bond, 0.0, 0.0, 0.0, 0.0, 0.0, ups, nacc};
+    block_sum_store(v, part + (long long)blockIdx.x * kNumSums);
+  }
+}
+
 // ------------------------------------------------------------ dispatch
 // Launch with programmatic stream serialization: the kernel may start while
 // its predecessor on the stream drains and waits (griddepcontrol.wait) for
@@ -786,8 +866,30 @@ static cudaError_t gen_dispatch(const IsingGenArgs& a, const IsingTable& tab, Rn
   return cudaGetLastError();
 }
 
+template <int ZT>
+static cudaError_t bond_dispatch(const IsingGenArgs& a, RngKey key, int colour, int proposal, bool update,
+                                 double* part, int grid, int tpb, cudaStream_t s) {
+  const bool m = part != nullptr;
+  if (!update) {
+    ising_bond_kernel<ZT, true, false, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, key, colour, part);
+  } else if (proposal == VG_PROPOSE_FLIP) {
+    if (m) ising_bond_kernel<ZT, true, true, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, key, colour, part);
+    else ising_bond_kernel<ZT, false, true, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, key, colour, part);
+  } else {
+    if (m) ising_bond_kernel<ZT, true, true, VG_PROPOSE_RANDOM><<<grid, tpb, 0, s>>>(a, key, colour, part);
+    else ising_bond_kernel<ZT, false, true, VG_PROPOSE_RANDOM><<<grid, tpb, 0, s>>>(a, key, colour, part);
+  }
+  return cudaGetLastError();
+}
+
 cudaError_t launch_ising_gen(const IsingGenArgs& a, const IsingTable& tab, RngKey key, int colour, int proposal,
                              bool update, long long* part, int grid, int tpb, cudaStream_t s) {
+  if (a.jb) {  // per-bond constants: FP64 partial rows in the same 8-byte slots
+    double* dpart = reinterpret_cast<double*>(part);
+    if (a.z <= 6) return bond_dispatch<6>(a, key, colour, proposal, update, dpart, grid, tpb, s);
+    if (a.z <= 8) return bond_dispatch<8>(a, key, colour, proposal, update, dpart, grid, tpb, s);
+    return bond_dispatch<12>(a, key, colour, proposal, update, dpart, grid, tpb, s);
+  }
   if (a.z <= 6) return gen_dispatch<6>(a, tab, key, colour, proposal, update, part, grid, tpb, s);
   if (a.z <= 8) return gen_dispatch<8>(a, tab, key, colour, proposal, update, part, grid, tpb, s);
   return gen_dispatch<12>(a, tab, key, colour, proposal, update, part, grid, tpb, s);

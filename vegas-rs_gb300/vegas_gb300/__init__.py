@@ -292,6 +292,15 @@ class Engine:
         _check(lib().vg_time_passes(self._h, C.c_uint64(n), int(measure), C.byref(a), C.byref(b)), self._h)
         return a.value, b.value
 
+    def set_exchange_bonds(self, J: Optional[np.ndarray]):
+        """Per-bond exchange constants (n_sites x coordination, the order of
+        Lattice.neighbours()); None restores the uniform constant."""
+        if J is None:
+            _check(lib().vg_set_exchange_bonds(self._h, None, 0), self._h)
+            return
+        a = np.ascontiguousarray(J, dtype=np.float64)
+        _check(lib().vg_set_exchange_bonds(self._h, a.ctypes.data_as(C.POINTER(C.c_double)), a.size), self._h)
+
     # observables
     def current_sums(self) -> np.ndarray:
         s = Sums()
