@@ -292,6 +292,43 @@ def run_cooldown_2d(V, torch, args):
             "path": {1: "generic", 2: "structured", 3: "resident"}.get(path, "?"), "cpu_baseline": cpu}
 
 
+def run_wolff(V, torch, args):
+    """docs/wolff.toml's workload shape: sc 10x10x10 Ising, Wolff cluster
+    steps; a bounded sample of 20,000 steps at T = 4.5 (near the critical
+    point, where clusters are largest in spread) on the single-block kernel,
+    beside the same steps of the oracle's cluster algorithm on one core."""
+    import oracle as O
+
+    lat = V.Lattice.sc(10, 10, 10)
+    n = 20000
+    with V.Engine(lat, V.hamiltonian(V.Exchange(1.0)), seed=SEED) as eng:
+        eng.init_random()
+        eng.set_thermostat(4.5)
+        eng.wolff_steps(2000)
+        s = torch.cuda.ExternalStream(eng.stream())
+        a, c = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(s)
+        lib = V.lib()
+        import ctypes as C
+
+        V._check(lib.vg_wolff_steps(eng._h, C.c_uint64(n), 0, None, None), eng._h)
+        c.record(s)
+        eng.synchronize()
+        ms = a.elapsed_time(c)
+        state = eng.get_state()
+    cpu = None
+    if not args.no_cpu_baseline:
+        g = O.Graph(O.lattice("sc", 10, 10, 10))
+        t0 = time.perf_counter()
+        _, obs = g.wolff_steps(state, 1.0, 4.5, SEED, 0, n)
+        dt = time.perf_counter() - t0
+        cpu = {"value": n / dt, "unit": "cluster steps/s", "cores": 1, "kind": "port",
+               "sample": f"{n} cluster steps of the oracle's Wolff algorithm at T = 4.5 on one core",
+               "mean_cluster": float(obs[:, 2].mean())}
+    return {"workload": "sc 10x10x10 Ising, Wolff cluster steps (docs/wolff.toml lattice), T = 4.5",
+            "value": n / (ms * 1e-3), "unit": "cluster steps/s", "ms": ms, "steps": n, "cpu_baseline": cpu}
+
+
 def run_heisenberg(V, torch, args):
     """Heisenberg sc 128^3, J=1, K=0.1 along z, B=0.05 along z, uniform-on-sphere
     proposals, FP32 updates with FP64 sums; a step is 100 measured sweeps at the
@@ -548,6 +585,7 @@ def main():
         batched = run_batched(V, torch, args)
 
     cool = run_cooldown_2d(V, torch, args) if not args.no_heisenberg else None
+    wolff = run_wolff(V, torch, args) if not args.no_heisenberg else None
     heis = hyst = None
     if not args.no_heisenberg:
         heis = run_heisenberg(V, torch, args)
@@ -585,6 +623,7 @@ def main():
             "batched": batched,
             "batched_vs_plain": (batched["value"] / value) if batched else None,
             "cooldown_2d": cool,
+            "wolff": wolff,
             "heisenberg": heis,
             "hysteresis_batch": hyst,
             "clocks": clk.summary(),

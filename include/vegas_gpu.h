@@ -180,6 +180,16 @@ int vg_synchronize(vg_ctx* ctx);
  * duration (ms).  The sweeps are real work (the sweep index advances). */
 int vg_time_passes(vg_ctx* ctx, uint64_t n, int32_t measure, double* mean_pass_ms, double* mean_sweep_ms);
 
+/* Wolff cluster steps (WolffIntegrator::step, src/integrator.rs:140-230) of
+ * an Ising context: each step picks a source site, grows the cluster of
+ * spins equal to it over bonds active with probability 1 - exp(-2 J / T)
+ * (the Hamiltonian's exchange constant J, the thermostat's T; the field is
+ * not used, as in the reference) and flips it.  Per step, E and |M| as
+ * vg_sweeps; vg_sums.accepted of vg_current_sums-style rows is the cluster
+ * size.  A step advances the context's sweep index by one.  Lattices of at
+ * most 16384 sites (one thread block). */
+int vg_wolff_steps(vg_ctx* ctx, uint64_t n_steps, int32_t measure, double* E, double* M);
+
 /* Per-bond exchange constants: Exchange's CSR with arbitrary J_ij
  * (src/energy.rs:169-206) instead of one constant for every bond.
  * J[i * z + k] is the constant of the bond from site i to its k-th

@@ -102,6 +102,8 @@ def lib():
         L.vo_heis_colour_sweeps_bonds.argtypes = [C.c_int64, C.c_int32, P(C.c_int32), P(C.c_double),
                                                   P(C.c_int32), C.c_int32, P(C.c_double), P(HeisParams), C.c_int,
                                                   C.c_uint64, C.c_uint32, C.c_uint32, C.c_int32, P(C.c_double)]
+        L.vo_wolff_steps.argtypes = [C.c_int64, C.c_int32, P(C.c_int32), P(C.c_int8), C.c_double, C.c_double,
+                                     C.c_uint64, C.c_uint32, C.c_uint32, C.c_int32, P(C.c_double)]
         L.vo_pcg64_seed.argtypes = [P(Pcg64), C.c_uint64]
         L.vo_pcg64_next.argtypes = [P(Pcg64)]
         L.vo_pcg64_next.restype = C.c_uint64
@@ -214,6 +216,14 @@ class Graph:
                                           C.byref(params), proposal, seed, replica, sweep0, nsweeps,
                                           _p(obs, C.c_double))
         return spin, obs[:nsweeps]
+
+    def wolff_steps(self, spin, J, T, seed, step0, nsteps, replica=0):
+        """Wolff cluster steps with the GPU's draws; obs rows (bond sum, M, cluster size)."""
+        spin = np.ascontiguousarray(spin, dtype=np.int8).copy()
+        obs = np.zeros((max(nsteps, 1), 3), dtype=np.float64)
+        lib().vo_wolff_steps(self.n, self.zmax, _p(self.nbr, C.c_int32), _p(spin, C.c_int8), J, T, seed, replica,
+                             step0, nsteps, _p(obs, C.c_double))
+        return spin, obs[:nsteps]
 
     def symmetric_bonds(self, rng, values=(0.5, 1.0, 1.5)):
         """Random symmetric per-bond constants drawn from `values`

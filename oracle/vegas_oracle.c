@@ -327,6 +327,71 @@ int vo_ising_colour_sweeps_bonds(int64_t n, int32_t zmax, const int32_t* nbr, co
   return 0;
 }
 
+/* Wolff cluster steps (WolffIntegrator::step, src/integrator.rs:140-230)
+ * with the GPU's draws: source = (Philox(step, 0, TAG_WOLFF_SOURCE << 24,
+ * replica).w0 * n) >> 32; the bond k of site i to j = nbr[i][k] (occurrence
+ * o among the repeated bonds of that pair) is active iff Philox(min(i, j),
+ * max(i, j), TAG_WOLFF_BOND << 24 | o << 20 | replica, step).w0 < thr, thr =
+ * ceil((1 - exp(-2 J / T)) 2^32).  The cluster is grown with a queue as the
+ * reference does; obs[3 t .. 3 t + 2] = {bond sum, magnetisation, cluster
+ * size} after step t. */
+int vo_wolff_steps(int64_t n, int32_t zmax, const int32_t* nbr, int8_t* spin, double J, double T, uint64_t seed,
+                   uint32_t replica, uint32_t step0, int32_t nsteps, double* obs) {
+  if (T < 2.220446049250313e-16) T = 2.220446049250313e-16;
+  const double p = 1.0 - exp(-2.0 * J / T);
+  uint64_t thr = 0;
+  if (p > 0.0) {
+    double x = ceil(p * 4294967296.0);
+    thr = x >= 4294967296.0 ? (1ull << 32) : (uint64_t)x;
+  }
+  uint8_t* in = (uint8_t*)malloc((size_t)n);
+  int64_t* queue = (int64_t*)malloc(sizeof(int64_t) * (size_t)n);
+  for (int32_t t = 0; t < nsteps; ++t) {
+    uint32_t step = step0 + (uint32_t)t;
+    uint32_t w[4];
+    draw(seed, step, 0, (uint32_t)VO_TAG_WOLFF_SOURCE << 24, replica, w);
+    int64_t src = (int64_t)(((uint64_t)w[0] * (uint64_t)n) >> 32);
+    memset(in, 0, (size_t)n);
+    int8_t ref = spin[src];
+    int64_t head = 0, tail = 0;
+    queue[tail++] = src;
+    in[src] = 1;
+    while (head < tail) {
+      int64_t i = queue[head++];
+      for (int k = 0; k < zmax; ++k) {
+        int32_t j = nbr[i * zmax + k];
+        if (j < 0 || in[j] || spin[j] != ref) continue;
+        uint32_t o = 0;
+        for (int q = 0; q < k; ++q) o += nbr[i * zmax + q] == j;
+        uint32_t lo = (uint32_t)(i < j ? i : j), hi = (uint32_t)(i < j ? j : i);
+        draw(seed, lo, hi, ((uint32_t)VO_TAG_WOLFF_BOND << 24) | (o << 20) | (replica & 0xFFFFFu), step, w);
+        if ((uint64_t)w[0] < thr) {
+          in[j] = 1;
+          queue[tail++] = j;
+        }
+      }
+    }
+    for (int64_t i = 0; i < n; ++i)
+      if (in[i]) spin[i] = (int8_t)(-spin[i]);
+    if (obs) {
+      int64_t bond = 0, mag = 0;
+      for (int64_t i = 0; i < n; ++i) {
+        mag += spin[i];
+        for (int k = 0; k < zmax; ++k) {
+          int32_t j = nbr[i * zmax + k];
+          if (j > i) bond += (int64_t)spin[i] * spin[j];
+        }
+      }
+      obs[3 * t] = (double)bond;
+      obs[3 * t + 1] = (double)mag;
+      obs[3 * t + 2] = (double)tail;
+    }
+  }
+  free(in);
+  free(queue);
+  return 0;
+}
+
 /* ===================================================== Heisenberg oracle */
 /* Uniform point on S^2 (Archimedes: z uniform in (-1,1), azimuth uniform):
  * z = (2k + 1 - 2^24) / 2^24 with k = w0 >> 8, azimuth = pi * (w1 >> 8) / 2^23.

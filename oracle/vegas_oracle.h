@@ -124,6 +124,12 @@ int vo_heis_colour_sweeps_bonds(int64_t n, int32_t zmax, const int32_t* nbr, con
                                 int proposal, uint64_t seed, uint32_t replica, uint32_t sweep0, int32_t nsweeps,
                                 double* obs);
 
+/* Wolff cluster steps with the GPU's draws (tags 9: source, 10: bonds).
+ * obs[3 t .. 3 t + 2] = {bond sum, magnetisation, cluster size}. */
+enum { VO_TAG_WOLFF_SOURCE = 9, VO_TAG_WOLFF_BOND = 10 };
+int vo_wolff_steps(int64_t n, int32_t zmax, const int32_t* nbr, int8_t* spin, double J, double T, uint64_t seed,
+                   uint32_t replica, uint32_t step0, int32_t nsteps, double* obs);
+
 /* ------------------------------------------------ (b) ref_cpu (faithful) */
 typedef struct {
   int32_t has_exchange; double J;

@@ -62,6 +62,8 @@ struct vg_ctx {
   double* h_pin = nullptr;  // pinned readback
   size_t h_pin_cap = 0;
   int64_t device_bytes = 0;
+  int32_t* d_wnbr = nullptr;             // Wolff: natural-order neighbour table [n][z]
+  uint8_t* d_wocc = nullptr;             // Wolff: occurrence of each bond among repeated ones
   bool bonds = false;                    // per-bond exchange constants set (generic path)
   double* d_jb[kMaxColours] = {};        // [z][n_c] per class, FP64
   float* d_jbf[kMaxColours] = {};        // the same in FP32 (FP32 Heisenberg kernels)
@@ -366,6 +368,8 @@ bool is_ising(const vg_ctx* c) { return c->opt.spin_kind == VG_SPIN_ISING; }
 bool sc_layout(const vg_ctx* c) { return c->path == VG_PATH_STRUCTURED || c->path == VG_PATH_RESIDENT; }
 bool fp64(const vg_ctx* c) { return c->opt.precision == VG_FP64; }
 size_t real_size(const vg_ctx* c) { return fp64(c) ? 8 : 4; }
+
+constexpr int64_t kWolffMaxSites = 16384;  // one block's shared memory holds the Wolff state
 
 int dalloc(vg_ctx* c, void** p, size_t bytes) {
   if (bytes == 0) bytes = 16;
@@ -791,6 +795,8 @@ void destroy(vg_ctx* c) {
     if (c->d_jbf[k]) cudaFree(c->d_jbf[k]);
   }
   if (c->d_stage) cudaFree(c->d_stage);
+  if (c->d_wnbr) cudaFree(c->d_wnbr);
+  if (c->d_wocc) cudaFree(c->d_wocc);
   if (c->d_part) cudaFree(c->d_part);
   if (c->d_sums) cudaFree(c->d_sums);
   if (c->d_flag) cudaFree(c->d_flag);
@@ -1326,6 +1332,76 @@ int vg_magnetization(vg_ctx* c, double m[3], double* mag) {
 int vg_energy_from_sums(const vg_ctx* c, const vg_sums* s, double* e, double* mag) {
   if (!c || !s) return VG_ERR_INVALID_ARG;
   energy_of(c, s, e, mag);
+  return VG_OK;
+}
+
+int vg_wolff_steps(vg_ctx* c, uint64_t n, int32_t measure, double* E, double* M) {
+  if (!c) return VG_ERR_INVALID_ARG;
+  if (!is_ising(c)) return fail(c, VG_ERR_UNSUPPORTED, "Wolff steps need an Ising context");
+  if (c->n > kWolffMaxSites)
+    return fail(c, VG_ERR_UNSUPPORTED, "Wolff steps run in one thread block: at most 16384 sites");
+  if (c->bonds) return fail(c, VG_ERR_UNSUPPORTED, "Wolff steps use the uniform exchange constant");
+  VG_CUDA(c, cudaSetDevice(c->device));
+  int rc;
+  if (!c->d_wnbr) {  // neighbour table and bond occurrences, natural site order
+    Geometry g;
+    std::string why;
+    if ((rc = geometry_init(&c->lat, &g, &why))) return fail(c, rc, why);
+    std::vector<int32_t> nbr;
+    build_neighbours(g, nbr);
+    std::vector<uint8_t> occ(nbr.size(), 0);
+    for (int64_t i = 0; i < c->n; ++i)
+      for (int k = 0; k < c->z; ++k) {
+        const int32_t t = nbr[(size_t)i * c->z + k];
+        uint8_t o = 0;
+        for (int q = 0; q < k; ++q) o += nbr[(size_t)i * c->z + q] == t;
+        occ[(size_t)i * c->z + k] = o;
+      }
+    if ((rc = dalloc(c, (void**)&c->d_wnbr, sizeof(int32_t) * nbr.size()))) return rc;
+    if ((rc = dalloc(c, (void**)&c->d_wocc, occ.size()))) return rc;
+    VG_CUDA(c, cudaMemcpy(c->d_wnbr, nbr.data(), sizeof(int32_t) * nbr.size(), cudaMemcpyHostToDevice));
+    VG_CUDA(c, cudaMemcpy(c->d_wocc, occ.data(), occ.size(), cudaMemcpyHostToDevice));
+  }
+  // bond probability 1 - exp(-2 J / T) as a threshold on a 32-bit word (src/integrator.rs:199-203)
+  const double J = c->ham.has_exchange ? c->ham.exchange : 0.0;
+  const double T = clamp_temperature(c->T);
+  const double p = 1.0 - std::exp(-2.0 * J / T);
+  unsigned long long thr;
+  if (!(p > 0.0)) thr = 0;
+  else {
+    const double x = std::ceil(p * 4294967296.0);
+    thr = x >= 4294967296.0 ? (1ull << 32) : (unsigned long long)x;
+  }
+  if ((rc = ensure_stage(c, (size_t)c->n))) return rc;
+  if (measure && (rc = ensure_sums(c, (size_t)std::max<uint64_t>(n, 1)))) return rc;
+  const int structured = sc_layout(c);
+  const ScMap m = sc_map(c);
+  ising_export<<<copy_grid(c, c->n), 256, 0, c->stream>>>((int8_t*)c->d_stage, c->n, structured, m,
+                                                          (const uint8_t*)c->spin[0][0],
+                                                          (const uint8_t*)c->spin[1][0]);
+  VG_CUDA(c, cudaGetLastError());
+  for (uint64_t t0 = 0; t0 < n; t0 += (1u << 30)) {
+    const uint32_t k = (uint32_t)std::min<uint64_t>(n - t0, 1u << 30);
+    const cudaError_t e = launch_ising_wolff((int8_t*)c->d_stage, (int)c->n, c->z, c->d_wnbr, c->d_wocc, thr,
+                                             rng_key(c, c->sweep + t0), k,
+                                             measure ? c->d_sums + t0 * kNumSums : nullptr, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "Wolff kernel launch");
+  }
+  VG_CUDA(c, cudaMemsetAsync(c->d_flag, 0, sizeof(int), c->stream));
+  ising_import<<<copy_grid(c, c->n), 256, 0, c->stream>>>((const int8_t*)c->d_stage, c->n, structured, m,
+                                                          (uint8_t*)c->spin[0][0], (uint8_t*)c->spin[1][0],
+                                                          c->d_flag);
+  VG_CUDA(c, cudaGetLastError());
+  c->sweep += n;
+  if (!measure) return sync_stream(c);
+  c->last_batch = n;
+  double* raw = nullptr;
+  if ((rc = read_raw(c, n, &raw))) return rc;
+  for (uint64_t t = 0; t < n; ++t) {
+    vg_sums s;
+    finish_sums(c, raw + t * kNumSums, &s);
+    energy_of(c, &s, E ? E + t : nullptr, M ? M + t : nullptr);
+  }
   return VG_OK;
 }
 

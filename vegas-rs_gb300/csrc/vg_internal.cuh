@@ -165,6 +165,10 @@ struct HeisParams {
 cudaError_t launch_ising_sc(const IsingScArgs& a, const IsingTable& tab, RngKey key, int colour,
                             int proposal, bool update, long long* part, int grid, int tpb, cudaStream_t s);
 int ising_sc_blocks_per_sm(const IsingScArgs& a, const IsingTable& tab, int tpb);
+// Wolff cluster steps on natural-order int8 +-1 spins, one block.
+size_t ising_wolff_smem(int n);
+cudaError_t launch_ising_wolff(int8_t* spins, int n, int z, const int32_t* nbr, const uint8_t* occ,
+                               unsigned long long thr, RngKey key, uint32_t n_steps, double* sums, cudaStream_t s);
 size_t ising_resident_smem(const IsingScArgs& a);
 cudaError_t launch_ising_resident(const IsingScArgs& a, const IsingTable& tab, RngKey key, int proposal,
                                   uint32_t n_sweeps, double* sums, int tpb, cudaStream_t s);

@@ -123,6 +123,7 @@ static void cpu_checks() {
   try {
     Input w = def;
     w.algorithm = "Wolff";
+    w.model = "Heisenberg";  // (Heisenberg, Wolff) is not implemented (src/input.rs:365)
     w.run(1, stdout);
   } catch (const NotImplementedError&) {
     wolff = true;

@@ -8,7 +8,8 @@
 // Zeeman), a random initial state, T = 2.8 with zero field, StatSensor on
 // stdout plus the optional observable / state outputs, then each stage in
 // order.  Ising uses the flip proposal and Heisenberg the random proposal,
-// as the reference picks; Wolff has no GPU integrator (not implemented).
+// as the reference picks; Wolff runs the GPU cluster steps for Ising and is
+// not implemented for Heisenberg (src/input.rs:354-365).
 #pragma once
 
 #include <cctype>
@@ -228,7 +229,11 @@ struct Input {
   }
 
   void run(uint64_t seed, FILE* out = stdout) const {
-    if (algorithm == "Wolff") throw NotImplementedError();
+    if (algorithm == "Wolff") {
+      if (model != "Ising") throw NotImplementedError();
+      run_with_spin<IsingSpin>(WolffIntegrator(seed), out);
+      return;
+    }
     if (model == "Ising") run_with_spin<IsingSpin>(MetropolisFlipIntegrator(seed), out);
     else run_with_spin<HeisenbergSpin>(MetropolisIntegrator(seed), out);
   }

@@ -9,8 +9,9 @@
 // is the state after exactly that sweep.
 //
 // The integrators are the GPU counterparts of MetropolisIntegrator
-// (random proposal, src/integrator.rs:56-92) and MetropolisFlipIntegrator
-// (flip proposal, :99-138); their RNG is the engine's counter-based Philox
+// (random proposal, src/integrator.rs:56-92), MetropolisFlipIntegrator
+// (flip proposal, :99-138) and WolffIntegrator (cluster steps, :140-230);
+// their RNG is the engine's counter-based Philox
 // stream keyed by (seed, replica, sweep), so relax_for / measure_for take no
 // RNG argument.
 #pragma once
@@ -35,6 +36,7 @@ struct GpuIntegrator {
   uint32_t replica = 0;
   int path = VG_PATH_AUTO;
   int precision = VG_FP32;
+  bool cluster = false;  // Wolff cluster steps (vg_wolff_steps) instead of Metropolis sweeps
 };
 
 struct MetropolisIntegrator : GpuIntegrator {
@@ -43,6 +45,12 @@ struct MetropolisIntegrator : GpuIntegrator {
 
 struct MetropolisFlipIntegrator : GpuIntegrator {
   explicit MetropolisFlipIntegrator(uint64_t seed = 0) : GpuIntegrator{VG_PROPOSE_FLIP, seed} {}
+};
+
+// WolffIntegrator (src/integrator.rs:140-230): one cluster flip per step,
+// bond probability from the Hamiltonian's exchange constant; Ising only.
+struct WolffIntegrator : GpuIntegrator {
+  explicit WolffIntegrator(uint64_t seed = 0) : GpuIntegrator{VG_PROPOSE_FLIP, seed} { cluster = true; }
 };
 
 template <typename H, typename I, typename S>
@@ -129,7 +137,12 @@ class Machine {
         E.resize(chunk);
         M.resize(chunk);
       }
-      check(vg_sweeps(ctx_, chunk, measure ? 1 : 0, measure ? E.data() : nullptr, measure ? M.data() : nullptr), ctx_);
+      if (integrator_.cluster)
+        check(vg_wolff_steps(ctx_, chunk, measure ? 1 : 0, measure ? E.data() : nullptr, measure ? M.data() : nullptr),
+              ctx_);
+      else
+        check(vg_sweeps(ctx_, chunk, measure ? 1 : 0, measure ? E.data() : nullptr, measure ? M.data() : nullptr),
+              ctx_);
       for (size_t k = 0; k < chunk; ++k) {
         const bool last = k + 1 == chunk;
         StepView<S> v{measure ? E[k] : 0.0, measure ? M[k] : 0.0, n_, [this, last]() {

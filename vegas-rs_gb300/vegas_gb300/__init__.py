@@ -292,6 +292,14 @@ class Engine:
         _check(lib().vg_time_passes(self._h, C.c_uint64(n), int(measure), C.byref(a), C.byref(b)), self._h)
         return a.value, b.value
 
+    def wolff_steps(self, n: int, measure: bool = True):
+        """n Wolff cluster steps (WolffIntegrator); returns (E, |M|) per step."""
+        E = np.zeros(max(n, 1))
+        M = np.zeros(max(n, 1))
+        _check(lib().vg_wolff_steps(self._h, C.c_uint64(n), int(measure), E.ctypes.data_as(C.POINTER(C.c_double)),
+                                    M.ctypes.data_as(C.POINTER(C.c_double))), self._h)
+        return E[:n], M[:n]
+
     def set_exchange_bonds(self, J: Optional[np.ndarray]):
         """Per-bond exchange constants (n_sites x coordination, the order of
         Lattice.neighbours()); None restores the uniform constant."""
