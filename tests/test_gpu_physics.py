@@ -79,6 +79,32 @@ def test_ising_matches_reference_cpu(V, O, T):
     c1, d1 = jackknife_var(Eg, scale=1.0 / (N * T * T))
     c2, d2 = jackknife_var(Er, scale=1.0 / (N * T * T))
     assert abs(c1 - c2) < 3 * np.hypot(d1, d2), (T, c1, d1, c2, d2)
+    # susceptibility Var(|M|)/(N T) (src/instrument.rs:123-126)
+    x1, f1 = jackknife_var(Mg, scale=1.0 / (N * T))
+    x2, f2 = jackknife_var(Mr, scale=1.0 / (N * T))
+    assert abs(x1 - x2) < 3 * np.hypot(f1, f2), (T, x1, f1, x2, f2)
+
+
+def test_ising_3d_matches_reference_cpu(V, O):
+    """sc 16^3, full PBC, T = 4.0 (ordered side of the transition)."""
+    T, L, therm, sweeps = 4.0, 16, 2000, 20000
+    N = L ** 3
+    H = V.hamiltonian(V.Exchange(1.0), V.Zeeman())
+    with V.Engine(V.Lattice.sc(L, L, L), H, seed=23) as eng:
+        eng.init_random()
+        eng.set_thermostat(T)
+        eng.sweeps(therm, measure=False)
+        Eg, Mg = eng.sweeps(sweeps)
+    g = O.Graph(O.lattice("sc", L, L, L))
+    Hr = O.Hamiltonian(has_exchange=1, J=1.0, has_zeeman=1, zeeman_sign=1.0, compound=1)
+    _, obs = g.ref_sweeps(0, g.ising_init(4), Hr, T, therm + sweeps, O.pcg64(99), proposal=O.PROPOSE_FLIP)
+    Er, Mr = obs[therm:, 0], obs[therm:, 1]
+    for a, b in ((Eg / N, Er / N), (Mg / N, Mr / N)):
+        (m1, e1), (m2, e2) = binned(a), binned(b)
+        assert abs(m1 - m2) < 3 * np.hypot(e1, e2), (m1, e1, m2, e2)
+    c1, d1 = jackknife_var(Eg, scale=1.0 / (N * T * T))
+    c2, d2 = jackknife_var(Er, scale=1.0 / (N * T * T))
+    assert abs(c1 - c2) < 3 * np.hypot(d1, d2), (c1, d1, c2, d2)
 
 
 def test_heisenberg_matches_reference_cpu(V, O):
@@ -100,3 +126,9 @@ def test_heisenberg_matches_reference_cpu(V, O):
     for a, b in ((Eg / N, obs[1000:, 0] / N), (Mg / N, obs[1000:, 1] / N)):
         (m1, e1), (m2, e2) = binned(a), binned(b)
         assert abs(m1 - m2) < 3 * np.hypot(e1, e2), (m1, e1, m2, e2)
+    c1, d1 = jackknife_var(Eg, scale=1.0 / (N * T * T))
+    c2, d2 = jackknife_var(obs[1000:, 0], scale=1.0 / (N * T * T))
+    assert abs(c1 - c2) < 3 * np.hypot(d1, d2), (c1, d1, c2, d2)
+    x1, f1 = jackknife_var(Mg, scale=1.0 / (N * T))
+    x2, f2 = jackknife_var(obs[1000:, 1], scale=1.0 / (N * T))
+    assert abs(x1 - x2) < 3 * np.hypot(f1, f2), (x1, f1, x2, f2)
