@@ -14,10 +14,17 @@
 // extent 2) are distinct bonds (occurrence 0, 1, ...), as in the
 // reference's neighbour list.
 //
-// The block keeps the spins (int8 +-1, natural site order), a cluster bit
-// mask and two frontier lists in shared memory and expands the frontier one
-// level per round; after the flip it writes the step's raw sums (bond sum,
-// up spins, cluster size) in the layout of the Metropolis kernels.
+// The block keeps the spins (int8 +-1, natural site order), a per-site
+// stamp (the step that last put the site in a cluster, so that nothing is
+// cleared between steps) and the cluster as one queue in shared memory.  The
+// queue grows one breadth-first level per round, with one barrier a level:
+// level L appends through counter L mod 3, whose value every thread reads
+// after the barrier, and thread 0 zeroes the counter of level L + 2 then, two
+// barriers before it is used again.  After the last level one pass over the
+// cluster's bonds flips the cluster and sums the bonds it cuts, which updates
+// the bond sum and the up count of the previous step instead of recounting
+// the lattice: the step's raw sums (bond sum, up spins, cluster size) land in
+// the layout of the Metropolis kernels.
 #include <cuda_runtime.h>
 
 #include "vg_internal.cuh"
@@ -34,116 +41,116 @@ __global__ void __launch_bounds__(1024) ising_wolff_kernel(int8_t* __restrict__ 
                                                            unsigned long long thr, RngKey key, uint32_t n_steps,
                                                            double* __restrict__ sums) {
   extern __shared__ uint32_t s_mem[];
-  uint32_t* inc = s_mem;                            // cluster bits, (n + 31) / 32 words
-  int32_t* fa = (int32_t*)(inc + ((n + 31) >> 5));  // frontier lists
-  int32_t* fb = fa + n;
-  int8_t* s = (int8_t*)(fb + n);
-  __shared__ int s_count[2];
-  __shared__ int s_src;
-  __shared__ int s_red[3][32];
-  const int nw = (n + 31) >> 5;
+  uint32_t* mark = s_mem;                  // step stamp + 1 of the last cluster holding the site
+  int32_t* q = (int32_t*)(mark + n);       // the cluster, in breadth-first order
+  int8_t* s = (int8_t*)(q + n);
+  __shared__ int s_cnt[3];
+  __shared__ int s_red[2][32];
+  __shared__ int s_cut;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) s[i] = spins[i];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    s[i] = spins[i];
+    mark[i] = 0u;
+  }
+  if (threadIdx.x < 3) s_cnt[threadIdx.x] = 0;
+  if (threadIdx.x == 0) s_cut = 0;
   __syncthreads();
+  // the bond sum and up count of the incoming state, once per call
+  long long bond = 0, ups = 0;
+  if (sums) {
+    int b = 0, u = 0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      const int si = s[i];
+      u += si > 0;
+      for (int k = 0; k < z; ++k) {  // each bond once, from its lower site
+        const int j = __ldg(nbr + (size_t)i * z + k);
+        if (j > i) b += si * s[j];
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      b += __shfl_down_sync(0xffffffffu, b, o);
+      u += __shfl_down_sync(0xffffffffu, u, o);
+    }
+    if (lane == 0) {
+      s_red[0][warp] = b;
+      s_red[1][warp] = u;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+        bond += s_red[0][w];
+        ups += s_red[1][w];
+      }
+  }
   for (uint32_t t = 0; t < n_steps; ++t) {
     const uint32_t step = key.sweep + t;
-    for (int i = threadIdx.x; i < nw; i += blockDim.x) inc[i] = 0u;
-    if (threadIdx.x == 0) {
-      const uint4 w = philox_ks(make_uint4(step, 0u, kTagWolffSource << 24, key.replica), key.ks);
-      s_src = (int)(((unsigned long long)w.x * (unsigned long long)n) >> 32);
-      s_count[0] = 1;
-      s_count[1] = 0;
-    }
-    __syncthreads();
-    const int src = s_src;
+    const uint32_t stamp = t + 1;
+    // the source depends on the step alone: every thread draws it
+    const uint4 w0 = philox_ks(make_uint4(step, 0u, kTagWolffSource << 24, key.replica), key.ks);
+    const int src = (int)(((unsigned long long)w0.x * (unsigned long long)n) >> 32);
     const int8_t ref = s[src];
-    if (threadIdx.x == 0) {
-      inc[src >> 5] = 1u << (src & 31);
-      fa[0] = src;
-    }
-    __syncthreads();
-    int32_t* cur = fa;
-    int32_t* nxt = fb;
-    int ci = 0;
-    int na = 1;
-    while (na > 0) {
-      for (int e = threadIdx.x; e < na; e += blockDim.x) {
-        const int site = cur[e];
-        for (int k = 0; k < z; ++k) {
-          const int j = __ldg(nbr + (size_t)site * z + k);
-          if (j < 0 || s[j] != ref) continue;
-          if ((inc[j >> 5] >> (j & 31)) & 1u) continue;
-          const uint32_t lo = (uint32_t)min(site, j), hi = (uint32_t)max(site, j);
-          const uint32_t o = __ldg(occ + (size_t)site * z + k);
-          const uint4 w = philox_ks(make_uint4(lo, hi, (kTagWolffBond << 24) | (o << 20) | (key.replica & 0xFFFFFu), step),
-                                    key.ks);
-          if ((unsigned long long)w.x < thr) {
-            const uint32_t bit = 1u << (j & 31);
-            if (!(atomicOr(&inc[j >> 5], bit) & bit)) nxt[atomicAdd(&s_count[ci ^ 1], 1)] = j;
-          }
-        }
+    mark[src] = stamp;  // the same value from every thread
+    if (threadIdx.x == 0) q[0] = src;
+    int lo = 0, hi = 1, lev = 0;
+    for (;;) {
+      // one thread per (frontier site, neighbour slot) of this level
+      const int items = (hi - lo) * z;
+      int* cnt = &s_cnt[lev % 3];
+      for (int e = threadIdx.x; e < items; e += blockDim.x) {
+        const int fi = e / z, k = e - fi * z;
+        const int site = lo == 0 ? src : q[lo + fi];
+        const int j = __ldg(nbr + (size_t)site * z + k);
+        if (j < 0 || s[j] != ref || mark[j] == stamp) continue;
+        const uint32_t a = (uint32_t)min(site, j), b = (uint32_t)max(site, j);
+        const uint32_t o = __ldg(occ + (size_t)site * z + k);
+        const uint4 w = philox_ks(make_uint4(a, b, (kTagWolffBond << 24) | (o << 20) | (key.replica & 0xFFFFFu), step),
+                                  key.ks);
+        if ((unsigned long long)w.x < thr && atomicExch(&mark[j], stamp) != stamp) q[hi + atomicAdd(cnt, 1)] = j;
       }
       __syncthreads();
-      na = s_count[ci ^ 1];
-      __syncthreads();
-      if (threadIdx.x == 0) s_count[ci] = 0;  // the list just consumed becomes the next one to fill
-      int32_t* tmp = cur;
-      cur = nxt;
-      nxt = tmp;
-      ci ^= 1;
-      __syncthreads();
+      const int added = *cnt;
+      if (threadIdx.x == 0) s_cnt[(lev + 2) % 3] = 0;
+      if (added == 0) break;
+      lo = hi;
+      hi += added;
+      ++lev;
     }
-    // flip the cluster, then this step's sums
-    int ups = 0, csize = 0, bond = 0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-      const bool in = (inc[i >> 5] >> (i & 31)) & 1u;
-      if (in) s[i] = (int8_t)(-s[i]);
-      csize += in;
+    // flip the cluster and sum the spins across its boundary (the cluster's
+    // sites only change, the boundary sites are only read)
+    int cut = 0;
+    for (int e = threadIdx.x; e < hi * z; e += blockDim.x) {
+      const int fi = e / z, k = e - fi * z;
+      const int site = q[fi];
+      const int j = __ldg(nbr + (size_t)site * z + k);
+      if (j >= 0 && mark[j] != stamp) cut += s[j];
+      if (k == 0) s[site] = (int8_t)(-ref);
     }
-    __syncthreads();
     if (sums) {
-      for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const int si = s[i];
-        ups += si > 0;
-        for (int k = 0; k < z; ++k) {  // each bond once, from its lower site
-          const int j = __ldg(nbr + (size_t)i * z + k);
-          if (j > i) bond += si * s[j];
-        }
-      }
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        bond += __shfl_down_sync(0xffffffffu, bond, o);
-        ups += __shfl_down_sync(0xffffffffu, ups, o);
-        csize += __shfl_down_sync(0xffffffffu, csize, o);
-      }
-      if (lane == 0) {
-        s_red[0][warp] = bond;
-        s_red[1][warp] = ups;
-        s_red[2][warp] = csize;
-      }
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        long long b = 0, u = 0, cs = 0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
-          b += s_red[0][w];
-          u += s_red[1][w];
-          cs += s_red[2][w];
-        }
-        double* out = sums + (size_t)t * kNumSums;
-        out[0] = (double)b;
-        out[1] = out[2] = out[3] = out[4] = out[5] = 0.0;
-        out[6] = (double)u;
-        out[7] = (double)cs;
-      }
-      __syncthreads();
+      for (int o = 16; o > 0; o >>= 1) cut += __shfl_down_sync(0xffffffffu, cut, o);
+      if (lane == 0 && cut) atomicAdd(&s_cut, cut);
+    }
+    __syncthreads();
+    if (sums && threadIdx.x == 0) {
+      // cut bonds change sign: bond sum -= 2 ref sum(boundary spins)
+      bond -= 2ll * ref * s_cut;
+      ups += ref > 0 ? -(long long)hi : (long long)hi;
+      s_cut = 0;  // read again only after the next step's first barrier
+      double* out = sums + (size_t)t * kNumSums;
+      out[0] = (double)bond;
+      out[1] = out[2] = out[3] = out[4] = out[5] = 0.0;
+      out[6] = (double)ups;
+      out[7] = (double)hi;
     }
   }
+  __syncthreads();
   for (int i = threadIdx.x; i < n; i += blockDim.x) spins[i] = s[i];
 }
 
 }  // namespace
 
-size_t ising_wolff_smem(int n) { return (size_t)((n + 31) / 32) * 4 + (size_t)n * 8 + (size_t)n; }
+size_t ising_wolff_smem(int n) { return (size_t)n * 9; }
 
 cudaError_t launch_ising_wolff(int8_t* spins, int n, int z, const int32_t* nbr, const uint8_t* occ,
                                unsigned long long thr, RngKey key, uint32_t n_steps, double* sums, cudaStream_t s) {
