@@ -173,23 +173,21 @@ __device__ __forceinline__ bool resolve_tie(uint32_t gid, int k, uint32_t s01, u
 // sites whose digit ties with the threshold digit (probability 1/256) are
 // queued per warp and resolved 32 at a time.  Otherwise the scalar
 // decide16 path runs in line.  Both give the decisions of "accept iff U < thr".
-template <int C, bool UNIFORM, bool MEASURE, bool UPDATE, int PROP>
-__global__ void __launch_bounds__(256, UNIFORM ? 4 : 2) ising_sc_kernel(const IsingScArgs a, const IsingTable tab, const RngKey key,
-                                                          long long* __restrict__ part) {
-  constexpr int Z = 6, W = 2 * Z + 1;
-  constexpr int kQ = 64;  // per-warp tie queue
-  __shared__ unsigned long long s_thr[2 * W];
-  __shared__ uint2 s_q[8][kQ];
-  pdl_launch_dependents();
-  for (int i = threadIdx.x; i < 2 * W; i += blockDim.x) s_thr[i] = tab.thr[i];
-  __syncthreads();
-  pdl_wait();
+constexpr int kScQueue = 64;  // per-warp tie queue
 
+// The 16-site groups base + lane for base in [first, end) step `step` (base
+// a multiple of 32 apart from `first`), adding the pass's sums to bond / ups
+// / nacc.  Every tie is resolved before returning.
+template <int C, bool UNIFORM, bool MEASURE, bool UPDATE, int PROP>
+__device__ __forceinline__ void sc1_range(const IsingScArgs& a, const IsingTable& tab, const RngKey& key,
+                                          const unsigned long long* s_thr, uint2 (*s_q)[kScQueue], uint32_t first,
+                                          uint32_t end, uint32_t step, int& bond, int& ups, int& nacc) {
+  constexpr int Z = 6, W = 2 * Z + 1;
+  constexpr int kQ = kScQueue;
   uint8_t* __restrict__ own = a.cls[C];
   const uint8_t* __restrict__ oth = a.cls[C ^ 1];
   const int zoff = Z - tab.zeff;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  int bond = 0, ups = 0, nacc = 0;
   int qn = 0;  // warp-uniform queue length
 
   // apply the first n queued ties (one per lane), then drop them
@@ -216,10 +214,9 @@ __global__ void __launch_bounds__(256, UNIFORM ? 4 : 2) ising_sc_kernel(const Is
     qn = rest;
   };
 
-  const uint32_t stride = gridDim.x * blockDim.x;
-  for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < a.groups; base += stride) {
+  for (uint32_t base = first; base < end; base += step) {
     const uint32_t gid = base + lane;
-    const bool active = gid < a.groups;
+    const bool active = gid < end;
     uint32_t tm = 0;  // sites of this group whose first digit tied
     uint32_t S[4] = {0, 0, 0, 0}, A[4] = {0, 0, 0, 0};
     if (active) {
@@ -380,6 +377,21 @@ __global__ void __launch_bounds__(256, UNIFORM ? 4 : 2) ising_sc_kernel(const Is
     }
   }
   if (UNIFORM && UPDATE && qn > 0) drain(qn);
+}
+
+template <int C, bool UNIFORM, bool MEASURE, bool UPDATE, int PROP>
+__global__ void __launch_bounds__(256, UNIFORM ? 4 : 2) ising_sc_kernel(const IsingScArgs a, const IsingTable tab, const RngKey key,
+                                                          long long* __restrict__ part) {
+  constexpr int W = 13;
+  __shared__ unsigned long long s_thr[2 * W];
+  __shared__ uint2 s_q[8][kScQueue];
+  pdl_launch_dependents();
+  for (int i = threadIdx.x; i < 2 * W; i += blockDim.x) s_thr[i] = tab.thr[i];
+  __syncthreads();
+  pdl_wait();
+  int bond = 0, ups = 0, nacc = 0;
+  sc1_range<C, UNIFORM, MEASURE, UPDATE, PROP>(a, tab, key, s_thr, s_q, blockIdx.x * blockDim.x + (threadIdx.x & ~31u),
+                                               a.groups, gridDim.x * blockDim.x, bond, ups, nacc);
   if (MEASURE) block_sum3_store(bond, ups, nacc, part + (size_t)blockIdx.x * kNumSums);
 }
 
@@ -390,7 +402,7 @@ __global__ void __launch_bounds__(256, UNIFORM ? 4 : 2) ising_sc_kernel(const Is
 // blocks, same tie resolution), so results are identical.  ALLPER: all axes
 // periodic, no missing rows.
 constexpr int kSc2MinBlocks = 3;  // 80 registers: the pair state stays in registers
-constexpr int kSc2Queue = 64;      // per-warp tie queue
+constexpr int kSc2Queue = kScQueue;  // per-warp tie queue
 
 // The pairs base + lane for base in [first, end) step `step` (base a
 // multiple of 32 apart from `first`), adding the pass's sums to bond / ups /
