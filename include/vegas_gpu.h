@@ -211,6 +211,25 @@ int vg_magnetization(vg_ctx* ctx, double m[3], double* magnitude);
 /* Total energy / |M| from raw sums with a context's Hamiltonian semantics. */
 int vg_energy_from_sums(const vg_ctx* ctx, const vg_sums* sums, double* energy, double* magnitude);
 
+/* Per-site energies of the current state: out[i] = Hamiltonian::energy(i)
+ * (src/energy.rs:45-52), the sum of the Hamiltonian's terms at site i as
+ * Compound::energy forms it (src/energy.rs:254-256): exchange
+ * -sum_j J_ij s_i.s_j over the site's neighbours (src/energy.rs:194-208),
+ * anisotropy K (s.e)^2 (:108-112), Zeeman |B| (s.b) with the reference's
+ * sign (:147-152), gauge g (:75-80), and -Kc (sx^4 + sy^4 + sz^4) for the
+ * cubic term.  Computed in FP64 on the device from the state as the context
+ * holds it; n = the number of sites. */
+int vg_site_energies(vg_ctx* ctx, double* out, int64_t n);
+
+/* Energy changes of single-site proposals (Heisenberg contexts):
+ * out[i] = energy of site i with its spin replaced by proposals[3i..3i+2],
+ * every other spin as it is, minus its current energy; the difference the
+ * Metropolis step accepts with probability min(1, exp(-dE / T))
+ * (src/integrator.rs:77-86).  Runs the
+ * sweeps' own energy-change function in the context's precision (FP32 or
+ * FP64), so FP32 rounding can be checked against FP64. */
+int vg_delta_energies(vg_ctx* ctx, const double* proposals, double* out, int64_t n);
+
 /* ------------------------------------------------------ batched replicas */
 /* Many independent Ising replicas (MetropolisFlipIntegrator,
  * src/integrator.rs:99-138, with Exchange only, h = 0) run at once: 32

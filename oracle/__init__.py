@@ -113,6 +113,9 @@ def lib():
         L.vo_ref_total_energy.argtypes = [C.c_int64, C.c_int32, P(C.c_int32), C.c_int32, P(C.c_int8),
                                           P(C.c_double), P(Hamiltonian), P(C.c_double), C.c_double]
         L.vo_ref_total_energy.restype = C.c_double
+        L.vo_ref_site_energies.argtypes = [C.c_int64, C.c_int32, P(C.c_int32), C.c_int32, P(C.c_int8),
+                                           P(C.c_double), P(Hamiltonian), P(C.c_double), C.c_double, P(C.c_double)]
+        L.vo_ref_site_energies.restype = None
         L.vo_ref_magnetization.argtypes = [C.c_int64, C.c_int32, P(C.c_int8), P(C.c_double)]
         L.vo_ref_magnetization.restype = C.c_double
         L.vo_ref_parallel.argtypes = [P(Lattice), C.c_int32, C.c_int32, P(Hamiltonian), C.c_double, C.c_double,
@@ -270,6 +273,21 @@ class Graph:
             sf = np.ascontiguousarray(spin, dtype=np.float64)
         return lib().vo_ref_total_energy(self.n, self.zmax, _p(self.nbr, C.c_int32), kind, _p(si, C.c_int8),
                                          _p(sf, C.c_double), C.byref(H), bb, bmag)
+
+
+    def ref_site_energies(self, kind, spin, H: Hamiltonian, b=(0.0, 0.0, 1.0), bmag=0.0):
+        """Hamiltonian::energy(i) of every site (src/energy.rs:45-52)."""
+        bb = (C.c_double * 3)(*b)
+        if kind == 0:
+            si = np.ascontiguousarray(spin, dtype=np.int8)
+            sf = np.zeros(3, dtype=np.float64)
+        else:
+            si = np.zeros(1, dtype=np.int8)
+            sf = np.ascontiguousarray(spin, dtype=np.float64)
+        out = np.zeros(max(self.n, 1))
+        lib().vo_ref_site_energies(self.n, self.zmax, _p(self.nbr, C.c_int32), kind, _p(si, C.c_int8),
+                                   _p(sf, C.c_double), C.byref(H), bb, bmag, _p(out, C.c_double))
+        return out[:self.n]
 
 
 class MscBatch:

@@ -724,6 +724,16 @@ double vo_ref_total_energy(int64_t n, int32_t zmax, const int32_t* nbr, int32_t 
   return e;
 }
 
+/* Hamiltonian::energy(i) of every site (src/energy.rs:45-52; Compound sums
+ * the terms' site energies, src/energy.rs:254-256). */
+void vo_ref_site_energies(int64_t n, int32_t zmax, const int32_t* nbr, int32_t kind, const int8_t* si,
+                          const double* sf, const vo_hamiltonian* H, const double b[3], double bmag, double* out) {
+  csr_t X = build_csr(n, zmax, nbr, H->J);
+  ref_ctx R = {kind, &X, H, {b[0], b[1], b[2]}, fabs(bmag)};
+  for (int64_t i = 0; i < n; ++i) out[i] = site_energy(&R, si, sf, i);
+  free_csr(&X);
+}
+
 /* MetropolisFlipIntegrator / MetropolisIntegrator::step
  * (src/integrator.rs:66-92, :113-137) followed by the instruments. */
 int vo_ref_sweeps(int64_t n, int32_t zmax, const int32_t* nbr, int32_t kind, int32_t proposal,

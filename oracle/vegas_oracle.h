@@ -161,6 +161,10 @@ double vo_ref_total_energy(int64_t n, int32_t zmax, const int32_t* nbr, int32_t 
                            const int8_t* spin_i8, const double* spin_f64, const vo_hamiltonian* H,
                            const double b[3], double bmag);
 double vo_ref_magnetization(int64_t n, int32_t spin_kind, const int8_t* spin_i8, const double* spin_f64);
+/* Hamiltonian::energy(i) of every site, the reference's per-site semantics. */
+void vo_ref_site_energies(int64_t n, int32_t zmax, const int32_t* nbr, int32_t spin_kind, const int8_t* spin_i8,
+                          const double* spin_f64, const vo_hamiltonian* H, const double b[3], double bmag,
+                          double* out);
 
 /* Independent reference chains on nthreads host threads (one lattice each),
  * for the multi-core CPU baseline.  Returns total attempted flips; *seconds

@@ -62,9 +62,13 @@ struct vg_ctx {
   double* h_pin = nullptr;  // pinned readback
   size_t h_pin_cap = 0;
   int64_t device_bytes = 0;
-  int32_t* d_wnbr = nullptr;             // Wolff: natural-order neighbour table [n][z]
+  int32_t* d_wnbr = nullptr;             // natural-order neighbour table [n][z] (Wolff, site energies)
   uint8_t* d_wocc = nullptr;             // Wolff: occurrence of each bond among repeated ones
   bool bonds = false;                    // per-bond exchange constants set (generic path)
+  std::vector<double> bonds_nat;         // those constants in neighbour-table layout [n][z]
+  double* d_jnat = nullptr;              // device copy of bonds_nat (uploaded on first use)
+  double* d_eaux = nullptr;              // site-energy buffers: proposals [n][3] + results [n]
+  size_t eaux_cap = 0;                   // doubles
   double* d_jb[kMaxColours] = {};        // [z][n_c] per class, FP64
   float* d_jbf[kMaxColours] = {};        // the same in FP32 (FP32 Heisenberg kernels)
   std::string err;
@@ -797,6 +801,8 @@ void destroy(vg_ctx* c) {
   if (c->d_stage) cudaFree(c->d_stage);
   if (c->d_wnbr) cudaFree(c->d_wnbr);
   if (c->d_wocc) cudaFree(c->d_wocc);
+  if (c->d_jnat) cudaFree(c->d_jnat);
+  if (c->d_eaux) cudaFree(c->d_eaux);
   if (c->d_part) cudaFree(c->d_part);
   if (c->d_sums) cudaFree(c->d_sums);
   if (c->d_flag) cudaFree(c->d_flag);
@@ -1141,10 +1147,12 @@ int vg_set_state(vg_ctx* c, const void* host, int64_t n) {
   return VG_OK;
 }
 
-int vg_get_state(vg_ctx* c, void* host, int64_t n) {
-  if (!c || !host) return fail(c, VG_ERR_INVALID_ARG, "NULL argument");
-  if (n != c->n) return fail(c, VG_ERR_INVALID_ARG, "state length does not match the lattice");
-  VG_CUDA(c, cudaSetDevice(c->device));
+namespace {
+
+// The state in natural site order into d_stage (int8 +-1, or [n][3]
+// doubles), enqueued on the context's stream.
+int export_natural(vg_ctx* c) {
+  const int64_t n = c->n;
   const size_t bytes = is_ising(c) ? (size_t)n : (size_t)n * 3 * sizeof(double);
   int rc = ensure_stage(c, bytes);
   if (rc) return rc;
@@ -1171,6 +1179,18 @@ int vg_get_state(vg_ctx* c, void* host, int64_t n) {
     heis_export<float><<<copy_grid(c, n), 256, 0, c->stream>>>((double*)c->d_stage, n, structured, m, P);
   }
   VG_CUDA(c, cudaGetLastError());
+  return VG_OK;
+}
+
+}  // namespace
+
+int vg_get_state(vg_ctx* c, void* host, int64_t n) {
+  if (!c || !host) return fail(c, VG_ERR_INVALID_ARG, "NULL argument");
+  if (n != c->n) return fail(c, VG_ERR_INVALID_ARG, "state length does not match the lattice");
+  VG_CUDA(c, cudaSetDevice(c->device));
+  const size_t bytes = is_ising(c) ? (size_t)n : (size_t)n * 3 * sizeof(double);
+  int rc = export_natural(c);
+  if (rc) return rc;
   VG_CUDA(c, cudaMemcpyAsync(host, c->d_stage, bytes, cudaMemcpyDeviceToHost, c->stream));
   VG_CUDA(c, cudaStreamSynchronize(c->stream));
   return VG_OK;
@@ -1335,6 +1355,35 @@ int vg_energy_from_sums(const vg_ctx* c, const vg_sums* s, double* e, double* ma
   return VG_OK;
 }
 
+namespace {
+
+// The neighbour table in natural site order and each bond's occurrence among
+// repeated bonds of one pair, built on first use.
+int ensure_natural_nbr(vg_ctx* c) {
+  if (c->d_wnbr) return VG_OK;
+  Geometry g;
+  std::string why;
+  int rc;
+  if ((rc = geometry_init(&c->lat, &g, &why))) return fail(c, rc, why);
+  std::vector<int32_t> nbr;
+  build_neighbours(g, nbr);
+  std::vector<uint8_t> occ(nbr.size(), 0);
+  for (int64_t i = 0; i < c->n; ++i)
+    for (int k = 0; k < c->z; ++k) {
+      const int32_t t = nbr[(size_t)i * c->z + k];
+      uint8_t o = 0;
+      for (int q = 0; q < k; ++q) o += nbr[(size_t)i * c->z + q] == t;
+      occ[(size_t)i * c->z + k] = o;
+    }
+  if ((rc = dalloc(c, (void**)&c->d_wnbr, sizeof(int32_t) * nbr.size()))) return rc;
+  if ((rc = dalloc(c, (void**)&c->d_wocc, occ.size()))) return rc;
+  VG_CUDA(c, cudaMemcpy(c->d_wnbr, nbr.data(), sizeof(int32_t) * nbr.size(), cudaMemcpyHostToDevice));
+  VG_CUDA(c, cudaMemcpy(c->d_wocc, occ.data(), occ.size(), cudaMemcpyHostToDevice));
+  return VG_OK;
+}
+
+}  // namespace
+
 int vg_wolff_steps(vg_ctx* c, uint64_t n, int32_t measure, double* E, double* M) {
   if (!c) return VG_ERR_INVALID_ARG;
   if (!is_ising(c)) return fail(c, VG_ERR_UNSUPPORTED, "Wolff steps need an Ising context");
@@ -1343,25 +1392,7 @@ int vg_wolff_steps(vg_ctx* c, uint64_t n, int32_t measure, double* E, double* M)
   if (c->bonds) return fail(c, VG_ERR_UNSUPPORTED, "Wolff steps use the uniform exchange constant");
   VG_CUDA(c, cudaSetDevice(c->device));
   int rc;
-  if (!c->d_wnbr) {  // neighbour table and bond occurrences, natural site order
-    Geometry g;
-    std::string why;
-    if ((rc = geometry_init(&c->lat, &g, &why))) return fail(c, rc, why);
-    std::vector<int32_t> nbr;
-    build_neighbours(g, nbr);
-    std::vector<uint8_t> occ(nbr.size(), 0);
-    for (int64_t i = 0; i < c->n; ++i)
-      for (int k = 0; k < c->z; ++k) {
-        const int32_t t = nbr[(size_t)i * c->z + k];
-        uint8_t o = 0;
-        for (int q = 0; q < k; ++q) o += nbr[(size_t)i * c->z + q] == t;
-        occ[(size_t)i * c->z + k] = o;
-      }
-    if ((rc = dalloc(c, (void**)&c->d_wnbr, sizeof(int32_t) * nbr.size()))) return rc;
-    if ((rc = dalloc(c, (void**)&c->d_wocc, occ.size()))) return rc;
-    VG_CUDA(c, cudaMemcpy(c->d_wnbr, nbr.data(), sizeof(int32_t) * nbr.size(), cudaMemcpyHostToDevice));
-    VG_CUDA(c, cudaMemcpy(c->d_wocc, occ.data(), occ.size(), cudaMemcpyHostToDevice));
-  }
+  if ((rc = ensure_natural_nbr(c))) return rc;
   // bond probability 1 - exp(-2 J / T) as a threshold on a 32-bit word (src/integrator.rs:199-203)
   const double J = c->ham.has_exchange ? c->ham.exchange : 0.0;
   const double T = clamp_temperature(c->T);
@@ -1409,6 +1440,12 @@ int vg_set_exchange_bonds(vg_ctx* c, const double* J, int64_t n_entries) {
   if (!c) return VG_ERR_INVALID_ARG;
   VG_CUDA(c, cudaSetDevice(c->device));
   VG_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (c->d_jnat) {  // stale natural-order copy
+    cudaFree(c->d_jnat);
+    c->device_bytes -= (int64_t)(sizeof(double) * c->bonds_nat.size());
+    c->d_jnat = nullptr;
+  }
+  c->bonds_nat.clear();
   if (!J) {  // back to the uniform constant
     for (int k = 0; k < kMaxColours; ++k) {
       if (c->d_jb[k]) cudaFree(c->d_jb[k]);
@@ -1465,8 +1502,93 @@ int vg_set_exchange_bonds(vg_ctx* c, const double* J, int64_t n_entries) {
     VG_CUDA(c, cudaMemcpy(c->d_jb[k], ell.data(), sizeof(double) * ell.size(), cudaMemcpyHostToDevice));
     VG_CUDA(c, cudaMemcpy(c->d_jbf[k], ellf.data(), sizeof(float) * ellf.size(), cudaMemcpyHostToDevice));
   }
+  c->bonds_nat.assign(J, J + (size_t)c->n * c->z);
+  for (size_t e = 0; e < nbr.size(); ++e)
+    if (nbr[e] < 0) c->bonds_nat[e] = 0.0;
   c->bonds = true;
   return VG_OK;
+}
+
+namespace {
+
+// Natural-order state, neighbour table, bond constants and an auxiliary
+// buffer of `aux` doubles for the energy entry points.
+int energy_setup(vg_ctx* c, size_t aux) {
+  int rc;
+  VG_CUDA(c, cudaSetDevice(c->device));
+  if ((rc = ensure_natural_nbr(c))) return rc;
+  if (c->bonds && !c->d_jnat) {
+    if ((rc = dalloc(c, (void**)&c->d_jnat, sizeof(double) * c->bonds_nat.size()))) return rc;
+    VG_CUDA(c, cudaMemcpy(c->d_jnat, c->bonds_nat.data(), sizeof(double) * c->bonds_nat.size(),
+                          cudaMemcpyHostToDevice));
+  }
+  if (aux > c->eaux_cap) {
+    if (c->d_eaux) {
+      cudaFree(c->d_eaux);
+      c->device_bytes -= (int64_t)(sizeof(double) * c->eaux_cap);
+      c->d_eaux = nullptr;
+      c->eaux_cap = 0;
+    }
+    if ((rc = dalloc(c, (void**)&c->d_eaux, sizeof(double) * aux))) return rc;
+    c->eaux_cap = aux;
+  }
+  return export_natural(c);
+}
+
+SiteTerms site_terms(const vg_ctx* c) {
+  const vg_hamiltonian_desc& h = c->ham;
+  SiteTerms t;
+  t.has_exchange = h.has_exchange;
+  t.has_anisotropy = h.has_anisotropy;
+  t.has_zeeman = h.has_zeeman;
+  t.has_gauge = h.has_gauge;
+  t.has_cubic = h.has_cubic;
+  t.J = h.exchange;
+  t.K = h.anisotropy;
+  for (int a = 0; a < 3; ++a) {
+    t.axis[a] = h.anisotropy_axis[a];
+    t.b[a] = c->bhat[a];
+  }
+  t.hz = zeeman_coef(c);
+  t.gauge = h.gauge;
+  t.Kc = h.cubic;
+  t.axis_sign = h.anisotropy_axis[2] >= 0.0 ? 1.0 : -1.0;
+  t.field_sign = c->bhat[2] >= 0.0 ? 1.0 : -1.0;
+  return t;
+}
+
+}  // namespace
+
+int vg_site_energies(vg_ctx* c, double* out, int64_t n) {
+  if (!c || !out) return fail(c, VG_ERR_INVALID_ARG, "NULL argument");
+  if (n != c->n) return fail(c, VG_ERR_INVALID_ARG, "output length does not match the lattice");
+  int rc;
+  if ((rc = energy_setup(c, (size_t)n))) return rc;
+  const cudaError_t e = launch_site_energies(is_ising(c), c->d_stage, n, c->z, c->d_wnbr, c->bonds ? c->d_jnat : nullptr,
+                                             site_terms(c), c->d_eaux, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "site energy launch");
+  VG_CUDA(c, cudaMemcpyAsync(out, c->d_eaux, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+  return sync_stream(c);
+}
+
+int vg_delta_energies(vg_ctx* c, const double* proposals, double* out, int64_t n) {
+  if (!c || !proposals || !out) return fail(c, VG_ERR_INVALID_ARG, "NULL argument");
+  if (is_ising(c)) return fail(c, VG_ERR_UNSUPPORTED, "energy changes of proposals are computed for Heisenberg spins");
+  if (n != c->n) return fail(c, VG_ERR_INVALID_ARG, "proposal length does not match the lattice");
+  int rc;
+  if ((rc = energy_setup(c, (size_t)n * 4))) return rc;
+  double* d_prop = c->d_eaux;
+  double* d_out = c->d_eaux + (size_t)n * 3;
+  VG_CUDA(c, cudaMemcpyAsync(d_prop, proposals, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+  const double* jn = c->bonds ? c->d_jnat : nullptr;
+  const cudaError_t e =
+      fp64(c) ? launch_heis_delta<double>((const double*)c->d_stage, d_prop, n, c->z, c->d_wnbr, jn,
+                                          heis_params<double>(c), d_out, c->stream)
+              : launch_heis_delta<float>((const double*)c->d_stage, d_prop, n, c->z, c->d_wnbr, jn,
+                                         heis_params<float>(c), d_out, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "energy change launch");
+  VG_CUDA(c, cudaMemcpyAsync(out, d_out, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+  return sync_stream(c);
 }
 
 int vg_lattice_neighbours(const vg_lattice_desc* lat, int32_t* nbr, int64_t cap, int64_t* n_sites, int32_t* zmax) {

@@ -64,6 +64,22 @@ __device__ __forceinline__ R quart(const V3<R>& s) {
   return a * a + b * b + c * c;
 }
 
+// Energy change of replacing spin s by p at a site whose neighbour field
+// (sum of J_ij s_j, or of s_j with P.J the uniform constant) is h: the
+// difference of the site's Compound energy (src/energy.rs:108-112, 147-152,
+// 194-208) plus the cubic term -Kc (sx^4 + sy^4 + sz^4).
+template <typename R>
+__device__ __forceinline__ R heis_delta_e(const V3<R>& s, const V3<R>& p, const V3<R>& h, const HeisParams<R>& P) {
+  const R dx = p.x - s.x, dy = p.y - s.y, dz = p.z - s.z;
+  const R pe = p.x * P.ax + p.y * P.ay + p.z * P.az;
+  const R se = s.x * P.ax + s.y * P.ay + s.z * P.az;
+  R de = -P.J * (dx * h.x + dy * h.y + dz * h.z);
+  de += P.K * (pe * pe - se * se);
+  de += P.hz * (dx * P.bx + dy * P.by + dz * P.bz);
+  de -= P.Kc * (quart(p) - quart(s));
+  return de;
+}
+
 // Proposal and acceptance draw of one site; returns the new spin and whether
 // it was accepted.
 template <typename R, int PROP>
@@ -85,13 +101,7 @@ __device__ __forceinline__ bool heis_update(const V3<R>& s, const V3<R>& h, cons
     p.y = -s.y;
     p.z = -s.z;
   }
-  const R dx = p.x - s.x, dy = p.y - s.y, dz = p.z - s.z;
-  const R pe = p.x * P.ax + p.y * P.ay + p.z * P.az;
-  const R se = s.x * P.ax + s.y * P.ay + s.z * P.az;
-  R de = -P.J * (dx * h.x + dy * h.y + dz * h.z);
-  de += P.K * (pe * pe - se * se);
-  de += P.hz * (dx * P.bx + dy * P.by + dz * P.bz);
-  de -= P.Kc * (quart(p) - quart(s));
+  const R de = heis_delta_e<R>(s, p, h, P);
   const R u = draw_u<R>(w);
   const bool acc = de <= (R)0 || u < exp_(-de * P.beta);
   out = acc ? p : s;

@@ -169,6 +169,19 @@ int ising_sc_blocks_per_sm(const IsingScArgs& a, const IsingTable& tab, int tpb)
 size_t ising_wolff_smem(int n);
 cudaError_t launch_ising_wolff(int8_t* spins, int n, int z, const int32_t* nbr, const uint8_t* occ,
                                unsigned long long thr, RngKey key, uint32_t n_steps, double* sums, cudaStream_t s);
+// Per-site energies and single-site energy changes on natural-order copies
+// of the state (int8 +-1, or [n][3] doubles); jnat (may be null): per-bond
+// constants in neighbour-table layout [n][z].
+struct SiteTerms {
+  int has_exchange, has_anisotropy, has_zeeman, has_gauge, has_cubic;
+  double J, K, axis[3], hz, b[3], gauge, Kc;
+  double axis_sign, field_sign;  // Ising: the z signs of the axis and the field
+};
+cudaError_t launch_site_energies(bool ising, const void* spins, int64_t n, int z, const int32_t* nbr,
+                                 const double* jnat, const SiteTerms& t, double* out, cudaStream_t s);
+template <typename R>
+cudaError_t launch_heis_delta(const double* spins, const double* prop, int64_t n, int z, const int32_t* nbr,
+                              const double* jnat, const HeisParams<R>& P, double* out, cudaStream_t s);
 size_t ising_resident_smem(const IsingScArgs& a);
 cudaError_t launch_ising_resident(const IsingScArgs& a, const IsingTable& tab, RngKey key, int proposal,
                                   uint32_t n_sweeps, double* sums, int tpb, cudaStream_t s);

@@ -320,6 +320,23 @@ class Engine:
         _check(lib().vg_total_energy(self._h, C.byref(e)), self._h)
         return e.value
 
+    def site_energies(self) -> np.ndarray:
+        """Hamiltonian::energy(i) for every site of the current state (FP64)."""
+        n = self.lattice.n_sites
+        out = np.zeros(max(n, 1))
+        _check(lib().vg_site_energies(self._h, out.ctypes.data_as(C.POINTER(C.c_double)), n), self._h)
+        return out[:n]
+
+    def delta_energies(self, proposals: np.ndarray) -> np.ndarray:
+        """Energy change of replacing each site's spin by proposals[i] (n x 3),
+        the others fixed, in the context's precision (Heisenberg)."""
+        n = self.lattice.n_sites
+        p = np.ascontiguousarray(proposals, dtype=np.float64).reshape(n, 3)
+        out = np.zeros(max(n, 1))
+        _check(lib().vg_delta_energies(self._h, p.ctypes.data_as(C.POINTER(C.c_double)),
+                                       out.ctypes.data_as(C.POINTER(C.c_double)), n), self._h)
+        return out[:n]
+
     def magnetization(self):
         m = (C.c_double * 3)()
         mag = C.c_double()

@@ -152,6 +152,8 @@ SIGNATURES = {
                                              C.c_void_p, C.c_void_p]),
     "vg_wolff_steps": (C.c_int, [C.c_void_p, C.c_uint64, C.c_int32, P(C.c_double), P(C.c_double)]),
     "vg_set_exchange_bonds": (C.c_int, [C.c_void_p, P(C.c_double), C.c_int64]),
+    "vg_site_energies": (C.c_int, [C.c_void_p, P(C.c_double), C.c_int64]),
+    "vg_delta_energies": (C.c_int, [C.c_void_p, P(C.c_double), P(C.c_double), C.c_int64]),
     "vg_lattice_neighbours": (C.c_int, [P(LatticeDesc), P(C.c_int32), C.c_int64, P(C.c_int64), P(C.c_int32)]),
     "vg_lattice_colouring": (C.c_int, [P(LatticeDesc), P(C.c_int32), C.c_int64, P(C.c_int32)]),
     "vg_host_alloc": (C.c_int, [P(C.c_void_p), C.c_uint64]),
