@@ -133,18 +133,27 @@ struct WordState {
   uint32_t acc;     // lanes accepted so far
 };
 
+// Threshold plane k of every drawing category for the lanes in its mask
+// (s_tab: the block's table plane-major, one uint4 of categories per plane).
+template <int ND>
+__device__ __forceinline__ uint32_t msc_plane(const WordState<ND>& w, const uint4* s_tab, int k) {
+  const uint4 t = s_tab[k];  // one shared-memory load for all categories
+  uint32_t T = w.m[0] & t.x;
+  if (ND > 1) T |= w.m[1] & t.y;
+  if (ND > 2) T |= w.m[2] & t.z;
+  if (ND > 3) T |= w.m[3] & t.w;
+  return T;
+}
+
 // Planes 4*blkno .. 4*blkno+3 of word j.
 template <int C, int ND>
 __device__ __forceinline__ void msc_block(WordState<ND>& w, uint32_t j, uint32_t sweep, uint32_t word_id,
-                                          int blkno, const uint32_t* s_tab, const KeySchedule& ks) {
+                                          int blkno, const uint4* s_tab, const KeySchedule& ks) {
   const uint4 bk = philox_ks(make_uint4(j, sweep, (kTagMsc << 24) | ((uint32_t)C << 8) | (uint32_t)blkno, word_id), ks);
   const uint32_t R[4] = {bk.x, bk.y, bk.z, bk.w};
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
-    const int k = 4 * blkno + i;
-    uint32_t T = 0;
-#pragma unroll
-    for (int q = 0; q < ND; ++q) T |= w.m[q] & s_tab[q * 33 + k];
+    const uint32_t T = msc_plane<ND>(w, s_tab, 4 * blkno + i);
     w.acc |= w.und & ~R[i] & T;
     w.und &= ~(R[i] ^ T);
   }
@@ -155,7 +164,7 @@ __device__ __forceinline__ void msc_block(WordState<ND>& w, uint32_t j, uint32_t
 // n < ZZ/2 for J > 0, n > ZZ/2 for J < 0 (none for J = 0).
 template <int C, int ZZ>
 __device__ __forceinline__ WordState<ZZ / 2> msc_word_start(const MscSeg& sg, uint32_t j, uint32_t s,
-                                                            const uint32_t* oth, const uint32_t* s_tab,
+                                                            const uint32_t* oth, const uint4* s_tab,
                                                             uint32_t sweep, const KeySchedule& ks, int jsign) {
   constexpr int ND = ZZ / 2;
   WordState<ND> w;
@@ -164,14 +173,14 @@ __device__ __forceinline__ WordState<ZZ / 2> msc_word_start(const MscSeg& sg, ui
   uint32_t b0, b1, b2;
   if (ZZ == 6) count6(a[0], a[1], a[2], a[3], a[4], a[5], b0, b1, b2);
   else count4(a[0], a[1], a[2], a[3], b0, b1, b2);
-  uint32_t draw = 0, alw = 0;
+  uint32_t draw = 0;
 #pragma unroll
   for (int q = 0; q < ND; ++q) {
     const int n = jsign > 0 ? q : ZZ / 2 + 1 + q;
     w.m[q] = jsign == 0 ? 0u : lanes_equal(b0, b1, b2, n);
     draw |= w.m[q];
-    alw |= w.m[q] & s_tab[q * 33 + 32];
   }
+  const uint32_t alw = msc_plane<ND>(w, s_tab, 32);
   w.acc = ~draw | alw;
   w.und = draw & ~alw;
   msc_block<C, ND>(w, j, sweep, sg.word_id, 0, s_tab, ks);
@@ -192,7 +201,7 @@ constexpr int kQueueWords = 4 + 3;  // j, s, und, acc, m[<= 3]
 
 template <int C, int ZZ, int TPB, int WPT, int WIF>
 __device__ __forceinline__ void msc_pass_body(const MscSeg& sg, uint32_t j0, uint32_t* own, const uint32_t* oth,
-                                              const uint32_t* s_tab, uint32_t sweep, const KeySchedule& ks,
+                                              const uint4* s_tab, uint32_t sweep, const KeySchedule& ks,
                                               int jsign, uint32_t (*s_q)[kQueue][kQueueWords]) {
   constexpr int ND = ZZ / 2;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -264,7 +273,7 @@ template <int C, int TPB, int WPT, int WIF>
 __global__ void __launch_bounds__(TPB) msc_pass(const MscSeg* __restrict__ segs, const int2* __restrict__ blocks,
                                                 const uint32_t* __restrict__ tabs, const MscDev* __restrict__ dev,
                                                 uint32_t t_off, KeySchedule ks, int jsign) {
-  __shared__ uint32_t s_tab[kTabWords];
+  __shared__ uint4 s_tab[33];  // plane k: the 4 categories' threshold words
   __shared__ uint32_t s_q[TPB / 32][kQueue][kQueueWords];
   pdl_launch_dependents();
   const int2 bl = blocks[blockIdx.x];
@@ -272,7 +281,8 @@ __global__ void __launch_bounds__(TPB) msc_pass(const MscSeg* __restrict__ segs,
   // Tables and counters change only in the exchange / advance kernels, which
   // complete before any pass of the next round starts; spins are read after
   // the wait for the previous pass.
-  for (int i = threadIdx.x; i < kTabWords; i += blockDim.x) s_tab[i] = tabs[(size_t)bl.x * kTabWords + i];
+  for (int i = threadIdx.x; i < kTabWords; i += blockDim.x)  // category-major in memory, plane-major here
+    reinterpret_cast<uint32_t*>(s_tab)[(i % 33) * 4 + i / 33] = tabs[(size_t)bl.x * kTabWords + i];
   const uint32_t sweep = dev->sweep0 + t_off;
   __syncthreads();
   pdl_wait();

@@ -191,6 +191,16 @@ static void gpu_checks(const std::string& dir) {
     double worst = 0.0;
     for (const auto& v : s.spins()) worst = std::max(worst, std::fabs(std::sqrt(v.dot(v)) - 1.0));
     CHECK(worst < 1e-6);
+    // Hamiltonian::energy per site: the Compound total is their sum
+    const std::vector<double> e = m.site_energies();
+    CHECK(e.size() == l.sites_len());
+    double sum = 0.0, mag = 0.0;
+    for (double v : e) {
+      sum += v;
+      mag += std::fabs(v);
+    }
+    CHECK(std::fabs(sum - m.total_energy()) <= 1e-6 * std::max(1.0, mag));
+    CHECK(m.energy(5) == e[5]);
   }
   // Program errors surface before any device work
   {

@@ -111,6 +111,24 @@ class Machine {
   }
   vg_ctx* context() const { return ctx_; }
 
+  // Hamiltonian::energy(thermostat, state, i) of every site of the current
+  // state (src/energy.rs:45-52), and Hamiltonian::total_energy
+  // (src/energy.rs:55-59 with each term's own total), on the device.
+  std::vector<double> site_energies() const {
+    std::vector<double> e(n_);
+    check(vg_site_energies(ctx_, e.data(), (int64_t)n_), ctx_);
+    return e;
+  }
+  double energy(size_t index) const {
+    if (index >= n_) throw VegasError("site index out of range");
+    return site_energies()[index];
+  }
+  double total_energy() const {
+    double e = 0.0;
+    check(vg_total_energy(ctx_, &e), ctx_);
+    return e;
+  }
+
  private:
   void push_thermostat() {
     const auto b = thermostat_.field().b_hat();
