@@ -186,8 +186,11 @@ int vg_time_passes(vg_ctx* ctx, uint64_t n, int32_t measure, double* mean_pass_m
  * (the Hamiltonian's exchange constant J, the thermostat's T; the field is
  * not used, as in the reference) and flips it.  Per step, E and |M| as
  * vg_sweeps; vg_sums.accepted of vg_current_sums-style rows is the cluster
- * size.  A step advances the context's sweep index by one.  Lattices of at
- * most 16384 sites (one thread block). */
+ * size.  A step advances the context's sweep index by one.  Lattices of up
+ * to 16384 sites run in one thread block's shared memory; larger ones in one
+ * cooperative launch over the whole grid (a grid barrier per breadth-first
+ * level; VG_ERR_TIMEOUT if one ever waits more than 2 s).  The uniform
+ * exchange constant only (no per-bond constants). */
 int vg_wolff_steps(vg_ctx* ctx, uint64_t n_steps, int32_t measure, double* E, double* M);
 
 /* Per-bond exchange constants: Exchange's CSR with arbitrary J_ij

@@ -36,6 +36,38 @@ def test_wolff_steps_bit_exact(V, O, cell, ext, pbc, T):
         assert eng.info().sweep_index == n
 
 
+# beyond one block's shared memory (16,384 sites): the multi-block kernel
+GRID_CASES = [
+    ("sc", (32, 32, 32), (1, 1, 1)),
+    ("sc", (256, 256, 1), (1, 1, 0)),
+    ("sc", (64, 2, 256), (1, 1, 1)),   # repeated bonds along y
+    ("bcc", (24, 24, 24), (1, 1, 1)),
+    ("fcc", (18, 18, 18), (1, 0, 1)),
+]
+
+
+@pytest.mark.parametrize("cell,ext,pbc", GRID_CASES)
+@pytest.mark.parametrize("T", [8.0, 4.5, 2.0])
+def test_wolff_grid_steps_bit_exact(V, O, cell, ext, pbc, T):
+    seed, J, n = 9, 1.0, 60
+    lat = getattr(V.Lattice, cell)(*ext, pbc=tuple(bool(p) for p in pbc))
+    assert lat.n_sites > 16384
+    g = O.Graph(O.lattice(cell, *ext, pbc))
+    with V.Engine(lat, V.hamiltonian(V.Exchange(J)), seed=seed) as eng:
+        eng.init_random()
+        s0 = eng.get_state()
+        eng.set_thermostat(T)
+        E, M = eng.wolff_steps(n)
+        ref, obs = g.wolff_steps(s0, J, T, seed, 0, n)
+        assert np.array_equal(eng.get_state(), ref)
+        np.testing.assert_array_equal(E, -J * obs[:, 0])
+        np.testing.assert_array_equal(M, np.abs(obs[:, 1]))
+        # unmeasured steps continue the same stream
+        eng.wolff_steps(5, measure=False)
+        ref2, _ = g.wolff_steps(ref, J, T, seed, n, 5)
+        assert np.array_equal(eng.get_state(), ref2)
+
+
 def test_wolff_then_metropolis_continue_one_stream(V, O):
     """Wolff steps and Metropolis sweeps share the context's counter."""
     lat = V.Lattice.sc(10, 10, 10)
@@ -80,10 +112,12 @@ def test_wolff_rejections(V):
         with pytest.raises(V.VegasGpuError) as e:
             eng.wolff_steps(1)
         assert e.value.status == 5
-    with V.Engine(V.Lattice.sc(32, 32, 32), V.hamiltonian(V.Exchange(1.0)), seed=1) as eng:
+    lat = V.Lattice.bcc(4, 4, 4)
+    with V.Engine(lat, V.hamiltonian(V.Exchange(1.0)), seed=1, path=V.PATH_GENERIC) as eng:
+        eng.set_exchange_bonds(np.ones((lat.n_sites, 8)))
         with pytest.raises(V.VegasGpuError) as e:
             eng.wolff_steps(1)
-        assert "16384" in str(e.value)
+        assert e.value.status == 5 and "uniform exchange" in str(e.value)
 
 
 def test_cli_runs_the_wolff_input(tmp_path):

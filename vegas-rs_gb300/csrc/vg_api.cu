@@ -64,6 +64,9 @@ struct vg_ctx {
   int64_t device_bytes = 0;
   int32_t* d_wnbr = nullptr;             // natural-order neighbour table [n][z] (Wolff, site energies)
   uint8_t* d_wocc = nullptr;             // Wolff: occurrence of each bond among repeated ones
+  uint32_t* d_wmark = nullptr;           // Wolff, multi-block: per-site step stamps [n]
+  int32_t* d_wq = nullptr;               // Wolff, multi-block: the cluster queue [n]
+  WolffGrid* d_wgrid = nullptr;          // Wolff, multi-block: counters and grid barrier
   bool bonds = false;                    // per-bond exchange constants set (generic path)
   std::vector<double> bonds_nat;         // those constants in neighbour-table layout [n][z]
   double* d_jnat = nullptr;              // device copy of bonds_nat (uploaded on first use)
@@ -373,7 +376,7 @@ bool sc_layout(const vg_ctx* c) { return c->path == VG_PATH_STRUCTURED || c->pat
 bool fp64(const vg_ctx* c) { return c->opt.precision == VG_FP64; }
 size_t real_size(const vg_ctx* c) { return fp64(c) ? 8 : 4; }
 
-constexpr int64_t kWolffMaxSites = 16384;  // one block's shared memory holds the Wolff state
+constexpr int64_t kWolffMaxSites = 16384;  // up to here one block's shared memory holds the Wolff state
 
 int dalloc(vg_ctx* c, void** p, size_t bytes) {
   if (bytes == 0) bytes = 16;
@@ -801,6 +804,9 @@ void destroy(vg_ctx* c) {
   if (c->d_stage) cudaFree(c->d_stage);
   if (c->d_wnbr) cudaFree(c->d_wnbr);
   if (c->d_wocc) cudaFree(c->d_wocc);
+  if (c->d_wmark) cudaFree(c->d_wmark);
+  if (c->d_wq) cudaFree(c->d_wq);
+  if (c->d_wgrid) cudaFree(c->d_wgrid);
   if (c->d_jnat) cudaFree(c->d_jnat);
   if (c->d_eaux) cudaFree(c->d_eaux);
   if (c->d_part) cudaFree(c->d_part);
@@ -1387,12 +1393,18 @@ int ensure_natural_nbr(vg_ctx* c) {
 int vg_wolff_steps(vg_ctx* c, uint64_t n, int32_t measure, double* E, double* M) {
   if (!c) return VG_ERR_INVALID_ARG;
   if (!is_ising(c)) return fail(c, VG_ERR_UNSUPPORTED, "Wolff steps need an Ising context");
-  if (c->n > kWolffMaxSites)
-    return fail(c, VG_ERR_UNSUPPORTED, "Wolff steps run in one thread block: at most 16384 sites");
+  if (c->n * (int64_t)c->z >= (int64_t)INT32_MAX)
+    return fail(c, VG_ERR_UNSUPPORTED, "Wolff steps index bonds with 32-bit integers: n_sites x z < 2^31");
   if (c->bonds) return fail(c, VG_ERR_UNSUPPORTED, "Wolff steps use the uniform exchange constant");
   VG_CUDA(c, cudaSetDevice(c->device));
   int rc;
   if ((rc = ensure_natural_nbr(c))) return rc;
+  const bool grid = c->n > kWolffMaxSites;
+  if (grid && !c->d_wgrid) {
+    if ((rc = dalloc(c, (void**)&c->d_wmark, sizeof(uint32_t) * (size_t)c->n))) return rc;
+    if ((rc = dalloc(c, (void**)&c->d_wq, sizeof(int32_t) * (size_t)c->n))) return rc;
+    if ((rc = dalloc(c, (void**)&c->d_wgrid, sizeof(WolffGrid)))) return rc;
+  }
   // bond probability 1 - exp(-2 J / T) as a threshold on a 32-bit word (src/integrator.rs:199-203)
   const double J = c->ham.has_exchange ? c->ham.exchange : 0.0;
   const double T = clamp_temperature(c->T);
@@ -1413,10 +1425,21 @@ int vg_wolff_steps(vg_ctx* c, uint64_t n, int32_t measure, double* E, double* M)
   VG_CUDA(c, cudaGetLastError());
   for (uint64_t t0 = 0; t0 < n; t0 += (1u << 30)) {
     const uint32_t k = (uint32_t)std::min<uint64_t>(n - t0, 1u << 30);
-    const cudaError_t e = launch_ising_wolff((int8_t*)c->d_stage, (int)c->n, c->z, c->d_wnbr, c->d_wocc, thr,
-                                             rng_key(c, c->sweep + t0), k,
-                                             measure ? c->d_sums + t0 * kNumSums : nullptr, c->stream);
+    double* sums = measure ? c->d_sums + t0 * kNumSums : nullptr;
+    const cudaError_t e =
+        grid ? launch_ising_wolff_grid((int8_t*)c->d_stage, (int)c->n, c->z, c->d_wnbr, c->d_wocc, thr,
+                                       rng_key(c, c->sweep + t0), k, sums, c->d_wmark, c->d_wq, c->d_wgrid,
+                                       c->sm_count, c->stream)
+             : launch_ising_wolff((int8_t*)c->d_stage, (int)c->n, c->z, c->d_wnbr, c->d_wocc, thr,
+                                  rng_key(c, c->sweep + t0), k, sums, c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "Wolff kernel launch");
+    if (grid) {  // a grid barrier that gave up leaves the flag set
+      unsigned int aborted = 0;
+      VG_CUDA(c, cudaMemcpyAsync(&aborted, &c->d_wgrid->abort_flag, sizeof(aborted), cudaMemcpyDeviceToHost,
+                                 c->stream));
+      VG_CUDA(c, cudaStreamSynchronize(c->stream));
+      if (aborted) return fail(c, VG_ERR_TIMEOUT, "Wolff steps: a grid barrier wait ran out (2 s)");
+    }
   }
   VG_CUDA(c, cudaMemsetAsync(c->d_flag, 0, sizeof(int), c->stream));
   ising_import<<<copy_grid(c, c->n), 256, 0, c->stream>>>((const int8_t*)c->d_stage, c->n, structured, m,

@@ -167,6 +167,21 @@ cudaError_t launch_ising_sc(const IsingScArgs& a, const IsingTable& tab, RngKey 
 int ising_sc_blocks_per_sm(const IsingScArgs& a, const IsingTable& tab, int tpb);
 // Wolff cluster steps on natural-order int8 +-1 spins, one block.
 size_t ising_wolff_smem(int n);
+// The same steps over the whole grid (one cooperative launch) for lattices
+// beyond one block: spins, stamps (mark, n words) and queue (q, n entries)
+// in global memory; g is zeroed by the launcher, and g->abort_flag != 0
+// after the launch means a grid barrier gave up.
+constexpr int kWolffGridTpb = 512;
+struct WolffGrid {
+  unsigned int cnt[3];                // appends of level L go to cnt[L % 3]
+  unsigned int bar_count, bar_gen;    // grid barrier
+  unsigned int abort_flag;
+  unsigned long long cut;             // this step's sum of boundary spins (two's complement)
+  unsigned long long bond0, ups0;     // sums of the incoming state
+};
+cudaError_t launch_ising_wolff_grid(int8_t* spins, int n, int z, const int32_t* nbr, const uint8_t* occ,
+                                    unsigned long long thr, RngKey key, uint32_t n_steps, double* sums,
+                                    uint32_t* mark, int32_t* q, WolffGrid* g, int sm_count, cudaStream_t s);
 cudaError_t launch_ising_wolff(int8_t* spins, int n, int z, const int32_t* nbr, const uint8_t* occ,
                                unsigned long long thr, RngKey key, uint32_t n_steps, double* sums, cudaStream_t s);
 // Per-site energies and single-site energy changes on natural-order copies

@@ -148,9 +148,184 @@ __global__ void __launch_bounds__(1024) ising_wolff_kernel(int8_t* __restrict__ 
   for (int i = threadIdx.x; i < n; i += blockDim.x) spins[i] = s[i];
 }
 
+// ------------------------------------------------------------ multi-block
+// Lattices beyond one block's shared memory: one cooperative launch runs
+// every step of a call with the same steps as above, the spins, stamps and
+// queue in global memory (read through L2: other blocks write them within
+// the launch), each level's frontier spread over the whole grid, and a grid
+// barrier after every level and after the flip.  Appends are aggregated
+// per warp.  A barrier wait gives up after two seconds: the block raises
+// the abort flag, every block leaves at its next barrier, and the host
+// reports the failure.
+
+__device__ __forceinline__ unsigned int ld_acquire_gpu(const unsigned int* p) {
+  unsigned int v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_gpu(unsigned int* p, unsigned int v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+constexpr unsigned long long kBarrierTimeoutNs = 2000000000ull;
+
+// All blocks of the grid; false when the barrier was abandoned.
+__device__ bool grid_barrier(WolffGrid* g) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    const unsigned int gen = ld_acquire_gpu(&g->bar_gen);
+    __threadfence();
+    if (atomicAdd(&g->bar_count, 1u) == gridDim.x - 1) {
+      atomicExch(&g->bar_count, 0u);
+      __threadfence();
+      st_release_gpu(&g->bar_gen, gen + 1);
+    } else {
+      const unsigned long long t0 = global_ns();
+      while (ld_acquire_gpu(&g->bar_gen) == gen) {
+        if (ld_acquire_gpu(&g->abort_flag) || global_ns() - t0 > kBarrierTimeoutNs) {
+          atomicExch(&g->abort_flag, 1u);
+          break;
+        }
+      }
+    }
+    __threadfence();
+    if (ld_acquire_gpu(&g->abort_flag)) ok = 0;
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+__global__ void __launch_bounds__(kWolffGridTpb) ising_wolff_grid_kernel(
+    int8_t* __restrict__ spins, int n, int z, const int32_t* __restrict__ nbr, const uint8_t* __restrict__ occ,
+    unsigned long long thr, RngKey key, uint32_t n_steps, double* __restrict__ sums, uint32_t* __restrict__ mark,
+    int32_t* __restrict__ q, WolffGrid* __restrict__ g) {
+  const int lane = threadIdx.x & 31;
+  const int gtid = blockIdx.x * blockDim.x + threadIdx.x, gsz = gridDim.x * blockDim.x;
+  const bool lead = gtid == 0;
+  for (int i = gtid; i < n; i += gsz) mark[i] = 0u;
+  if (sums) {  // the bond sum and up count of the incoming state
+    int b = 0, u = 0;
+    for (int i = gtid; i < n; i += gsz) {
+      const int si = spins[i];
+      u += si > 0;
+      for (int k = 0; k < z; ++k) {
+        const int j = __ldg(nbr + (size_t)i * z + k);
+        if (j > i) b += si * spins[j];
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      b += __shfl_down_sync(0xffffffffu, b, o);
+      u += __shfl_down_sync(0xffffffffu, u, o);
+    }
+    if (lane == 0) {
+      atomicAdd(&g->bond0, (unsigned long long)(long long)b);
+      atomicAdd(&g->ups0, (unsigned long long)(long long)u);
+    }
+  }
+  if (!grid_barrier(g)) return;
+  long long bond = (long long)__ldcg(&g->bond0), ups = (long long)__ldcg(&g->ups0);
+  for (uint32_t t = 0; t < n_steps; ++t) {
+    const uint32_t step = key.sweep + t;
+    const uint32_t stamp = t + 1;
+    const uint4 w0 = philox_ks(make_uint4(step, 0u, kTagWolffSource << 24, key.replica), key.ks);
+    const int src = (int)(((unsigned long long)w0.x * (unsigned long long)n) >> 32);
+    const int8_t ref = __ldcg(spins + src);
+    if (lead) {
+      mark[src] = stamp;
+      q[0] = src;
+    }
+    int lo = 0, hi = 1, lev = 0;
+    for (;;) {
+      const int items = (hi - lo) * z;
+      unsigned int* cnt = &g->cnt[lev % 3];
+      for (int base = gtid - lane; base < items; base += gsz) {
+        const int e = base + lane;
+        int j = -1;
+        bool want = false;
+        if (e < items) {
+          const int fi = e / z, k = e - fi * z;
+          const int site = lo == 0 ? src : __ldcg(q + lo + fi);
+          j = __ldg(nbr + (size_t)site * z + k);
+          if (j >= 0 && __ldcg(spins + j) == ref && __ldcg(mark + j) != stamp) {
+            const uint32_t a = (uint32_t)min(site, j), b = (uint32_t)max(site, j);
+            const uint32_t o = __ldg(occ + (size_t)site * z + k);
+            const uint4 w = philox_ks(
+                make_uint4(a, b, (kTagWolffBond << 24) | (o << 20) | (key.replica & 0xFFFFFu), step), key.ks);
+            want = (unsigned long long)w.x < thr && atomicExch(mark + j, stamp) != stamp;
+          }
+        }
+        const unsigned int m = __ballot_sync(0xffffffffu, want);
+        if (m) {
+          const int leader = __ffs(m) - 1;
+          unsigned int pos = 0;
+          if (lane == leader) pos = atomicAdd(cnt, (unsigned int)__popc(m));
+          pos = __shfl_sync(0xffffffffu, pos, leader);
+          if (want) q[hi + (int)pos + __popc(m & ((1u << lane) - 1u))] = j;
+        }
+      }
+      if (!grid_barrier(g)) return;
+      const int added = (int)__ldcg(cnt);
+      if (lead) g->cnt[(lev + 2) % 3] = 0u;  // used again two barriers later
+      if (added == 0) break;
+      lo = hi;
+      hi += added;
+      ++lev;
+    }
+    // flip the cluster and sum the spins across its boundary
+    int cut = 0;
+    for (int e = gtid; e < hi * z; e += gsz) {
+      const int fi = e / z, k = e - fi * z;
+      const int site = __ldcg(q + fi);
+      const int j = __ldg(nbr + (size_t)site * z + k);
+      if (j >= 0 && __ldcg(mark + j) != stamp) cut += __ldcg(spins + j);
+      if (k == 0) spins[site] = (int8_t)(-ref);
+    }
+    if (sums) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) cut += __shfl_down_sync(0xffffffffu, cut, o);
+      if (lane == 0 && cut) atomicAdd(&g->cut, (unsigned long long)(long long)cut);
+    }
+    if (!grid_barrier(g)) return;
+    if (sums && lead) {
+      const long long c = (long long)atomicExch(&g->cut, 0ull);  // read and clear for the next step
+      bond -= 2ll * ref * c;
+      ups += ref > 0 ? -(long long)hi : (long long)hi;
+      double* out = sums + (size_t)t * kNumSums;
+      out[0] = (double)bond;
+      out[1] = out[2] = out[3] = out[4] = out[5] = 0.0;
+      out[6] = (double)ups;
+      out[7] = (double)hi;
+    }
+  }
+}
+
 }  // namespace
 
 size_t ising_wolff_smem(int n) { return (size_t)n * 9; }
+
+cudaError_t launch_ising_wolff_grid(int8_t* spins, int n, int z, const int32_t* nbr, const uint8_t* occ,
+                                    unsigned long long thr, RngKey key, uint32_t n_steps, double* sums,
+                                    uint32_t* mark, int32_t* q, WolffGrid* g, int sm_count, cudaStream_t s) {
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ising_wolff_grid_kernel, kWolffGridTpb, 0);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) return cudaErrorCooperativeLaunchTooLarge;
+  // one block per SM: every block must be resident (cooperative launch), and
+  // a barrier costs one atomic per block
+  dim3 grid((unsigned)sm_count), block(kWolffGridTpb);
+  if ((e = cudaMemsetAsync(g, 0, sizeof(WolffGrid), s)) != cudaSuccess) return e;
+  void* args[] = {&spins, &n, &z, &nbr, &occ, &thr, &key, &n_steps, &sums, &mark, &q, &g};
+  return cudaLaunchCooperativeKernel((const void*)ising_wolff_grid_kernel, grid, block, args, 0, s);
+}
 
 cudaError_t launch_ising_wolff(int8_t* spins, int n, int z, const int32_t* nbr, const uint8_t* occ,
                                unsigned long long thr, RngKey key, uint32_t n_steps, double* sums, cudaStream_t s) {
