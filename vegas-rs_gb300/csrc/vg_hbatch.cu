@@ -744,7 +744,15 @@ int vg_hbatch_create(const vg_hbatch_desc* d, const vg_heis_replica* reps, int32
   b->ncell = (uint32_t)ncell;
   b->w = (!b->fp64 && L.nx % 4 == 0) ? 4 : 1;
   const uint32_t runs = b->ncell / (uint32_t)b->w;
-  b->nbx = (int)std::min<uint32_t>((runs + kPassTpb - 1) / kPassTpb, 4096u);
+  // two waves of resident blocks over all replicas (four per SM at the pass
+  // kernels' 64 registers), each block walking several runs of 256: fewer
+  // block rows to reduce in the measured sweeps than one block per 256 runs
+  // (fcc 64^3 cells x 64 replicas: 60.3 -> 63.9 flips/ns; one wave 60.6,
+  // four 63.6, sixteen 62.2)
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device) != cudaSuccess || sms < 1) sms = 1;
+  const uint32_t wave = (uint32_t)std::max(1, 2 * sms * kPassMinBlocks / n_rep);
+  b->nbx = (int)std::min<uint32_t>(std::min<uint32_t>((runs + kPassTpb - 1) / kPassTpb, wave), 4096u);
   auto fill = [&](auto& a) {
     a.ncell = b->ncell;
     a.nx = L.nx;
