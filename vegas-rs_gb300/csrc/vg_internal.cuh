@@ -174,8 +174,9 @@ size_t ising_wolff_smem(int n);
 constexpr int kWolffGridTpb = 512;
 struct WolffGrid {
   unsigned int cnt[3];                // appends of level L go to cnt[L % 3]
-  unsigned int bar_count, bar_gen;    // grid barrier
+  unsigned int bar_count;             // grid barrier: arrivals
   unsigned int abort_flag;
+  unsigned long long bar_word;        // grid barrier: generation << 32 | handed value
   unsigned long long cut;             // this step's sum of boundary spins (two's complement)
   unsigned long long bond0, ups0;     // sums of the incoming state
 };

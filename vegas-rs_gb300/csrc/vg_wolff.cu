@@ -163,9 +163,6 @@ __device__ __forceinline__ unsigned int ld_acquire_gpu(const unsigned int* p) {
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
-__device__ __forceinline__ void st_release_gpu(unsigned int* p, unsigned int v) {
-  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
 __device__ __forceinline__ unsigned long long global_ns() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -174,32 +171,59 @@ __device__ __forceinline__ unsigned long long global_ns() {
 
 constexpr unsigned long long kBarrierTimeoutNs = 2000000000ull;
 
-// All blocks of the grid; false when the barrier was abandoned.
-__device__ bool grid_barrier(WolffGrid* g) {
+__device__ __forceinline__ unsigned long long ld_acquire_gpu64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_gpu64(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned int atom_add_acq_rel_gpu(unsigned int* p, unsigned int v) {
+  unsigned int old;
+  asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
+__device__ __forceinline__ unsigned int ld_relaxed_gpu(const unsigned int* p) {
+  unsigned int v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// All blocks of the grid.  The release word carries (generation, value):
+// the last block to arrive reads *fold (every block's writes before the
+// barrier are visible to it) and hands it to all blocks with the release,
+// so a level's append count costs no extra round trip.  Returns false when
+// the barrier was abandoned (a wait ran out, here or in another block).
+__device__ bool grid_barrier(WolffGrid* g, const unsigned int* fold, unsigned int* folded) {
   __shared__ int s_ok;
+  __shared__ unsigned int s_fold;
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
-    const unsigned int gen = ld_acquire_gpu(&g->bar_gen);
-    __threadfence();
-    if (atomicAdd(&g->bar_count, 1u) == gridDim.x - 1) {
-      atomicExch(&g->bar_count, 0u);
-      __threadfence();
-      st_release_gpu(&g->bar_gen, gen + 1);
+    const unsigned int gen = (unsigned int)(ld_acquire_gpu64(&g->bar_word) >> 32);
+    unsigned long long w;
+    if (atom_add_acq_rel_gpu(&g->bar_count, 1u) == gridDim.x - 1) {
+      g->bar_count = 0u;  // ordered before the release below
+      w = ((unsigned long long)(gen + 1u) << 32) | (fold ? ld_relaxed_gpu(fold) : 0u);
+      st_release_gpu64(&g->bar_word, w);
     } else {
       const unsigned long long t0 = global_ns();
-      while (ld_acquire_gpu(&g->bar_gen) == gen) {
-        if (ld_acquire_gpu(&g->abort_flag) || global_ns() - t0 > kBarrierTimeoutNs) {
+      for (unsigned int k = 1;; ++k) {
+        w = ld_acquire_gpu64(&g->bar_word);
+        if ((unsigned int)(w >> 32) != gen) break;
+        if ((k & 255u) == 0u && (ld_acquire_gpu(&g->abort_flag) || global_ns() - t0 > kBarrierTimeoutNs)) {
           atomicExch(&g->abort_flag, 1u);
+          ok = 0;
           break;
         }
       }
     }
-    __threadfence();
-    if (ld_acquire_gpu(&g->abort_flag)) ok = 0;
     s_ok = ok;
+    s_fold = (unsigned int)w;
   }
   __syncthreads();
+  if (folded) *folded = s_fold;
   return s_ok != 0;
 }
 
@@ -231,7 +255,7 @@ __global__ void __launch_bounds__(kWolffGridTpb) ising_wolff_grid_kernel(
       atomicAdd(&g->ups0, (unsigned long long)(long long)u);
     }
   }
-  if (!grid_barrier(g)) return;
+  if (!grid_barrier(g, nullptr, nullptr)) return;
   long long bond = (long long)__ldcg(&g->bond0), ups = (long long)__ldcg(&g->ups0);
   for (uint32_t t = 0; t < n_steps; ++t) {
     const uint32_t step = key.sweep + t;
@@ -272,8 +296,8 @@ __global__ void __launch_bounds__(kWolffGridTpb) ising_wolff_grid_kernel(
           if (want) q[hi + (int)pos + __popc(m & ((1u << lane) - 1u))] = j;
         }
       }
-      if (!grid_barrier(g)) return;
-      const int added = (int)__ldcg(cnt);
+      unsigned int added;
+      if (!grid_barrier(g, cnt, &added)) return;
       if (lead) g->cnt[(lev + 2) % 3] = 0u;  // used again two barriers later
       if (added == 0) break;
       lo = hi;
@@ -294,7 +318,7 @@ __global__ void __launch_bounds__(kWolffGridTpb) ising_wolff_grid_kernel(
       for (int o = 16; o > 0; o >>= 1) cut += __shfl_down_sync(0xffffffffu, cut, o);
       if (lane == 0 && cut) atomicAdd(&g->cut, (unsigned long long)(long long)cut);
     }
-    if (!grid_barrier(g)) return;
+    if (!grid_barrier(g, nullptr, nullptr)) return;
     if (sums && lead) {
       const long long c = (long long)atomicExch(&g->cut, 0ull);  // read and clear for the next step
       bond -= 2ll * ref * c;
