@@ -11,7 +11,11 @@
 // looks up the site's threshold and compares its 32-bit uniform digit by
 // digit with the same Philox blocks the grid kernels use (byte (j & 15) of
 // block (j >> 4, sweep, tag, colour | digit)), so results are bit-identical
-// to the grid path.
+// to the grid path.  When every thread holds at most one site per class
+// (lattices up to 2,048 sites) the neighbour indices are formed once per
+// launch; the first digit's block starts before the neighbour loads; the
+// sweep sums go through double-buffered shared slots, so a sweep costs two
+// block barriers.
 #include <cuda_runtime.h>
 
 #include "vg_internal.cuh"
@@ -25,12 +29,82 @@ __device__ __forceinline__ uint32_t block_byte_k(const uint4& b, int k) {
   return (w >> (8 * (k & 3))) & 0xFFu;
 }
 
+// Shared-memory indices (in the other class) of the neighbours of class-C
+// entry j; -1 where an open axis drops the bond.
+__device__ __forceinline__ void resident_nbrs(const IsingScArgs& a, int C, uint32_t j, int (&nb)[6]) {
+  const int row = (int)fdiv(j >> 4, a.fG);  // a row holds G groups of 16
+  const int h = (int)(j - (uint32_t)row * a.Hx);
+  const int z = (int)fdiv((uint32_t)row, a.fLy);
+  const int y = row - z * a.Ly;
+  const int p = (y + z + C) & 1;
+  const int rb = row * a.Hx;
+  const int plane = a.Ly * a.Hx;
+  nb[0] = rb + h;
+  const int hx = p ? h + 1 : h - 1;
+  nb[1] = (hx >= 0 && hx < a.Hx) ? rb + hx : (a.pbx ? rb + (hx < 0 ? a.Hx - 1 : 0) : -1);
+  nb[2] = y > 0 ? rb - a.Hx + h : (a.pby ? rb + (a.Ly - 1) * a.Hx + h : -1);
+  nb[3] = y < a.Ly - 1 ? rb + a.Hx + h : (a.pby ? rb - (a.Ly - 1) * a.Hx + h : -1);
+  nb[4] = z > 0 ? rb - plane + h : (a.pbz ? rb + (a.Lz - 1) * plane + h : -1);
+  nb[5] = z < a.Lz - 1 ? rb + plane + h : (a.pbz ? rb - (a.Lz - 1) * plane + h : -1);
+}
+
+// One site's update in a colour pass; adds to the sweep's sums.
+template <int PROP>
+__device__ __forceinline__ void resident_site(int C, uint32_t j, const int (&nb)[6], uint8_t* own,
+                                              const uint8_t* oth, const unsigned long long* s_thr,
+                                              const RngKey& key, uint32_t sweep, int& bond, int& ups, int& nacc) {
+  const uint32_t g = j >> 4;
+  const int k = (int)(j & 15u);
+  // the first digit's block does not depend on the spins: start it first
+  const uint4 b0 =
+      philox_ks(make_uint4(g, sweep, (kTagIsingAccept << 24) | ((uint32_t)C << 8), key.replica), key.ks);
+  int nsum = 0;
+#pragma unroll
+  for (int i = 0; i < 6; ++i)
+    if (nb[i] >= 0) nsum += 2 * (int)oth[nb[i]] - 1;
+  const uint32_t s01 = own[j];
+  bool cand = true;
+  if (PROP == VG_PROPOSE_RANDOM) {
+    const uint4 pb = philox_ks(make_uint4(g, sweep, (kTagIsingPropose << 24) | ((uint32_t)C << 8), key.replica),
+                               key.ks);
+    cand = (block_byte_k(pb, k) < 128 ? 1u : 0u) != s01;
+  }
+  bool acc = false;
+  if (cand) {
+    const unsigned long long th = s_thr[s01 * 13 + nsum + 6];
+    if (th >= (1ull << 32)) {
+      acc = true;
+    } else if (th > 0ull) {
+      uint32_t ub = block_byte_k(b0, k), tb = ((uint32_t)th >> 24) & 0xFFu;
+      if (ub != tb) {
+        acc = ub < tb;
+      } else {  // tie on the first digit (probability 1/256): later digits
+        for (int d = 1; d < 4; ++d) {
+          const uint4 bd = philox_ks(
+              make_uint4(g, sweep, (kTagIsingAccept << 24) | ((uint32_t)C << 8) | (uint32_t)d, key.replica), key.ks);
+          ub = block_byte_k(bd, k);
+          tb = ((uint32_t)th >> (24 - 8 * d)) & 0xFFu;
+          if (ub != tb) {
+            acc = ub < tb;
+            break;
+          }
+        }
+      }
+    }
+  }
+  const uint32_t sn = acc ? (s01 ^ 1u) : s01;
+  if (acc) own[j] = (uint8_t)sn;
+  ups += (int)sn;
+  nacc += acc;
+  if (C == 1) bond += sn ? nsum : -nsum;
+}
+
 template <int PROP>
 __global__ void __launch_bounds__(1024) ising_resident_kernel(IsingScArgs a, IsingTable tab, RngKey key,
                                                               uint32_t n_sweeps, double* __restrict__ sums) {
   extern __shared__ uint8_t s_spin[];  // class 0 then class 1, n_c bytes each
   __shared__ unsigned long long s_thr[2 * 13];
-  __shared__ int s_red[3][32];
+  __shared__ int s_red[2][3][32];      // per sweep parity: no barrier after the read
   const uint32_t n_c = a.groups * 16u;
   uint8_t* cls[2] = {s_spin, s_spin + n_c};
   for (uint32_t i = threadIdx.x; i < n_c; i += blockDim.x) {
@@ -39,102 +113,66 @@ __global__ void __launch_bounds__(1024) ising_resident_kernel(IsingScArgs a, Isi
   }
   for (int i = threadIdx.x; i < 26; i += blockDim.x) s_thr[i] = tab.thr[i];
   __syncthreads();
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = (int)(blockDim.x >> 5);
+  // at most one site per thread and class: its neighbours once per launch
+  const bool one = n_c <= blockDim.x;
+  const bool mine = threadIdx.x < n_c;
+  int nb0[6], nb1[6];
+  if (one && mine) {
+    resident_nbrs(a, 0, threadIdx.x, nb0);
+    resident_nbrs(a, 1, threadIdx.x, nb1);
+  }
   for (uint32_t t = 0; t < n_sweeps; ++t) {
     const uint32_t sweep = key.sweep + t;
     int bond = 0, ups = 0, nacc = 0;
+#pragma unroll
     for (int C = 0; C < 2; ++C) {
       uint8_t* own = cls[C];
       const uint8_t* oth = cls[C ^ 1];
-      for (uint32_t j = threadIdx.x; j < n_c; j += blockDim.x) {
-        const int row = (int)fdiv(j >> 4, a.fG);  // a row holds G groups of 16
-        const int h = (int)(j - (uint32_t)row * a.Hx);
-        const int z = (int)fdiv((uint32_t)row, a.fLy);
-        const int y = row - z * a.Ly;
-        const int p = (y + z + C) & 1;
-        const int rb = row * a.Hx;
-        int nsum = 0, nb = 0;
-        auto add = [&](int q) {
-          nsum += 2 * (int)oth[q] - 1;
-          ++nb;
-        };
-        add(rb + h);
-        const int hx = p ? h + 1 : h - 1;
-        if (hx >= 0 && hx < a.Hx) add(rb + hx);
-        else if (a.pbx) add(rb + (hx < 0 ? a.Hx - 1 : 0));
-        if (y > 0) add(rb - a.Hx + h);
-        else if (a.pby) add(rb + (a.Ly - 1) * a.Hx + h);
-        if (y < a.Ly - 1) add(rb + a.Hx + h);
-        else if (a.pby) add(rb - (a.Ly - 1) * a.Hx + h);
-        const int plane = a.Ly * a.Hx;
-        if (z > 0) add(rb - plane + h);
-        else if (a.pbz) add(rb + (a.Lz - 1) * plane + h);
-        if (z < a.Lz - 1) add(rb + plane + h);
-        else if (a.pbz) add(rb - (a.Lz - 1) * plane + h);
-        (void)nb;
-        const uint32_t s01 = own[j];
-        const uint32_t g = j >> 4;
-        const int k = (int)(j & 15u);
-        bool cand = true;
-        if (PROP == VG_PROPOSE_RANDOM) {
-          const uint4 pb = philox_ks(make_uint4(g, sweep, (kTagIsingPropose << 24) | ((uint32_t)C << 8), key.replica),
-                                     key.ks);
-          const uint32_t up = block_byte_k(pb, k) < 128 ? 1u : 0u;
-          cand = up != s01;
+      if (one) {
+        if (mine) resident_site<PROP>(C, threadIdx.x, C ? nb1 : nb0, own, oth, s_thr, key, sweep, bond, ups, nacc);
+      } else {
+        for (uint32_t j = threadIdx.x; j < n_c; j += blockDim.x) {
+          int nb[6];
+          resident_nbrs(a, C, j, nb);
+          resident_site<PROP>(C, j, nb, own, oth, s_thr, key, sweep, bond, ups, nacc);
         }
-        bool acc = false;
-        if (cand) {
-          const unsigned long long th = s_thr[s01 * 13 + nsum + 6];
-          if (th >= (1ull << 32)) {
-            acc = true;
-          } else if (th > 0ull) {
-            for (int d = 0; d < 4; ++d) {
-              const uint4 bd = philox_ks(
-                  make_uint4(g, sweep, (kTagIsingAccept << 24) | ((uint32_t)C << 8) | (uint32_t)d, key.replica),
-                  key.ks);
-              const uint32_t ub = block_byte_k(bd, k), tb = ((uint32_t)th >> (24 - 8 * d)) & 0xFFu;
-              if (ub != tb) {
-                acc = ub < tb;
-                break;
-              }
-            }
-          }
-        }
-        const uint32_t sn = acc ? (s01 ^ 1u) : s01;
-        if (acc) own[j] = (uint8_t)sn;
-        ups += (int)sn;
-        nacc += acc;
-        if (C == 1) bond += sn ? nsum : -nsum;
       }
-      __syncthreads();
+      if (C == 0) __syncthreads();
     }
-    // block sums of this sweep
+    // sweep sums: per warp, then over the warps by warp 0
+#pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       bond += __shfl_down_sync(0xffffffffu, bond, o);
       ups += __shfl_down_sync(0xffffffffu, ups, o);
       nacc += __shfl_down_sync(0xffffffffu, nacc, o);
     }
+    int (*red)[32] = s_red[t & 1];
     if (lane == 0) {
-      s_red[0][warp] = bond;
-      s_red[1][warp] = ups;
-      s_red[2][warp] = nacc;
+      red[0][warp] = bond;
+      red[1][warp] = ups;
+      red[2][warp] = nacc;
     }
-    __syncthreads();
-    if (threadIdx.x == 0 && sums) {
-      long long b = 0, u = 0, c = 0;
-      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
-        b += s_red[0][w];
-        u += s_red[1][w];
-        c += s_red[2][w];
+    __syncthreads();  // also ends the class-1 pass
+    if (warp == 0 && sums) {
+      int b = lane < nwarp ? red[0][lane] : 0, u = lane < nwarp ? red[1][lane] : 0,
+          c = lane < nwarp ? red[2][lane] : 0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        b += __shfl_down_sync(0xffffffffu, b, o);
+        u += __shfl_down_sync(0xffffffffu, u, o);
+        c += __shfl_down_sync(0xffffffffu, c, o);
       }
-      double* o = sums + (size_t)t * kNumSums;
-      o[0] = (double)b;
-      o[1] = o[2] = o[3] = o[4] = o[5] = 0.0;
-      o[6] = (double)u;
-      o[7] = (double)c;
+      if (lane == 0) {
+        double* o = sums + (size_t)t * kNumSums;
+        o[0] = (double)b;
+        o[1] = o[2] = o[3] = o[4] = o[5] = 0.0;
+        o[6] = (double)u;
+        o[7] = (double)c;
+      }
     }
-    __syncthreads();
   }
+  __syncthreads();
   for (uint32_t i = threadIdx.x; i < n_c; i += blockDim.x) {
     a.cls[0][i] = cls[0][i];
     a.cls[1][i] = cls[1][i];
