@@ -174,14 +174,15 @@ def run_reference(args, rank):
     threads = os.cpu_count() or 1
     H = O.Hamiltonian(has_exchange=1, J=1.0, compound=0)
     lat = O.lattice("sc", L, L, L)
-    # bounded sample: each step is one measured reference sweep of the
-    # 256^3 lattice on every host core (lattice setup included once per call)
-    steps = max(1, min(args.steps, 3))
-    flips, dt = O.ref_parallel(lat, 0, H, 4.5, steps, threads, seed=SEED, measure=True)
+    # each step is one measured reference sweep of a 256^3 lattice on every
+    # host core (about five seconds); the warm-up sweeps run untimed first
+    steps = max(1, args.steps)
+    warm = max(0, args.warmup)
+    flips, dt = O.ref_parallel(lat, 0, H, 4.5, steps, threads, seed=SEED, measure=True, warmup=warm)
     v = flips / (dt * 1e9)
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "flips/ns", "n_gpus": args.gpus,
-        "steps": steps, "warmup": 0, "ms_per_step": dt * 1e3 / steps, "higher_is_better": True,
+        "steps": steps, "warmup": warm, "ms_per_step": dt * 1e3 / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "ising-sc-256^3-pbc-J1-h0 (reference random-site Metropolis, CLI measurement)",
                    "lattice": [L, L, L], "threads": threads},

@@ -119,7 +119,7 @@ def lib():
         L.vo_ref_magnetization.argtypes = [C.c_int64, C.c_int32, P(C.c_int8), P(C.c_double)]
         L.vo_ref_magnetization.restype = C.c_double
         L.vo_ref_parallel.argtypes = [P(Lattice), C.c_int32, C.c_int32, P(Hamiltonian), C.c_double, C.c_double,
-                                      C.c_int32, C.c_int32, C.c_int32, C.c_uint64, P(C.c_double)]
+                                      C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, P(C.c_double)]
         L.vo_ref_parallel.restype = C.c_int64
         L.vo_cooldown_temperatures.argtypes = [C.c_double, C.c_double, C.c_double, P(C.c_double), C.c_int32]
         L.vo_cooldown_temperatures.restype = C.c_int32
@@ -374,10 +374,11 @@ def accumulate(x):
 
 
 def ref_parallel(lat: Lattice, kind, H: Hamiltonian, T, nsweeps, nthreads, seed=1, proposal=PROPOSE_FLIP,
-                 measure=True, bmag=0.0):
-    """Independent reference chains, one per thread (field bmag along z);
-    returns (flips, seconds of sweeping)."""
+                 measure=True, bmag=0.0, warmup=0):
+    """Independent reference chains, one per thread (field bmag along z):
+    `warmup` untimed sweeps, then `nsweeps` timed ones; returns (flips,
+    seconds of timed sweeping)."""
     sec = C.c_double()
-    flips = int(lib().vo_ref_parallel(C.byref(lat), kind, proposal, C.byref(H), T, bmag, nsweeps, int(measure),
-                                      nthreads, seed, C.byref(sec)))
+    flips = int(lib().vo_ref_parallel(C.byref(lat), kind, proposal, C.byref(H), T, bmag, warmup, nsweeps,
+                                      int(measure), nthreads, seed, C.byref(sec)))
     return flips, sec.value

@@ -792,7 +792,7 @@ int vo_ref_sweeps(int64_t n, int32_t zmax, const int32_t* nbr, int32_t kind, int
 
 typedef struct {
   const vo_lattice* lat;
-  int32_t kind, proposal, nsweeps, measure;
+  int32_t kind, proposal, nsweeps, measure, nwarm;
   const vo_hamiltonian* H;
   double T, bmag;
   uint64_t seed;
@@ -826,6 +826,12 @@ static void* par_worker(void* arg) {
   }
   double* obs = (double*)malloc(sizeof(double) * 2 * (size_t)(J->nsweeps > 0 ? J->nsweeps : 1));
   double b[3] = {0, 0, 1};
+  if (J->nwarm > 0) { /* untimed warm-up sweeps */
+    double* wo = (double*)malloc(sizeof(double) * 2 * (size_t)J->nwarm);
+    vo_ref_sweeps(n, z, nbr, J->kind, J->proposal, si, sf, J->H, J->T, b, J->bmag, &rng, J->nwarm, J->measure, 1,
+                  wo);
+    free(wo);
+  }
   pthread_barrier_wait(J->start); /* all chains set up: time the sweeps only */
   double t0 = now_s();
   vo_ref_sweeps(n, z, nbr, J->kind, J->proposal, si, sf, J->H, J->T, b, J->bmag, &rng, J->nsweeps, J->measure, 1,
@@ -840,15 +846,15 @@ static void* par_worker(void* arg) {
 }
 
 int64_t vo_ref_parallel(const vo_lattice* lat, int32_t kind, int32_t proposal, const vo_hamiltonian* H,
-                        double T, double bmag, int32_t nsweeps, int32_t measure, int32_t nthreads, uint64_t seed,
-                        double* seconds) {
+                        double T, double bmag, int32_t nwarm, int32_t nsweeps, int32_t measure, int32_t nthreads,
+                        uint64_t seed, double* seconds) {
   if (nthreads < 1) nthreads = 1;
   pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)nthreads);
   par_job* jobs = (par_job*)malloc(sizeof(par_job) * (size_t)nthreads);
   pthread_barrier_t start;
   pthread_barrier_init(&start, NULL, (unsigned)nthreads);
   for (int k = 0; k < nthreads; ++k) {
-    par_job j = {lat, kind, proposal, nsweeps, measure, H, T, bmag, seed + 7919ull * (uint64_t)k, 0, &start, 0.0};
+    par_job j = {lat, kind, proposal, nsweeps, measure, nwarm, H, T, bmag, seed + 7919ull * (uint64_t)k, 0, &start, 0.0};
     jobs[k] = j;
     pthread_create(&th[k], NULL, par_worker, &jobs[k]);
   }

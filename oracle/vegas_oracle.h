@@ -167,11 +167,12 @@ void vo_ref_site_energies(int64_t n, int32_t zmax, const int32_t* nbr, int32_t s
                           double* out);
 
 /* Independent reference chains on nthreads host threads (one lattice each),
- * for the multi-core CPU baseline.  Returns total attempted flips; *seconds
- * receives the slowest chain's sweep time (setup excluded). */
+ * for the multi-core CPU baseline: nwarm untimed sweeps, then nsweeps timed
+ * ones.  Returns the timed attempted flips; *seconds receives the slowest
+ * chain's timed sweep time (setup and warm-up excluded). */
 int64_t vo_ref_parallel(const vo_lattice* lat, int32_t spin_kind, int32_t proposal,
-                        const vo_hamiltonian* H, double T, double bmag, int32_t nsweeps, int32_t measure,
-                        int32_t nthreads, uint64_t seed, double* seconds);
+                        const vo_hamiltonian* H, double T, double bmag, int32_t nwarm, int32_t nsweeps,
+                        int32_t measure, int32_t nthreads, uint64_t seed, double* seconds);
 
 /* --------------------------------- (a) colour_cpu: batched multi-spin coding */
 /* A replica group: n_rep replicas (a multiple of 32) of one sc lattice that
