@@ -13,10 +13,14 @@
 // block (j >> 4, sweep, tag, colour | digit)), so results are bit-identical
 // to the grid path.  When every thread holds at most one site per class
 // (lattices up to 2,048 sites) the neighbour indices are formed once per
-// launch; the first digit's block starts before the neighbour loads; the
-// sweep sums go through double-buffered shared slots, so a sweep costs two
-// block barriers.
+// launch and the first digit's block starts before the neighbour loads; up
+// to 1,024 sites the sixteen threads of a group also share the first-digit
+// blocks of eight sweeps (one Philox block per thread per eight sweeps).
+// The sweep sums go through double-buffered shared slots, so a sweep costs
+// two block barriers.
 #include <cuda_runtime.h>
+
+#include <algorithm>
 
 #include "vg_internal.cuh"
 
@@ -49,15 +53,19 @@ __device__ __forceinline__ void resident_nbrs(const IsingScArgs& a, int C, uint3
 }
 
 // One site's update in a colour pass; adds to the sweep's sums.
+// r0: the word of the first digit's block holding this site's byte, when the
+// caller already has it (otherwise null: the block is drawn here).
 template <int PROP>
 __device__ __forceinline__ void resident_site(int C, uint32_t j, const int (&nb)[6], uint8_t* own,
                                               const uint8_t* oth, const unsigned long long* s_thr,
-                                              const RngKey& key, uint32_t sweep, int& bond, int& ups, int& nacc) {
+                                              const RngKey& key, uint32_t sweep, const uint32_t* r0, int& bond,
+                                              int& ups, int& nacc) {
   const uint32_t g = j >> 4;
   const int k = (int)(j & 15u);
   // the first digit's block does not depend on the spins: start it first
-  const uint4 b0 =
-      philox_ks(make_uint4(g, sweep, (kTagIsingAccept << 24) | ((uint32_t)C << 8), key.replica), key.ks);
+  uint4 b0 = make_uint4(0u, 0u, 0u, 0u);
+  if (r0) b0.x = b0.y = b0.z = b0.w = *r0;
+  else b0 = philox_ks(make_uint4(g, sweep, (kTagIsingAccept << 24) | ((uint32_t)C << 8), key.replica), key.ks);
   int nsum = 0;
 #pragma unroll
   for (int i = 0; i < 6; ++i)
@@ -99,8 +107,13 @@ __device__ __forceinline__ void resident_site(int C, uint32_t j, const int (&nb)
   if (C == 1) bond += sn ? nsum : -nsum;
 }
 
-template <int PROP>
-__global__ void __launch_bounds__(1024) ising_resident_kernel(IsingScArgs a, IsingTable tab, RngKey key,
+// MAXT: the block bound.  Lattices of up to 1,024 sites run 512 threads at
+// most, with the registers to keep the neighbours and the shared first-digit
+// blocks without spilling (sc 32x32x1: 0.77 -> 0.91 flips/ns); larger ones
+// run up to 1,024 threads and draw each pass's block per site (a 512-thread
+// bound there would put two sites on a thread: 2,048 sites 0.98 -> 0.69).
+template <int PROP, int MAXT>
+__global__ void __launch_bounds__(MAXT) ising_resident_kernel(IsingScArgs a, IsingTable tab, RngKey key,
                                                               uint32_t n_sweeps, double* __restrict__ sums) {
   extern __shared__ uint8_t s_spin[];  // class 0 then class 1, n_c bytes each
   __shared__ unsigned long long s_thr[2 * 13];
@@ -115,6 +128,7 @@ __global__ void __launch_bounds__(1024) ising_resident_kernel(IsingScArgs a, Isi
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = (int)(blockDim.x >> 5);
   // at most one site per thread and class: its neighbours once per launch
+  constexpr bool kShare = MAXT <= 512;  // shared first-digit blocks
   const bool one = n_c <= blockDim.x;
   const bool mine = threadIdx.x < n_c;
   int nb0[6], nb1[6];
@@ -122,20 +136,40 @@ __global__ void __launch_bounds__(1024) ising_resident_kernel(IsingScArgs a, Isi
     resident_nbrs(a, 0, threadIdx.x, nb0);
     resident_nbrs(a, 1, threadIdx.x, nb1);
   }
+  // One site per thread: the sixteen lanes of a half warp share one group,
+  // so every eight sweeps lane i of the half warp draws the first-digit
+  // block of colour pass i (sweep i / 2, colour i % 2) and each pass takes
+  // its site's word from that lane by shuffles: one Philox block per lane
+  // per eight sweeps instead of one per pass.
+  uint4 blk = make_uint4(0u, 0u, 0u, 0u);
+  const uint32_t grp = threadIdx.x >> 4, wq = (threadIdx.x >> 2) & 3u;
   for (uint32_t t = 0; t < n_sweeps; ++t) {
     const uint32_t sweep = key.sweep + t;
+    if (kShare && one && (t & 7u) == 0u) {
+      const uint32_t pi = (uint32_t)lane & 15u;
+      blk = philox_ks(make_uint4(grp, sweep + (pi >> 1), (kTagIsingAccept << 24) | ((pi & 1u) << 8), key.replica),
+                      key.ks);
+    }
     int bond = 0, ups = 0, nacc = 0;
 #pragma unroll
     for (int C = 0; C < 2; ++C) {
       uint8_t* own = cls[C];
       const uint8_t* oth = cls[C ^ 1];
-      if (one) {
-        if (mine) resident_site<PROP>(C, threadIdx.x, C ? nb1 : nb0, own, oth, s_thr, key, sweep, bond, ups, nacc);
+      if (kShare && one) {
+        const int src = (lane & 16) | (int)(2u * (t & 7u) + (uint32_t)C);
+        const uint32_t w0 = __shfl_sync(0xffffffffu, blk.x, src), w1 = __shfl_sync(0xffffffffu, blk.y, src),
+                       w2 = __shfl_sync(0xffffffffu, blk.z, src), w3 = __shfl_sync(0xffffffffu, blk.w, src);
+        const uint32_t r0 = wq == 0 ? w0 : wq == 1 ? w1 : wq == 2 ? w2 : w3;
+        if (mine)
+          resident_site<PROP>(C, threadIdx.x, C ? nb1 : nb0, own, oth, s_thr, key, sweep, &r0, bond, ups, nacc);
+      } else if (one) {
+        if (mine)
+          resident_site<PROP>(C, threadIdx.x, C ? nb1 : nb0, own, oth, s_thr, key, sweep, nullptr, bond, ups, nacc);
       } else {
         for (uint32_t j = threadIdx.x; j < n_c; j += blockDim.x) {
           int nb[6];
           resident_nbrs(a, C, j, nb);
-          resident_site<PROP>(C, j, nb, own, oth, s_thr, key, sweep, bond, ups, nacc);
+          resident_site<PROP>(C, j, nb, own, oth, s_thr, key, sweep, nullptr, bond, ups, nacc);
         }
       }
       if (C == 0) __syncthreads();
@@ -183,22 +217,29 @@ __global__ void __launch_bounds__(1024) ising_resident_kernel(IsingScArgs a, Isi
 
 size_t ising_resident_smem(const IsingScArgs& a) { return (size_t)a.groups * 16u * 2u; }
 
+namespace {
+
+template <int PROP, int MAXT>
+cudaError_t launch_resident(const IsingScArgs& a, const IsingTable& tab, RngKey key, uint32_t n_sweeps,
+                            double* sums, int tpb, size_t smem, cudaStream_t s) {
+  const cudaError_t e = cudaFuncSetAttribute(ising_resident_kernel<PROP, MAXT>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  ising_resident_kernel<PROP, MAXT><<<1, std::min(tpb, MAXT), smem, s>>>(a, tab, key, n_sweeps, sums);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
 cudaError_t launch_ising_resident(const IsingScArgs& a, const IsingTable& tab, RngKey key, int proposal,
                                   uint32_t n_sweeps, double* sums, int tpb, cudaStream_t s) {
   const size_t smem = ising_resident_smem(a);
-  cudaError_t e;
-  if (proposal == VG_PROPOSE_RANDOM) {
-    e = cudaFuncSetAttribute(ising_resident_kernel<VG_PROPOSE_RANDOM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem);
-    if (e != cudaSuccess) return e;
-    ising_resident_kernel<VG_PROPOSE_RANDOM><<<1, tpb, smem, s>>>(a, tab, key, n_sweeps, sums);
-  } else {
-    e = cudaFuncSetAttribute(ising_resident_kernel<VG_PROPOSE_FLIP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem);
-    if (e != cudaSuccess) return e;
-    ising_resident_kernel<VG_PROPOSE_FLIP><<<1, tpb, smem, s>>>(a, tab, key, n_sweeps, sums);
-  }
-  return cudaGetLastError();
+  const bool small = a.groups * 16u <= 512u;  // one site per thread within 512 threads
+  if (proposal == VG_PROPOSE_RANDOM)
+    return small ? launch_resident<VG_PROPOSE_RANDOM, 512>(a, tab, key, n_sweeps, sums, tpb, smem, s)
+                 : launch_resident<VG_PROPOSE_RANDOM, 1024>(a, tab, key, n_sweeps, sums, tpb, smem, s);
+  return small ? launch_resident<VG_PROPOSE_FLIP, 512>(a, tab, key, n_sweeps, sums, tpb, smem, s)
+               : launch_resident<VG_PROPOSE_FLIP, 1024>(a, tab, key, n_sweeps, sums, tpb, smem, s);
 }
 
 }  // namespace vg
