@@ -298,7 +298,8 @@ def run_wolff(V, torch, args):
     steps; a bounded sample of 20,000 steps at T = 4.5 (near the critical
     point, where clusters are largest in spread) on the single-block kernel,
     beside the same steps of the oracle's cluster algorithm on one core; and
-    sc 64^3 near T_c on the multi-block kernel."""
+    sc 64^3 and 128^3 near T_c on the bit-packed one-block and the
+    multi-block kernels."""
     import oracle as O
 
     lat = V.Lattice.sc(10, 10, 10)
@@ -327,38 +328,42 @@ def run_wolff(V, torch, args):
         cpu = {"value": n / dt, "unit": "cluster steps/s", "cores": 1, "kind": "port",
                "sample": f"{n} cluster steps of the oracle's Wolff algorithm at T = 4.5 on one core",
                "mean_cluster": float(obs[:, 2].mean())}
-    # a lattice beyond one block: the multi-block kernel, equilibrated near T_c
-    L, ng = 64, 300
-    with V.Engine(V.Lattice.sc(L, L, L), V.hamiltonian(V.Exchange(1.0)), seed=SEED) as eng:
-        eng.init_random()
-        eng.set_thermostat(4.5)
-        eng.sweeps(300, measure=False)
-        eng.wolff_steps(300, measure=False)
-        state_g = eng.get_state()
-        step0 = eng.info().sweep_index
-        s = torch.cuda.ExternalStream(eng.stream())
-        a, c = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(s)
-        _, Mg = eng.wolff_steps(ng)
-        c.record(s)
-        eng.synchronize()
-        ms_g = a.elapsed_time(c)
-    grid = {"workload": f"sc {L}^3 Ising, Wolff cluster steps at T = 4.5 after 300 Metropolis sweeps and 300 "
-                        "cluster steps (multi-block kernel, measured steps)",
-            "value": ng / (ms_g * 1e-3), "unit": "cluster steps/s", "ms": ms_g, "steps": ng,
-            "mean_abs_m_per_spin": float(Mg.mean() / L ** 3)}
-    if not args.no_cpu_baseline:
-        g = O.Graph(O.lattice("sc", L, L, L))
-        m = 20
-        t0 = time.perf_counter()
-        _, obs = g.wolff_steps(state_g, 1.0, 4.5, SEED, step0, m)
-        dt = time.perf_counter() - t0
-        grid["cpu_baseline"] = {"value": m / dt, "unit": "cluster steps/s", "cores": 1, "kind": "port",
-                                "sample": f"{m} cluster steps of the oracle's Wolff algorithm from the same state",
-                                "mean_cluster": float(obs[:, 2].mean())}
+    # larger lattices near T_c: 64^3 (spins and marks as bits in one block)
+    # and 128^3 (the multi-block kernel), equilibrated first
+    larger = {}
+    for L, kind in ((64, "one-block bit-packed kernel"), (128, "multi-block kernel")):
+        ng = 300
+        with V.Engine(V.Lattice.sc(L, L, L), V.hamiltonian(V.Exchange(1.0)), seed=SEED) as eng:
+            eng.init_random()
+            eng.set_thermostat(4.5)
+            eng.sweeps(300, measure=False)
+            eng.wolff_steps(300, measure=False)
+            state_g = eng.get_state()
+            step0 = eng.info().sweep_index
+            s = torch.cuda.ExternalStream(eng.stream())
+            a, c = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(s)
+            _, Mg = eng.wolff_steps(ng)
+            c.record(s)
+            eng.synchronize()
+            ms_g = a.elapsed_time(c)
+        entry = {"workload": f"sc {L}^3 Ising, Wolff cluster steps at T = 4.5 after 300 Metropolis sweeps and 300 "
+                             f"cluster steps ({kind}, measured steps)",
+                 "value": ng / (ms_g * 1e-3), "unit": "cluster steps/s", "ms": ms_g, "steps": ng,
+                 "mean_abs_m_per_spin": float(Mg.mean() / L ** 3)}
+        if not args.no_cpu_baseline:
+            g = O.Graph(O.lattice("sc", L, L, L))
+            m = 20
+            t0 = time.perf_counter()
+            _, obs = g.wolff_steps(state_g, 1.0, 4.5, SEED, step0, m)
+            dt = time.perf_counter() - t0
+            entry["cpu_baseline"] = {"value": m / dt, "unit": "cluster steps/s", "cores": 1, "kind": "port",
+                                     "sample": f"{m} cluster steps of the oracle's Wolff algorithm from the same state",
+                                     "mean_cluster": float(obs[:, 2].mean())}
+        larger[f"sc{L}"] = entry
     return {"workload": "sc 10x10x10 Ising, Wolff cluster steps (docs/wolff.toml lattice), T = 4.5",
             "value": n / (ms * 1e-3), "unit": "cluster steps/s", "ms": ms, "steps": n, "cpu_baseline": cpu,
-            "multi_block": grid}
+            "larger": larger}
 
 
 def run_heisenberg(V, torch, args):

@@ -36,8 +36,8 @@ def test_wolff_steps_bit_exact(V, O, cell, ext, pbc, T):
         assert eng.info().sweep_index == n
 
 
-# beyond one block's shared memory (16,384 sites): the multi-block kernel
-GRID_CASES = [
+# beyond 16,384 sites: spins and cluster marks as bits in one block
+MID_CASES = [
     ("sc", (32, 32, 32), (1, 1, 1)),
     ("sc", (256, 256, 1), (1, 1, 0)),
     ("sc", (64, 2, 256), (1, 1, 1)),   # repeated bonds along y
@@ -46,12 +46,16 @@ GRID_CASES = [
 ]
 
 
-@pytest.mark.parametrize("cell,ext,pbc", GRID_CASES)
-@pytest.mark.parametrize("T", [8.0, 4.5, 2.0])
-def test_wolff_grid_steps_bit_exact(V, O, cell, ext, pbc, T):
-    seed, J, n = 9, 1.0, 60
+# beyond 786,432 sites: the multi-block kernel (grid barrier per level)
+GRID_CASES = [
+    ("sc", (96, 96, 96), (1, 1, 1)),
+    ("fcc", (60, 60, 60), (1, 1, 0)),
+]
+
+
+def _wolff_bit_exact(V, O, cell, ext, pbc, T, n):
+    seed, J = 9, 1.0
     lat = getattr(V.Lattice, cell)(*ext, pbc=tuple(bool(p) for p in pbc))
-    assert lat.n_sites > 16384
     g = O.Graph(O.lattice(cell, *ext, pbc))
     with V.Engine(lat, V.hamiltonian(V.Exchange(J)), seed=seed) as eng:
         eng.init_random()
@@ -66,6 +70,19 @@ def test_wolff_grid_steps_bit_exact(V, O, cell, ext, pbc, T):
         eng.wolff_steps(5, measure=False)
         ref2, _ = g.wolff_steps(ref, J, T, seed, n, 5)
         assert np.array_equal(eng.get_state(), ref2)
+    return lat.n_sites
+
+
+@pytest.mark.parametrize("cell,ext,pbc", MID_CASES)
+@pytest.mark.parametrize("T", [8.0, 4.5, 2.0])
+def test_wolff_mid_steps_bit_exact(V, O, cell, ext, pbc, T):
+    assert 16384 < _wolff_bit_exact(V, O, cell, ext, pbc, T, 60) <= 786432
+
+
+@pytest.mark.parametrize("cell,ext,pbc", GRID_CASES)
+@pytest.mark.parametrize("T", [4.5, 2.0])
+def test_wolff_grid_steps_bit_exact(V, O, cell, ext, pbc, T):
+    assert _wolff_bit_exact(V, O, cell, ext, pbc, T, 12) > 786432
 
 
 def test_wolff_then_metropolis_continue_one_stream(V, O):

@@ -376,7 +376,8 @@ bool sc_layout(const vg_ctx* c) { return c->path == VG_PATH_STRUCTURED || c->pat
 bool fp64(const vg_ctx* c) { return c->opt.precision == VG_FP64; }
 size_t real_size(const vg_ctx* c) { return fp64(c) ? 8 : 4; }
 
-constexpr int64_t kWolffMaxSites = 16384;  // up to here one block's shared memory holds the Wolff state
+constexpr int64_t kWolffMaxSites = 16384;    // up to here one block holds the Wolff state as bytes and stamps
+constexpr int64_t kWolffMidSites = 786432;   // up to here one block holds spins and marks as bits
 
 int dalloc(vg_ctx* c, void** p, size_t bytes) {
   if (bytes == 0) bytes = 16;
@@ -1399,10 +1400,11 @@ int vg_wolff_steps(vg_ctx* c, uint64_t n, int32_t measure, double* E, double* M)
   VG_CUDA(c, cudaSetDevice(c->device));
   int rc;
   if ((rc = ensure_natural_nbr(c))) return rc;
-  const bool grid = c->n > kWolffMaxSites;
+  const bool mid = c->n > kWolffMaxSites && c->n <= kWolffMidSites;
+  const bool grid = c->n > kWolffMidSites;
+  if ((mid || grid) && !c->d_wq && (rc = dalloc(c, (void**)&c->d_wq, sizeof(int32_t) * (size_t)c->n))) return rc;
   if (grid && !c->d_wgrid) {
     if ((rc = dalloc(c, (void**)&c->d_wmark, sizeof(uint32_t) * (size_t)c->n))) return rc;
-    if ((rc = dalloc(c, (void**)&c->d_wq, sizeof(int32_t) * (size_t)c->n))) return rc;
     if ((rc = dalloc(c, (void**)&c->d_wgrid, sizeof(WolffGrid)))) return rc;
   }
   // bond probability 1 - exp(-2 J / T) as a threshold on a 32-bit word (src/integrator.rs:199-203)
@@ -1426,12 +1428,14 @@ int vg_wolff_steps(vg_ctx* c, uint64_t n, int32_t measure, double* E, double* M)
   for (uint64_t t0 = 0; t0 < n; t0 += (1u << 30)) {
     const uint32_t k = (uint32_t)std::min<uint64_t>(n - t0, 1u << 30);
     double* sums = measure ? c->d_sums + t0 * kNumSums : nullptr;
+    const RngKey key = rng_key(c, c->sweep + t0);
     const cudaError_t e =
-        grid ? launch_ising_wolff_grid((int8_t*)c->d_stage, (int)c->n, c->z, c->d_wnbr, c->d_wocc, thr,
-                                       rng_key(c, c->sweep + t0), k, sums, c->d_wmark, c->d_wq, c->d_wgrid,
-                                       c->sm_count, c->stream)
-             : launch_ising_wolff((int8_t*)c->d_stage, (int)c->n, c->z, c->d_wnbr, c->d_wocc, thr,
-                                  rng_key(c, c->sweep + t0), k, sums, c->stream);
+        grid ? launch_ising_wolff_grid((int8_t*)c->d_stage, (int)c->n, c->z, c->d_wnbr, c->d_wocc, thr, key, k, sums,
+                                       c->d_wmark, c->d_wq, c->d_wgrid, c->sm_count, c->stream)
+        : mid ? launch_ising_wolff_mid((int8_t*)c->d_stage, (int)c->n, c->z, c->d_wnbr, c->d_wocc, thr, key, k, sums,
+                                       c->d_wq, c->stream)
+              : launch_ising_wolff((int8_t*)c->d_stage, (int)c->n, c->z, c->d_wnbr, c->d_wocc, thr, key, k, sums,
+                                   c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "Wolff kernel launch");
     if (grid) {  // a grid barrier that gave up leaves the flag set
       unsigned int aborted = 0;

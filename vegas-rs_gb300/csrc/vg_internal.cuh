@@ -167,6 +167,13 @@ cudaError_t launch_ising_sc(const IsingScArgs& a, const IsingTable& tab, RngKey 
 int ising_sc_blocks_per_sm(const IsingScArgs& a, const IsingTable& tab, int tpb);
 // Wolff cluster steps on natural-order int8 +-1 spins, one block.
 size_t ising_wolff_smem(int n);
+// The same steps in one block for lattices whose spins and cluster marks fit
+// its shared memory as bits (ising_wolff_mid_smem(n) bytes); q: the cluster
+// queue in global memory, n entries.
+size_t ising_wolff_mid_smem(int n);
+cudaError_t launch_ising_wolff_mid(int8_t* spins, int n, int z, const int32_t* nbr, const uint8_t* occ,
+                                   unsigned long long thr, RngKey key, uint32_t n_steps, double* sums, int32_t* q,
+                                   cudaStream_t s);
 // The same steps over the whole grid (one cooperative launch) for lattices
 // beyond one block: spins, stamps (mark, n words) and queue (q, n entries)
 // in global memory; g is zeroed by the launcher, and g->abort_flag != 0

@@ -332,6 +332,131 @@ __global__ void __launch_bounds__(kWolffGridTpb) ising_wolff_grid_kernel(
   }
 }
 
+// ------------------------------------------------------------ mid-size
+// Lattices beyond 16,384 sites whose spins and cluster marks fit one block's
+// shared memory as bits (a quarter byte per site): the same steps in one
+// block, the queue in global memory (written and read by this block only),
+// a block barrier per level.  One SM's bond draws against a grid barrier per
+// level: near T_c the levels, not the draws, set the time of a step.
+__global__ void __launch_bounds__(1024) ising_wolff_mid_kernel(int8_t* __restrict__ spins, int n, int z,
+                                                               const int32_t* __restrict__ nbr,
+                                                               const uint8_t* __restrict__ occ,
+                                                               unsigned long long thr, RngKey key, uint32_t n_steps,
+                                                               double* __restrict__ sums, int32_t* __restrict__ q) {
+  extern __shared__ uint32_t s_bits[];
+  const int nw = (n + 31) >> 5;
+  uint32_t* up = s_bits;        // bit i: site i is up
+  uint32_t* in = s_bits + nw;   // bit i: site i is in this step's cluster
+  __shared__ int s_cnt[3];
+  __shared__ int s_red[2][32];
+  __shared__ int s_cut;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int w = threadIdx.x; w < nw; w += blockDim.x) {
+    uint32_t b = 0;
+    for (int i = 0; i < 32 && 32 * w + i < n; ++i) b |= (uint32_t)(spins[32 * w + i] > 0) << i;
+    up[w] = b;
+    in[w] = 0u;
+  }
+  if (threadIdx.x < 3) s_cnt[threadIdx.x] = 0;
+  if (threadIdx.x == 0) s_cut = 0;
+  __syncthreads();
+  auto spin_of = [&](int i) { return (int)((up[i >> 5] >> (i & 31)) & 1u) * 2 - 1; };
+  long long bond = 0, ups = 0;
+  if (sums) {  // the bond sum and up count of the incoming state, once per call
+    int b = 0, u = 0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      const int si = spin_of(i);
+      u += si > 0;
+      for (int k = 0; k < z; ++k) {
+        const int j = __ldg(nbr + (size_t)i * z + k);
+        if (j > i) b += si * spin_of(j);
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      b += __shfl_down_sync(0xffffffffu, b, o);
+      u += __shfl_down_sync(0xffffffffu, u, o);
+    }
+    if (lane == 0) {
+      s_red[0][warp] = b;
+      s_red[1][warp] = u;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+        bond += s_red[0][w];
+        ups += s_red[1][w];
+      }
+  }
+  for (uint32_t t = 0; t < n_steps; ++t) {
+    const uint32_t step = key.sweep + t;
+    const uint4 w0 = philox_ks(make_uint4(step, 0u, kTagWolffSource << 24, key.replica), key.ks);
+    const int src = (int)(((unsigned long long)w0.x * (unsigned long long)n) >> 32);
+    const int ref = spin_of(src);
+    if (threadIdx.x == 0) {
+      q[0] = src;
+      atomicOr(&in[src >> 5], 1u << (src & 31));
+    }
+    int lo = 0, hi = 1, lev = 0;
+    for (;;) {
+      const int items = (hi - lo) * z;
+      int* cnt = &s_cnt[lev % 3];
+      for (int e = threadIdx.x; e < items; e += blockDim.x) {
+        const int fi = e / z, k = e - fi * z;
+        const int site = lo == 0 ? src : q[lo + fi];
+        const int j = __ldg(nbr + (size_t)site * z + k);
+        if (j < 0 || spin_of(j) != ref || ((in[j >> 5] >> (j & 31)) & 1u)) continue;
+        const uint32_t a = (uint32_t)min(site, j), b = (uint32_t)max(site, j);
+        const uint32_t o = __ldg(occ + (size_t)site * z + k);
+        const uint4 w = philox_ks(make_uint4(a, b, (kTagWolffBond << 24) | (o << 20) | (key.replica & 0xFFFFFu), step),
+                                  key.ks);
+        if ((unsigned long long)w.x >= thr) continue;
+        const uint32_t bit = 1u << (j & 31);
+        if (!(atomicOr(&in[j >> 5], bit) & bit)) q[hi + atomicAdd(cnt, 1)] = j;
+      }
+      __syncthreads();
+      const int added = *cnt;
+      if (threadIdx.x == 0) s_cnt[(lev + 2) % 3] = 0;
+      if (added == 0) break;
+      lo = hi;
+      hi += added;
+      ++lev;
+    }
+    // flip the cluster and sum the spins across its boundary
+    int cut = 0;
+    for (int e = threadIdx.x; e < hi * z; e += blockDim.x) {
+      const int fi = e / z, k = e - fi * z;
+      const int site = q[fi];
+      const int j = __ldg(nbr + (size_t)site * z + k);
+      if (j >= 0 && !((in[j >> 5] >> (j & 31)) & 1u)) cut += spin_of(j);
+      if (k == 0) atomicXor(&up[site >> 5], 1u << (site & 31));
+    }
+    if (sums) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) cut += __shfl_down_sync(0xffffffffu, cut, o);
+      if (lane == 0 && cut) atomicAdd(&s_cut, cut);
+    }
+    __syncthreads();
+    // clear the cluster marks for the next step
+    for (int i = threadIdx.x; i < hi; i += blockDim.x) {
+      const int site = q[i];
+      atomicAnd(&in[site >> 5], ~(1u << (site & 31)));
+    }
+    if (sums && threadIdx.x == 0) {
+      bond -= 2ll * ref * s_cut;
+      ups += ref > 0 ? -(long long)hi : (long long)hi;
+      s_cut = 0;
+      double* out = sums + (size_t)t * kNumSums;
+      out[0] = (double)bond;
+      out[1] = out[2] = out[3] = out[4] = out[5] = 0.0;
+      out[6] = (double)ups;
+      out[7] = (double)hi;
+    }
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < n; i += blockDim.x) spins[i] = (int8_t)spin_of(i);
+}
+
 }  // namespace
 
 size_t ising_wolff_smem(int n) { return (size_t)n * 9; }
@@ -349,6 +474,19 @@ cudaError_t launch_ising_wolff_grid(int8_t* spins, int n, int z, const int32_t* 
   if ((e = cudaMemsetAsync(g, 0, sizeof(WolffGrid), s)) != cudaSuccess) return e;
   void* args[] = {&spins, &n, &z, &nbr, &occ, &thr, &key, &n_steps, &sums, &mark, &q, &g};
   return cudaLaunchCooperativeKernel((const void*)ising_wolff_grid_kernel, grid, block, args, 0, s);
+}
+
+size_t ising_wolff_mid_smem(int n) { return (size_t)((n + 31) / 32) * 8; }
+
+cudaError_t launch_ising_wolff_mid(int8_t* spins, int n, int z, const int32_t* nbr, const uint8_t* occ,
+                                   unsigned long long thr, RngKey key, uint32_t n_steps, double* sums, int32_t* q,
+                                   cudaStream_t s) {
+  const size_t smem = ising_wolff_mid_smem(n);
+  cudaError_t e =
+      cudaFuncSetAttribute(ising_wolff_mid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  ising_wolff_mid_kernel<<<1, 1024, smem, s>>>(spins, n, z, nbr, occ, thr, key, n_steps, sums, q);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_ising_wolff(int8_t* spins, int n, int z, const int32_t* nbr, const uint8_t* occ,
