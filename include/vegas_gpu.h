@@ -187,7 +187,8 @@ int vg_time_passes(vg_ctx* ctx, uint64_t n, int32_t measure, double* mean_pass_m
  * not used, as in the reference) and flips it.  Per step, E and |M| as
  * vg_sweeps; vg_sums.accepted of vg_current_sums-style rows is the cluster
  * size.  A step advances the context's sweep index by one.  Lattices of up
- * to 16384 sites run in one thread block's shared memory; larger ones in one
+ * to 786432 sites run in one thread block's shared memory (spins and marks
+ * as bytes up to 16384 sites, as bits beyond); larger ones in one
  * cooperative launch over the whole grid (a grid barrier per breadth-first
  * level; VG_ERR_TIMEOUT if one ever waits more than 2 s).  The uniform
  * exchange constant only (no per-bond constants). */
