@@ -107,19 +107,22 @@ __device__ __forceinline__ void msc_anti(const MscSeg& sg, int C, uint32_t j, ui
   const int z = (int)fdiv((uint32_t)row, sg.fLy);
   const int y = row - z * sg.Ly;
   const int p = (y + z + C) & 1;
+  // 32-bit word offsets (a class holds fewer than 2^31 words): no wide
+  // multiplies beside Philox's
   const int rb = row * sg.Hx;
+  const int plane = sg.Ly * sg.Hx;
   const int hx = p ? (h + 1 == sg.Hx ? 0 : h + 1) : (h == 0 ? sg.Hx - 1 : h - 1);
-  const int ym = y == 0 ? row + sg.Ly - 1 : row - 1;
-  const int yp = y == sg.Ly - 1 ? row - (sg.Ly - 1) : row + 1;
-  a[0] = s ^ __ldg(oth + rb + h);
-  a[1] = s ^ __ldg(oth + rb + hx);
-  a[2] = s ^ __ldg(oth + (size_t)ym * sg.Hx + h);
-  a[3] = s ^ __ldg(oth + (size_t)yp * sg.Hx + h);
+  const int oym = y == 0 ? rb + plane - sg.Hx : rb - sg.Hx;
+  const int oyp = y == sg.Ly - 1 ? rb - plane + sg.Hx : rb + sg.Hx;
+  a[0] = s ^ __ldg(oth + (uint32_t)(rb + h));
+  a[1] = s ^ __ldg(oth + (uint32_t)(rb + hx));
+  a[2] = s ^ __ldg(oth + (uint32_t)(oym + h));
+  a[3] = s ^ __ldg(oth + (uint32_t)(oyp + h));
   if (sg.dim3) {
-    const int zm = z == 0 ? row + (sg.Lz - 1) * sg.Ly : row - sg.Ly;
-    const int zp = z == sg.Lz - 1 ? row - (sg.Lz - 1) * sg.Ly : row + sg.Ly;
-    a[4] = s ^ __ldg(oth + (size_t)zm * sg.Hx + h);
-    a[5] = s ^ __ldg(oth + (size_t)zp * sg.Hx + h);
+    const int ozm = z == 0 ? rb + (sg.Lz - 1) * plane : rb - plane;
+    const int ozp = z == sg.Lz - 1 ? rb - (sg.Lz - 1) * plane : rb + plane;
+    a[4] = s ^ __ldg(oth + (uint32_t)(ozm + h));
+    a[5] = s ^ __ldg(oth + (uint32_t)(ozp + h));
   } else {
     a[4] = a[5] = 0u;
   }
