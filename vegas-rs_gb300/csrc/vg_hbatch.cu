@@ -148,10 +148,10 @@ __device__ __forceinline__ void add_class(const HbArgs<R>& a, const R* rep_base,
     for (int iy = 0; iy < (Dy ? 2 : 1); ++iy) {
       if (iy && !nb.yok) continue;
       const int yy = iy ? nb.ys : y;
-      const size_t row = ((size_t)zz * a.ny + yy) * a.nx;
+      const uint32_t row = ((uint32_t)zz * (uint32_t)a.ny + (uint32_t)yy) * (uint32_t)a.nx;  // < ncell < 2^32
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        const R* pl = rep_base + (size_t)(Q * 3 + c) * a.ncell;
+        const R* pl = rep_base + (uint32_t)(Q * 3 + c) * a.ncell;  // a replica holds < 2^32 values
         const Run<R, W> v = load_run<R, W>(pl + row + x0);
 #pragma unroll
         for (int k = 0; k < W; ++k) acc[c].v[k] += v.v[k];
@@ -715,6 +715,8 @@ int vg_hbatch_create(const vg_hbatch_desc* d, const vg_heis_replica* reps, int32
   const int nb = L.cell == VG_CELL_BCC ? 2 : 4;
   const double ncell = (double)L.nx * L.ny * L.nz;
   if (ncell * nb > 2147483647.0) return hfail(nullptr, VG_ERR_UNSUPPORTED, "lattice has more than 2^31-1 sites");
+  if (3.0 * ncell * nb >= 4294967296.0)  // 32-bit offsets within a replica
+    return hfail(nullptr, VG_ERR_UNSUPPORTED, "a replica holds more than 2^32 spin components");
   for (int k = 0; k < 3; ++k)
     if (!std::isfinite(d->anisotropy_axis[k]) || !std::isfinite(d->field_axis[k]))
       return hfail(nullptr, VG_ERR_INVALID_ARG, "axes must be finite");
