@@ -545,6 +545,7 @@ IsingScArgs ising_sc_args(const vg_ctx* c) {
   a.pbz = c->lat.pbc_z != 0;
   a.fG = make_fastdiv((uint32_t)a.G);
   a.fLy = make_fastdiv((uint32_t)a.Ly);
+  set_sc_offsets(a);
   return a;
 }
 
@@ -949,7 +950,8 @@ int vg_ctx_create_ex(const vg_lattice_desc* lat, const vg_hamiltonian_desc* ham,
   // x extent and even extents on every periodic axis (so that the
   // checkerboard is the greedy colouring); Ising also needs x/2 to be a
   // multiple of 16 (one uint4 per 16-site group).
-  const bool sc_ok = g.cell == VG_CELL_SC && lat->nx % 2 == 0 && (!lat->pbc_y || lat->ny % 2 == 0) &&
+  const bool sc_ok = g.cell == VG_CELL_SC && g.n / 2 <= (int64_t)INT32_MAX && lat->nx % 2 == 0 &&
+                     (!lat->pbc_y || lat->ny % 2 == 0) &&
                      (!lat->pbc_z || lat->nz % 2 == 0) &&
                      (opt->spin_kind != VG_SPIN_ISING || (lat->nx / 2) % kIsingGroup == 0);
   if (opt->path == VG_PATH_STRUCTURED && !sc_ok) {

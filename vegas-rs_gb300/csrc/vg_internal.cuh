@@ -114,7 +114,17 @@ struct IsingScArgs {          // sc checkerboard, class-separated uint8 0/1
   int Hx, Ly, Lz, G;          // Hx = Lx/2, G = Hx/16
   int pbx, pby, pbz;
   FastDiv fG, fLy;
+  // byte offsets within a class (a class holds fewer than 2^31 sites): a
+  // z plane, and the wrap-around jumps along y and z
+  uint32_t plane, ywrap, zwrap;
 };
+
+// The offsets of IsingScArgs from its extents (set after Hx, Ly, Lz).
+inline void set_sc_offsets(IsingScArgs& a) {
+  a.plane = (uint32_t)a.Ly * (uint32_t)a.Hx;
+  a.ywrap = (uint32_t)(a.Ly - 1) * (uint32_t)a.Hx;
+  a.zwrap = (uint32_t)(a.Lz - 1) * a.plane;
+}
 
 struct IsingGenArgs {         // any lattice: natural order uint8 0/1 + ELL
   uint8_t* spin;

@@ -258,10 +258,10 @@ __device__ __forceinline__ void sc1_range(const IsingScArgs& a, const IsingTable
       const int rzm = z > 0 ? row - a.Ly : (a.pbz ? row + (a.Lz - 1) * a.Ly : -1);
       const int rzp = z < a.Lz - 1 ? row + a.Ly : (a.pbz ? row - (a.Lz - 1) * a.Ly : -1);
       const uint4 zero4 = make_uint4(0, 0, 0, 0);
-      const uint4 Ym = rym >= 0 ? __ldg(reinterpret_cast<const uint4*>(oth + (size_t)rym * a.Hx + h0)) : zero4;
-      const uint4 Yp = ryp >= 0 ? __ldg(reinterpret_cast<const uint4*>(oth + (size_t)ryp * a.Hx + h0)) : zero4;
-      const uint4 Zm = rzm >= 0 ? __ldg(reinterpret_cast<const uint4*>(oth + (size_t)rzm * a.Hx + h0)) : zero4;
-      const uint4 Zp = rzp >= 0 ? __ldg(reinterpret_cast<const uint4*>(oth + (size_t)rzp * a.Hx + h0)) : zero4;
+      const uint4 Ym = rym >= 0 ? __ldg(reinterpret_cast<const uint4*>(oth + (uint32_t)rym * (uint32_t)a.Hx + h0)) : zero4;
+      const uint4 Yp = ryp >= 0 ? __ldg(reinterpret_cast<const uint4*>(oth + (uint32_t)ryp * (uint32_t)a.Hx + h0)) : zero4;
+      const uint4 Zm = rzm >= 0 ? __ldg(reinterpret_cast<const uint4*>(oth + (uint32_t)rzm * (uint32_t)a.Hx + h0)) : zero4;
+      const uint4 Zp = rzp >= 0 ? __ldg(reinterpret_cast<const uint4*>(oth + (uint32_t)rzp * (uint32_t)a.Hx + h0)) : zero4;
 
       S[0] = Sv.x;
       S[1] = Sv.y;
@@ -458,7 +458,7 @@ __device__ __forceinline__ void sc2_range(const IsingScArgs& a, const FastDiv& f
       const int z = (int)fdiv((uint32_t)row, a.fLy);
       const int y = row - z * a.Ly;
       const int p = (y + z + C) & 1;
-      const size_t rb = (size_t)row * a.Hx;
+      const uint32_t rb = (uint32_t)row * (uint32_t)a.Hx;  // 32-bit: no wide multiply beside Philox's
 
       const uint4 Sa = *reinterpret_cast<const uint4*>(own + rb + h0);
       const uint4 Sb = *reinterpret_cast<const uint4*>(own + rb + h0 + 16);
@@ -483,13 +483,12 @@ __device__ __forceinline__ void sc2_range(const IsingScArgs& a, const FastDiv& f
         for (int i = 0; i < 7; ++i) X1[i] = __byte_perm(X0[i], X0[i + 1], 0x4321);
         X1[7] = __byte_perm(X0[7], e, 0x4321);
       }
-      const size_t plane = (size_t)a.Ly * a.Hx;
-      size_t oym, oyp, ozm, ozp;  // neighbour row offsets
+      uint32_t oym, oyp, ozm, ozp;  // neighbour row offsets
       bool hym = true, hyp = true, hzm = true, hzp = true;
-      oym = y > 0 ? rb - a.Hx : rb + (size_t)(a.Ly - 1) * a.Hx;
-      oyp = y < a.Ly - 1 ? rb + a.Hx : rb - (size_t)(a.Ly - 1) * a.Hx;
-      ozm = z > 0 ? rb - plane : rb + (size_t)(a.Lz - 1) * plane;
-      ozp = z < a.Lz - 1 ? rb + plane : rb - (size_t)(a.Lz - 1) * plane;
+      oym = y > 0 ? rb - (uint32_t)a.Hx : rb + a.ywrap;
+      oyp = y < a.Ly - 1 ? rb + (uint32_t)a.Hx : rb - a.ywrap;
+      ozm = z > 0 ? rb - a.plane : rb + a.zwrap;
+      ozp = z < a.Lz - 1 ? rb + a.plane : rb - a.zwrap;
       if (!ALLPER) {
         hym = y > 0 || a.pby;
         hyp = y < a.Ly - 1 || a.pby;
@@ -497,7 +496,7 @@ __device__ __forceinline__ void sc2_range(const IsingScArgs& a, const FastDiv& f
         hzp = z < a.Lz - 1 || a.pbz;
       }
       const uint4 zero4 = make_uint4(0, 0, 0, 0);
-      auto ld2 = [&](bool has, size_t off, uint32_t (&v)[8]) {
+      auto ld2 = [&](bool has, uint32_t off, uint32_t (&v)[8]) {
         const uint4 u0 = has ? __ldg(reinterpret_cast<const uint4*>(oth + off + h0)) : zero4;
         const uint4 u1 = has ? __ldg(reinterpret_cast<const uint4*>(oth + off + h0 + 16)) : zero4;
         v[0] = u0.x; v[1] = u0.y; v[2] = u0.z; v[3] = u0.w;

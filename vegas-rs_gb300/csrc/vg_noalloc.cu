@@ -176,6 +176,7 @@ extern "C" int vg_ising_sc_sweeps_noalloc(const vg_lattice_desc* L, double excha
   a.pbz = L->pbc_z != 0;
   a.fG = make_fastdiv((uint32_t)a.G);
   a.fLy = make_fastdiv((uint32_t)a.Ly);
+  set_sc_offsets(a);
   const int tpb = 256;
   const long long want = ((long long)a.groups + tpb - 1) / tpb;
   const int grid = (int)std::max(1LL, std::min(want, (long long)sms * 8));
