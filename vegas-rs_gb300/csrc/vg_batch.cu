@@ -54,6 +54,7 @@ struct MscSeg {          // one replica word of one group
   int nd;                // drawing categories (dE > 0)
   int dn[4];             // their anti-aligned counts
   int rep0;              // global index of lane 0
+  int plane, zwrap;      // words per z plane, (Lz - 1) planes
 };
 
 struct MscGroupDev {
@@ -110,7 +111,7 @@ __device__ __forceinline__ void msc_anti(const MscSeg& sg, int C, uint32_t j, ui
   // 32-bit word offsets (a class holds fewer than 2^31 words): no wide
   // multiplies beside Philox's
   const int rb = row * sg.Hx;
-  const int plane = sg.Ly * sg.Hx;
+  const int plane = sg.plane;
   const int hx = p ? (h + 1 == sg.Hx ? 0 : h + 1) : (h == 0 ? sg.Hx - 1 : h - 1);
   const int oym = y == 0 ? rb + plane - sg.Hx : rb - sg.Hx;
   const int oyp = y == sg.Ly - 1 ? rb - plane + sg.Hx : rb + sg.Hx;
@@ -119,8 +120,8 @@ __device__ __forceinline__ void msc_anti(const MscSeg& sg, int C, uint32_t j, ui
   a[2] = s ^ __ldg(oth + (uint32_t)(oym + h));
   a[3] = s ^ __ldg(oth + (uint32_t)(oyp + h));
   if (sg.dim3) {
-    const int ozm = z == 0 ? rb + (sg.Lz - 1) * plane : rb - plane;
-    const int ozp = z == sg.Lz - 1 ? rb - (sg.Lz - 1) * plane : rb + plane;
+    const int ozm = z == 0 ? rb + sg.zwrap : rb - plane;
+    const int ozp = z == sg.Lz - 1 ? rb - sg.zwrap : rb + plane;
     a[4] = s ^ __ldg(oth + (uint32_t)(ozm + h));
     a[5] = s ^ __ldg(oth + (uint32_t)(ozp + h));
   } else {
@@ -759,6 +760,8 @@ int vg_batch_create(const vg_replica_group* groups, int32_t n_groups, double J, 
       s.dim3 = G.z == 6;
       s.fHx = make_fastdiv((uint32_t)s.Hx);
       s.fLy = make_fastdiv((uint32_t)s.Ly);
+      s.plane = s.Ly * s.Hx;
+      s.zwrap = (s.Lz - 1) * s.plane;
       s.fLx = make_fastdiv((uint32_t)G.lat.nx);
       s.word_id = (uint32_t)b->segs.size();
       s.group = (int)(&G - &b->groups[0]);
