@@ -561,25 +561,25 @@ __device__ __forceinline__ void sc2_range(const IsingScArgs& a, const FastDiv& f
       if (MEASURE) {
         // byte-wise sums over the eight words stay below 256 (Sn and F bytes
         // are 0/1, M bytes at most 2 Z), then one byte dot product each
-        uint32_t su = 0, sf = 0;
+        // byte sums as dot products: the ALU pipe is the busier one here
+        unsigned su = 0, sf = 0;
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
-          su += Sn[i];
-          sf += F[i];
+          su = __dp4a(Sn[i], 0x01010101u, su);
+          sf = __dp4a(F[i], 0x01010101u, sf);
         }
-        const int u = (int)__dp4a(su, 0x01010101u, 0u);
+        const int u = (int)su;
         ups += u;
-        nacc += (int)__dp4a(sf, 0x01010101u, 0u);
+        nacc += (int)sf;
         if (C == 1) {  // every neighbour of class 1 has the lower colour: all bonds counted here
-          unsigned sm = 0;
-          uint32_t sM = 0;
+          unsigned sm = 0, m = 0;
 #pragma unroll
           for (int i = 0; i < 8; ++i) {
             const uint32_t M = 2u * A[i] + zoff;  // neighbour sum + Z per byte
             sm = __dp4a(Sn[i], M, sm);
-            sM += M;
+            m = __dp4a(M, 0x01010101u, m);
           }
-          bond += 2 * (int)sm - (int)__dp4a(sM, 0x01010101u, 0u) - Z * (2 * u - 32);
+          bond += 2 * (int)sm - (int)m - Z * (2 * u - 32);
         }
       }
     }
