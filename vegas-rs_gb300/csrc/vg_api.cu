@@ -757,6 +757,9 @@ int validate_ham(const vg_hamiltonian_desc* h, std::string* why) {
 }
 
 int setup_generic(vg_ctx* c, const Geometry& g) {
+  // the kernels index a class's neighbour table [z][n_c] with 32-bit offsets
+  if ((int64_t)g.z * g.n >= (int64_t)UINT32_MAX)
+    return fail(c, VG_ERR_UNSUPPORTED, "the generic path needs n_sites x coordination < 2^32");
   std::vector<int32_t> nbr, col;
   build_neighbours(g, nbr);
   c->ncol = greedy_colouring(g, nbr, col);
@@ -1001,7 +1004,8 @@ int vg_ctx_create_ex(const vg_lattice_desc* lat, const vg_hamiltonian_desc* ham,
   long long items = 0;
   for (int k = 0; k < c->ncol; ++k) {
     const long long nc = c->class_size[k];
-    items = std::max(items, is_ising(c) ? (nc + 15) / 16 : nc);
+    // the structured Ising kernels take 16-site groups, every other kernel one entry per thread
+    items = std::max(items, is_ising(c) && sc_layout(c) ? (nc + 15) / 16 : nc);
   }
   c->grid = launch_grid(c, items);
   if (is_ising(c) && sc_layout(c) && opt->blocks_per_sm <= 0) {

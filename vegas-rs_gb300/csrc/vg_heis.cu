@@ -210,9 +210,9 @@ __global__ void __launch_bounds__(256) heis_gen_kernel(const HeisGenArgs<R> a, c
 #pragma unroll
     for (int k = 0; k < ZT; ++k) {
       if (k < a.zc) {
-        const int t = __ldg(a.nbr + (long long)k * a.n_c + j);
+        const int t = __ldg(a.nbr + ((uint32_t)k * (uint32_t)a.n_c + (uint32_t)j));
         if (t >= 0) {
-          const R wk = a.jb ? __ldg(a.jb + (long long)k * a.n_c + j) : (R)1;
+          const R wk = a.jb ? __ldg(a.jb + ((uint32_t)k * (uint32_t)a.n_c + (uint32_t)j)) : (R)1;
           const R vx = wk * a.x[t], vy = wk * a.y[t], vz = wk * a.z[t];
           hs.x += vx;
           hs.y += vy;

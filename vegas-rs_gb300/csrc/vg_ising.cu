@@ -65,22 +65,6 @@ __device__ __forceinline__ uint32_t decide16(const unsigned long long (&t)[16], 
 __device__ __forceinline__ uint32_t spread4(uint32_t m) { return ((m & 0xFu) * 0x00204081u) & 0x01010101u; }
 __device__ __forceinline__ uint32_t gather4(uint32_t x) { return (((x & 0x01010101u) * 0x01020408u) >> 24) & 0xFu; }
 
-// Random +-1 proposal of IsingSpin::rand (src/state.rs:76-84): byte < 128
-// (u < 0.5) proposes Up.  Returns the mask of sites whose proposal differs.
-__device__ __forceinline__ uint32_t propose_random16(const uint32_t (&s)[4], const RngKey& key, uint32_t g,
-                                                     int colour) {
-  const uint4 b = philox_ks(make_uint4(g, key.sweep, (kTagIsingPropose << 24) | ((uint32_t)colour << 8), key.replica),
-                            key.ks);
-  const uint32_t w[4] = {b.x, b.y, b.z, b.w};
-  uint32_t diff = 0;
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const uint32_t up = (~w[i] >> 7) & 0x01010101u;
-    diff |= gather4(up ^ s[i]) << (4 * i);
-  }
-  return diff;
-}
-
 // ------------------------------------------------------------------ sc
 // Byte-parallel helpers: a 32-bit word carries 4 sites, one byte each.
 // PRMT selector from 4 bytes in [0, 7].
@@ -630,6 +614,51 @@ __global__ void __launch_bounds__(256, kSc2MinBlocks) ising_sc2_kernel(const Isi
 }
 
 // ------------------------------------------------------------- generic
+// One class entry per thread (entry j of the class: site sites[j]), so that a
+// class of a few hundred thousand sites still fills the GPU.  Entry j draws
+// byte (j & 15) of the blocks of group j >> 4, exactly as the 16-entry
+// kernels do: the sixteen lanes of a half warp compute their group's block
+// together (the same instructions, no extra issue).
+
+// Acceptance of "U < th" with the first digit ub0 already drawn; later
+// digits only on a tie (probability 1/256).
+__device__ __forceinline__ bool decide1(unsigned long long th, uint32_t ub0, const RngKey& key, uint32_t g, int k,
+                                        int colour) {
+  if (th >= (1ull << 32)) return true;
+  if (th == 0ull) return false;
+  uint32_t tb = ((uint32_t)th >> 24) & 0xFFu;
+  if (ub0 != tb) return ub0 < tb;
+  for (int d = 1; d < 4; ++d) {
+    const uint4 b = philox_ks(
+        make_uint4(g, key.sweep, (kTagIsingAccept << 24) | ((uint32_t)colour << 8) | (uint32_t)d, key.replica),
+        key.ks);
+    const uint32_t ub = blk_byte(b, k);
+    tb = ((uint32_t)th >> (24 - 8 * d)) & 0xFFu;
+    if (ub != tb) return ub < tb;
+  }
+  return false;  // U == th: not below the threshold
+}
+
+// The first-digit byte of entry j and, for random proposals, whether its
+// proposal differs from s (byte < 128 proposes Up).
+template <bool UPDATE, int PROP>
+__device__ __forceinline__ void draw1(const RngKey& key, uint32_t g, int k, int colour, uint32_t& ub0,
+                                      uint32_t& prop_up) {
+  ub0 = 0u;
+  prop_up = 0u;
+  if (!UPDATE) return;
+  ub0 = blk_byte(
+      philox_ks(make_uint4(g, key.sweep, (kTagIsingAccept << 24) | ((uint32_t)colour << 8), key.replica), key.ks),
+      k);
+  if (PROP == VG_PROPOSE_RANDOM)
+    prop_up = blk_byte(philox_ks(make_uint4(g, key.sweep, (kTagIsingPropose << 24) | ((uint32_t)colour << 8),
+                                            key.replica),
+                                 key.ks),
+                       k) < 128u
+                  ? 1u
+                  : 0u;
+}
+
 template <int ZT, bool MEASURE, bool UPDATE, int PROP>
 __global__ void __launch_bounds__(256) ising_gen_kernel(const IsingGenArgs a, const IsingTable tab, const RngKey key,
                                                         const int colour, long long* __restrict__ part) {
@@ -641,59 +670,37 @@ __global__ void __launch_bounds__(256) ising_gen_kernel(const IsingGenArgs a, co
   __syncthreads();
 
   long long bond = 0, ups = 0, nacc = 0;
-  const long long ngroups = (a.n_c + 15) >> 4;
   const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < ngroups; g += stride) {
-    const long long j0 = g << 4;
-    int site[16], nsum[16], nlow[16];
-    uint32_t S[4] = {0, 0, 0, 0}, valid = 0;
+  for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < a.n_c; j += stride) {
+    const uint32_t g = (uint32_t)(j >> 4);
+    const int k = (int)(j & 15);
+    uint32_t ub0, up;
+    draw1<UPDATE, PROP>(key, g, k, colour, ub0, up);
+    const int i = __ldg(a.sites + j);
+    const int s = a.spin[i];
+    const uint32_t lm = __ldg(a.lowmask + j);
+    int nsum = 0, nlow = 0;
 #pragma unroll
-    for (int k = 0; k < 16; ++k) {
-      const long long j = j0 + k;
-      site[k] = -1;
-      nsum[k] = 0;
-      nlow[k] = 0;
-      if (j < a.n_c) {
-        valid |= 1u << k;
-        const int i = __ldg(a.sites + j);
-        site[k] = i;
-        S[k >> 2] |= (uint32_t)a.spin[i] << (8 * (k & 3));
-        const uint32_t lm = __ldg(a.lowmask + j);
-#pragma unroll
-        for (int q = 0; q < ZT; ++q) {
-          if (q < z) {
-            const int t = __ldg(a.nbr + (long long)q * a.n_c + j);
-            if (t >= 0) {
-              const int v = 2 * (int)a.spin[t] - 1;
-              nsum[k] += v;
-              if ((lm >> q) & 1u) nlow[k] += v;
-            }
-          }
+    for (int q = 0; q < ZT; ++q) {
+      if (q < z) {
+        const int t = __ldg(a.nbr + ((uint32_t)q * (uint32_t)a.n_c + (uint32_t)j));
+        if (t >= 0) {
+          const int v = 2 * (int)a.spin[t] - 1;
+          nsum += v;
+          if ((lm >> q) & 1u) nlow += v;
         }
       }
     }
-    uint32_t flip = 0;
-    if (UPDATE) {
-      const uint32_t cand = (PROP == VG_PROPOSE_FLIP ? 0xFFFFu : propose_random16(S, key, (uint32_t)g, colour)) & valid;
-      unsigned long long t[16];
-#pragma unroll
-      for (int k = 0; k < 16; ++k) {
-        const int s = (S[k >> 2] >> (8 * (k & 3))) & 1;
-        t[k] = s_thr[s * Wz + nsum[k] + z];
-      }
-      flip = decide16(t, cand, key, (uint32_t)g, colour) & cand;
+    bool acc = false;
+    if (UPDATE && (PROP == VG_PROPOSE_FLIP || up != (uint32_t)s))
+      acc = decide1(s_thr[s * Wz + nsum + z], ub0, key, g, k, colour);
+    const int sn = s ^ (int)acc;
+    if (acc) a.spin[i] = (uint8_t)sn;
+    if (MEASURE) {
+      ups += sn;
+      bond += sn ? nlow : -nlow;
+      nacc += acc;
     }
-#pragma unroll
-    for (int k = 0; k < 16; ++k) {
-      const int s = (S[k >> 2] >> (8 * (k & 3))) & 1;
-      const int sn = s ^ (int)((flip >> k) & 1u);
-      if ((flip >> k) & 1u) a.spin[site[k]] = (uint8_t)sn;
-      if (MEASURE && ((valid >> k) & 1u)) {
-        ups += sn;
-        bond += sn ? nlow[k] : -nlow[k];
-      }
-    }
-    if (MEASURE) nacc += __popc(flip);
   }
   if (MEASURE) {
     long long v[kNumSums] = {bond, 0, 0, 0, 0, 0, ups, nacc};
@@ -713,67 +720,50 @@ __global__ void __launch_bounds__(256) ising_bond_kernel(const IsingGenArgs a, c
                                                          double* __restrict__ part) {
   double bond = 0.0, ups = 0.0, nacc = 0.0;
   const int z = a.z;
-  const long long ngroups = (a.n_c + 15) >> 4;
   const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < ngroups; g += stride) {
-    const long long j0 = g << 4;
-    int site[16];
-    double hlow[16];
-    unsigned long long t[16];
-    uint32_t S[4] = {0, 0, 0, 0}, valid = 0;
+  for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < a.n_c; j += stride) {
+    const uint32_t g = (uint32_t)(j >> 4);
+    const int k = (int)(j & 15);
+    uint32_t ub0, up;
+    draw1<UPDATE, PROP>(key, g, k, colour, ub0, up);
+    const int i = __ldg(a.sites + j);
+    const uint32_t s01 = a.spin[i];
+    const uint32_t lm = __ldg(a.lowmask + j);
+    double hj = 0.0, hlow = 0.0;
 #pragma unroll
-    for (int k = 0; k < 16; ++k) {
-      const long long j = j0 + k;
-      site[k] = -1;
-      hlow[k] = 0.0;
-      t[k] = 0;
-      if (j < a.n_c) {
-        valid |= 1u << k;
-        const int i = __ldg(a.sites + j);
-        site[k] = i;
-        const uint32_t s01 = a.spin[i];
-        S[k >> 2] |= s01 << (8 * (k & 3));
-        const uint32_t lm = __ldg(a.lowmask + j);
-        double hj = 0.0;
-#pragma unroll
-        for (int q = 0; q < ZT; ++q) {
-          if (q < z) {
-            const int nb = __ldg(a.nbr + (long long)q * a.n_c + j);
-            if (nb >= 0) {
-              const double v = __ldg(a.jb + (long long)q * a.n_c + j) * (double)(2 * (int)a.spin[nb] - 1);
-              hj += v;
-              if ((lm >> q) & 1u) hlow[k] += v;
-            }
-          }
-        }
-        const double sd = s01 ? 1.0 : -1.0;
-        const double e_old = -sd * hj + a.hz * sd;
-        const double e_new = -(-sd) * hj + a.hz * (-sd);
-        const double de = e_new - e_old;
-        if (de <= 0.0) {
-          t[k] = 1ull << 32;
-        } else {
-          const double x = ceil(exp(-de / a.T) * 4294967296.0);
-          t[k] = x >= 4294967296.0 ? (1ull << 32) : x <= 0.0 ? 0ull : (unsigned long long)x;
+    for (int q = 0; q < ZT; ++q) {
+      if (q < z) {
+        const uint32_t e = (uint32_t)q * (uint32_t)a.n_c + (uint32_t)j;
+        const int nb = __ldg(a.nbr + e);
+        if (nb >= 0) {
+          const double v = __ldg(a.jb + e) * (double)(2 * (int)a.spin[nb] - 1);
+          hj += v;
+          if ((lm >> q) & 1u) hlow += v;
         }
       }
     }
-    uint32_t flip = 0;
-    if (UPDATE) {
-      const uint32_t cand = (PROP == VG_PROPOSE_FLIP ? 0xFFFFu : propose_random16(S, key, (uint32_t)g, colour)) & valid;
-      flip = decide16(t, cand, key, (uint32_t)g, colour) & cand;
-    }
-#pragma unroll
-    for (int k = 0; k < 16; ++k) {
-      const int s = (S[k >> 2] >> (8 * (k & 3))) & 1;
-      const int sn = s ^ (int)((flip >> k) & 1u);
-      if ((flip >> k) & 1u) a.spin[site[k]] = (uint8_t)sn;
-      if (MEASURE && ((valid >> k) & 1u)) {
-        ups += (double)sn;
-        bond += sn ? hlow[k] : -hlow[k];
+    bool acc = false;
+    if (UPDATE && (PROP == VG_PROPOSE_FLIP || up != s01)) {
+      const double sd = s01 ? 1.0 : -1.0;
+      const double e_old = -sd * hj + a.hz * sd;
+      const double e_new = -(-sd) * hj + a.hz * (-sd);
+      const double de = e_new - e_old;
+      unsigned long long th;
+      if (de <= 0.0) {
+        th = 1ull << 32;
+      } else {
+        const double x = ceil(exp(-de / a.T) * 4294967296.0);
+        th = x >= 4294967296.0 ? (1ull << 32) : x <= 0.0 ? 0ull : (unsigned long long)x;
       }
+      acc = decide1(th, ub0, key, g, k, colour);
     }
-    if (MEASURE) nacc += (double)__popc(flip);
+    const int sn = (int)s01 ^ (int)acc;
+    if (acc) a.spin[i] = (uint8_t)sn;
+    if (MEASURE) {
+      ups += (double)sn;
+      bond += sn ? hlow : -hlow;
+      nacc += acc ? 1.0 : 0.0;
+    }
   }
   if (MEASURE) {
     double v[kNumSums] = {bond, 0.0, 0.0, 0.0, 0.0, 0.0, ups, nacc};
