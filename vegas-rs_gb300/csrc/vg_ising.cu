@@ -660,7 +660,7 @@ __device__ __forceinline__ void draw1(const RngKey& key, uint32_t g, int k, int 
 }
 
 template <int ZT, bool MEASURE, bool UPDATE, int PROP>
-__global__ void __launch_bounds__(256) ising_gen_kernel(const IsingGenArgs a, const IsingTable tab, const RngKey key,
+__global__ void __launch_bounds__(256, 4) ising_gen_kernel(const IsingGenArgs a, const IsingTable tab, const RngKey key,
                                                         const int colour, long long* __restrict__ part) {
   constexpr int W = 2 * ZT + 1;
   __shared__ unsigned long long s_thr[2 * W];
@@ -669,7 +669,7 @@ __global__ void __launch_bounds__(256) ising_gen_kernel(const IsingGenArgs a, co
   for (int i = threadIdx.x; i < 2 * Wz; i += blockDim.x) s_thr[i] = tab.thr[i];
   __syncthreads();
 
-  long long bond = 0, ups = 0, nacc = 0;
+  int bond = 0, ups = 0, nacc = 0;  // per thread: a few entries of at most +-z each
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < a.n_c; j += stride) {
     const uint32_t g = (uint32_t)(j >> 4);
@@ -702,10 +702,7 @@ __global__ void __launch_bounds__(256) ising_gen_kernel(const IsingGenArgs a, co
       nacc += acc;
     }
   }
-  if (MEASURE) {
-    long long v[kNumSums] = {bond, 0, 0, 0, 0, 0, ups, nacc};
-    block_sum_store(v, part + (long long)blockIdx.x * kNumSums);
-  }
+  if (MEASURE) block_sum3_store(bond, ups, nacc, part + (size_t)blockIdx.x * kNumSums);
 }
 
 // Per-bond exchange constants (Exchange's CSR with arbitrary J_ij,
