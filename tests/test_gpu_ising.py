@@ -20,7 +20,15 @@ CASES = [
     ("bcc", (3, 5, 2), (1, 0, 1), "generic"),
     ("fcc", (4, 4, 4), (1, 1, 1), "generic"),
     ("fcc", (3, 3, 3), (1, 1, 0), "generic"),
+    # bcc / fcc with x a multiple of 16: one array per sublattice, 16-cell runs
+    ("bcc", (16, 4, 4), (1, 1, 1), "structured"),
+    ("bcc", (16, 3, 2), (1, 0, 1), "structured"),   # open y
+    ("bcc", (32, 2, 1), (0, 1, 1), "structured"),   # open x; z of extent 1 (doubled bonds)
+    ("fcc", (16, 4, 4), (1, 1, 1), "structured"),
+    ("fcc", (16, 3, 3), (1, 1, 0), "structured"),   # open z
+    ("fcc", (32, 2, 5), (0, 1, 1), "structured"),   # open x
 ]
+SUB = CASES[14:]
 
 
 def _engine(V, cell, ext, pbc, ham, seed, **kw):
@@ -46,7 +54,7 @@ def test_flip_sweeps_bit_exact(V, O, cell, ext, pbc, path):
         np.testing.assert_array_equal(M, np.abs(obs[:, 1]).astype(float))
 
 
-@pytest.mark.parametrize("cell,ext,pbc,path", CASES[:2] + CASES[4:9])
+@pytest.mark.parametrize("cell,ext,pbc,path", CASES[:2] + CASES[4:9] + SUB)
 def test_random_proposal_and_field_bit_exact(V, O, cell, ext, pbc, path):
     """MetropolisIntegrator (random +-1 proposal) with Exchange + Zeeman, field Down."""
     seed, J, T, mag, n = 99, 0.7, 2.1, 0.35, 5
@@ -82,6 +90,34 @@ def test_all_paths_agree(V, ext, pbc, proposal):
     for o in out[1:]:
         assert np.array_equal(out[0][0], o[0])
         assert np.array_equal(out[0][1], o[1]) and np.array_equal(out[0][2], o[2])
+
+
+@pytest.mark.parametrize("proposal", [0, 1])
+@pytest.mark.parametrize("cell,ext,pbc", [(c, e, p) for c, e, p, _ in SUB])
+def test_sublattice_and_generic_paths_agree(V, cell, ext, pbc, proposal):
+    """bcc / fcc: the sublattice kernel and the ELL kernel give the same
+    states and per-sweep sums, including the measurement-only pass."""
+    H = V.hamiltonian(V.Exchange(0.8), V.Zeeman(), V.Gauge(0.1))
+    out = []
+    for path in (V.PATH_STRUCTURED, V.PATH_GENERIC):
+        with _engine(V, cell, ext, pbc, H, 21, path=path, proposal=proposal) as eng:
+            assert eng.info().path == path
+            eng.init_random()
+            eng.set_thermostat(3.7, (0, 0, -1), 0.3)
+            sums = eng.sweeps_sums(70)
+            out.append((eng.get_state(), sums, eng.total_energy(), eng.magnetization()[1]))
+    assert np.array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
+    assert out[0][2] == out[1][2] and out[0][3] == out[1][3]
+
+
+def test_sublattice_needs_x_multiple_of_16(V):
+    H = V.hamiltonian(V.Exchange(1.0))
+    with pytest.raises(V.VegasGpuError) as e:
+        _engine(V, "fcc", (24, 4, 4), (1, 1, 1), H, 1, path=V.PATH_STRUCTURED)
+    assert e.value.status == 5
+    with _engine(V, "fcc", (24, 4, 4), (1, 1, 1), H, 1) as eng:
+        assert eng.info().path == V.PATH_GENERIC
 
 
 def test_resume_from_sweep_index(V):

@@ -206,7 +206,12 @@ int greedy_colouring(const Geometry& g, const std::vector<int32_t>& nbr, std::ve
 struct ScMap {
   uint32_t Lx, Ly, Hx;
   FastDiv fLx, fLy;
+  int nbshift;       // sublattice layout: log2 of the basis size
+  long long ncell;   // sublattice layout: entries per class
 };
+
+// Layouts of the Ising class arrays: 0 natural order, 1 sc checkerboard
+// (two arrays), 2 bcc / fcc sublattices (one array, class q at q ncell).
 
 __device__ __forceinline__ void sc_locate(long long i, const ScMap& m, int& c, long long& j) {
   const uint32_t ii = (uint32_t)i;
@@ -216,57 +221,50 @@ __device__ __forceinline__ void sc_locate(long long i, const ScMap& m, int& c, l
   j = (long long)r * m.Hx + (x >> 1);
 }
 
-__global__ void ising_import(const int8_t* __restrict__ src, long long n, int structured, ScMap m, uint8_t* d0,
+__device__ __forceinline__ long long ising_offset(long long i, int layout, const ScMap& m, int& c) {
+  if (layout == 2) {
+    c = 0;
+    return (i & ((1ll << m.nbshift) - 1)) * m.ncell + (i >> m.nbshift);
+  }
+  c = 0;
+  if (layout == 0) return i;
+  long long j;
+  sc_locate(i, m, c, j);
+  return j;
+}
+
+__global__ void ising_import(const int8_t* __restrict__ src, long long n, int layout, ScMap m, uint8_t* d0,
                              uint8_t* d1, int* flag) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const int8_t v = src[i];
     if (v != 1 && v != -1) atomicOr(flag, 1);
-    const uint8_t b = v > 0 ? 1 : 0;
-    if (structured) {
-      int c;
-      long long j;
-      sc_locate(i, m, c, j);
-      (c ? d1 : d0)[j] = b;
-    } else {
-      d0[i] = b;
-    }
+    int c;
+    const long long j = ising_offset(i, layout, m, c);
+    (c ? d1 : d0)[j] = v > 0 ? 1 : 0;
   }
 }
 
-__global__ void ising_export(int8_t* __restrict__ dst, long long n, int structured, ScMap m, const uint8_t* d0,
+__global__ void ising_export(int8_t* __restrict__ dst, long long n, int layout, ScMap m, const uint8_t* d0,
                              const uint8_t* d1) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    uint8_t b;
-    if (structured) {
-      int c;
-      long long j;
-      sc_locate(i, m, c, j);
-      b = (c ? d1 : d0)[j];
-    } else {
-      b = d0[i];
-    }
-    dst[i] = b ? 1 : -1;
+    int c;
+    const long long j = ising_offset(i, layout, m, c);
+    dst[i] = (c ? d1 : d0)[j] ? 1 : -1;
   }
 }
 
 // State::rand_with_size for Ising (src/state.rs:260-262, :76-84): site i is
 // Up iff byte (i & 15) of the block (i >> 4, 0, tag) is < 128 (u < 0.5).
-__global__ void ising_init(long long n, int structured, ScMap m, uint8_t* d0, uint8_t* d1, RngKey key) {
+__global__ void ising_init(long long n, int layout, ScMap m, uint8_t* d0, uint8_t* d1, RngKey key) {
   const long long ng = (n + 15) >> 4;
   for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += (long long)gridDim.x * blockDim.x) {
     const uint4 b = philox(make_uint4((uint32_t)g, 0u, kTagInitIsing << 24, key.replica), key.k0, key.k1);
     for (int k = 0; k < 16; ++k) {
       const long long i = (g << 4) + k;
       if (i >= n) break;
-      const uint8_t up = blk_byte(b, k) < 128 ? 1 : 0;
-      if (structured) {
-        int c;
-        long long j;
-        sc_locate(i, m, c, j);
-        (c ? d1 : d0)[j] = up;
-      } else {
-        d0[i] = up;
-      }
+      int c;
+      const long long j = ising_offset(i, layout, m, c);
+      (c ? d1 : d0)[j] = blk_byte(b, k) < 128 ? 1 : 0;
     }
   }
 }
@@ -372,7 +370,12 @@ constexpr int kChunk = 64;  // sweeps per reduction launch
 
 bool is_ising(const vg_ctx* c) { return c->opt.spin_kind == VG_SPIN_ISING; }
 // the checkerboard class layout (structured grid kernels or the resident kernel)
-bool sc_layout(const vg_ctx* c) { return c->path == VG_PATH_STRUCTURED || c->path == VG_PATH_RESIDENT; }
+bool sc_layout(const vg_ctx* c) {
+  return (c->path == VG_PATH_STRUCTURED || c->path == VG_PATH_RESIDENT) && c->lat.cell == VG_CELL_SC;
+}
+// bcc / fcc Ising with one array per sublattice (the structured path of those cells)
+bool sub_layout(const vg_ctx* c) { return c->path == VG_PATH_STRUCTURED && c->lat.cell != VG_CELL_SC; }
+int ising_layout(const vg_ctx* c) { return sc_layout(c) ? 1 : sub_layout(c) ? 2 : 0; }
 bool fp64(const vg_ctx* c) { return c->opt.precision == VG_FP64; }
 size_t real_size(const vg_ctx* c) { return fp64(c) ? 8 : 4; }
 
@@ -396,7 +399,26 @@ ScMap sc_map(const vg_ctx* c) {
   m.Hx = (uint32_t)(c->lat.nx / 2);
   m.fLx = make_fastdiv(m.Lx);
   m.fLy = make_fastdiv(m.Ly);
+  m.nbshift = c->lat.cell == VG_CELL_FCC ? 2 : c->lat.cell == VG_CELL_BCC ? 1 : 0;
+  m.ncell = (long long)c->lat.nx * c->lat.ny * c->lat.nz;
   return m;
+}
+
+IsingSubArgs ising_sub_args(const vg_ctx* c) {
+  IsingSubArgs a;
+  a.base = (uint8_t*)c->spin[0][0];
+  a.nx = c->lat.nx;
+  a.ny = c->lat.ny;
+  a.nz = c->lat.nz;
+  a.ncell = (uint32_t)a.nx * (uint32_t)a.ny * (uint32_t)a.nz;
+  a.groups = a.ncell / 16u;
+  a.z = c->z;
+  a.pbx = c->lat.pbc_x != 0;
+  a.pby = c->lat.pbc_y != 0;
+  a.pbz = c->lat.pbc_z != 0;
+  a.fnx = make_fastdiv((uint32_t)a.nx);
+  a.fny = make_fastdiv((uint32_t)a.ny);
+  return a;
 }
 
 RngKey rng_key(const vg_ctx* c, uint64_t sweep) {
@@ -559,6 +581,9 @@ int launch_pass(vg_ctx* c, int colour, bool update, uint64_t sweep, void* part_r
     if (sc_layout(c)) {
       e = launch_ising_sc(ising_sc_args(c), tab, key, colour, c->opt.proposal, update, part, c->grid, c->tpb,
                           c->stream);
+    } else if (sub_layout(c)) {
+      e = launch_ising_sub(ising_sub_args(c), c->ncol, tab, key, colour, c->opt.proposal, update, part, c->grid,
+                           c->tpb, c->stream);
     } else {
       IsingGenArgs a;
       a.spin = (uint8_t*)c->spin[0][0];
@@ -957,9 +982,14 @@ int vg_ctx_create_ex(const vg_lattice_desc* lat, const vg_hamiltonian_desc* ham,
                      (!lat->pbc_y || lat->ny % 2 == 0) &&
                      (!lat->pbc_z || lat->nz % 2 == 0) &&
                      (opt->spin_kind != VG_SPIN_ISING || (lat->nx / 2) % kIsingGroup == 0);
-  if (opt->path == VG_PATH_STRUCTURED && !sc_ok) {
+  // bcc / fcc Ising: one array per sublattice, runs of 16 cells along x
+  const bool sub_ok = opt->spin_kind == VG_SPIN_ISING && (g.cell == VG_CELL_BCC || g.cell == VG_CELL_FCC) &&
+                      lat->nx % kIsingGroup == 0 && g.n / g.nb <= (int64_t)INT32_MAX;
+  if (opt->path == VG_PATH_STRUCTURED && !sc_ok && !sub_ok) {
     destroy(c);
-    return fail(nullptr, VG_ERR_UNSUPPORTED, "lattice does not admit the structured checkerboard path");
+    return fail(nullptr, VG_ERR_UNSUPPORTED,
+                "lattice does not admit a structured path (sc checkerboard, or bcc / fcc Ising with x a multiple "
+                "of 16)");
   }
   const bool res_ok = sc_ok && opt->spin_kind == VG_SPIN_ISING && g.n <= 65536;
   if (opt->path == VG_PATH_RESIDENT && !res_ok) {
@@ -967,7 +997,7 @@ int vg_ctx_create_ex(const vg_lattice_desc* lat, const vg_hamiltonian_desc* ham,
     return fail(nullptr, VG_ERR_UNSUPPORTED, "the resident path needs an Ising lattice of at most 65536 sites "
                                              "that admits the checkerboard layout");
   }
-  if (opt->path == VG_PATH_GENERIC || !sc_ok) c->path = VG_PATH_GENERIC;
+  if (opt->path == VG_PATH_GENERIC || !(sc_ok || sub_ok)) c->path = VG_PATH_GENERIC;
   else if (opt->path == VG_PATH_RESIDENT || (opt->path == VG_PATH_AUTO && res_ok && g.n <= 8192)) c->path = VG_PATH_RESIDENT;
   else c->path = VG_PATH_STRUCTURED;
 
@@ -985,6 +1015,13 @@ int vg_ctx_create_ex(const vg_lattice_desc* lat, const vg_hamiltonian_desc* ham,
         destroy(c);
         return rc;
       }
+    }
+  } else if (sub_layout(c)) {
+    c->ncol = g.nb;
+    c->class_size.assign(g.nb, g.n / g.nb);
+    if ((rc = dalloc(c, &c->spin[0][0], (size_t)g.n))) {
+      destroy(c);
+      return rc;
     }
   } else {
     rc = setup_generic(c, g);
@@ -1005,7 +1042,7 @@ int vg_ctx_create_ex(const vg_lattice_desc* lat, const vg_hamiltonian_desc* ham,
   for (int k = 0; k < c->ncol; ++k) {
     const long long nc = c->class_size[k];
     // the structured Ising kernels take 16-site groups, every other kernel one entry per thread
-    items = std::max(items, is_ising(c) && sc_layout(c) ? (nc + 15) / 16 : nc);
+    items = std::max(items, is_ising(c) && (sc_layout(c) || sub_layout(c)) ? (nc + 15) / 16 : nc);
   }
   c->grid = launch_grid(c, items);
   if (is_ising(c) && sc_layout(c) && opt->blocks_per_sm <= 0) {
@@ -1090,10 +1127,11 @@ int vg_init_random(vg_ctx* c) {
   if (!c) return VG_ERR_INVALID_ARG;
   VG_CUDA(c, cudaSetDevice(c->device));
   const RngKey key = rng_key(c, 0);
-  const int structured = sc_layout(c);
+  const int structured = sc_layout(c);  // Heisenberg: checkerboard or natural order
+  const int layout = ising_layout(c);
   const ScMap m = sc_map(c);
   if (is_ising(c)) {
-    ising_init<<<copy_grid(c, (c->n + 15) / 16), 256, 0, c->stream>>>(c->n, structured, m, (uint8_t*)c->spin[0][0],
+    ising_init<<<copy_grid(c, (c->n + 15) / 16), 256, 0, c->stream>>>(c->n, layout, m, (uint8_t*)c->spin[0][0],
                                                                        (uint8_t*)c->spin[1][0], key);
   } else if (fp64(c)) {
     Planes<double> P;
@@ -1126,10 +1164,11 @@ int vg_set_state(vg_ctx* c, const void* host, int64_t n) {
   if (rc) return rc;
   VG_CUDA(c, cudaMemcpyAsync(c->d_stage, host, bytes, cudaMemcpyHostToDevice, c->stream));
   VG_CUDA(c, cudaMemsetAsync(c->d_flag, 0, sizeof(int), c->stream));
-  const int structured = sc_layout(c);
+  const int structured = sc_layout(c);  // Heisenberg: checkerboard or natural order
+  const int layout = ising_layout(c);
   const ScMap m = sc_map(c);
   if (is_ising(c)) {
-    ising_import<<<copy_grid(c, n), 256, 0, c->stream>>>((const int8_t*)c->d_stage, n, structured, m,
+    ising_import<<<copy_grid(c, n), 256, 0, c->stream>>>((const int8_t*)c->d_stage, n, layout, m,
                                                          (uint8_t*)c->spin[0][0], (uint8_t*)c->spin[1][0], c->d_flag);
   } else if (fp64(c)) {
     Planes<double> P;
@@ -1169,10 +1208,11 @@ int export_natural(vg_ctx* c) {
   const size_t bytes = is_ising(c) ? (size_t)n : (size_t)n * 3 * sizeof(double);
   int rc = ensure_stage(c, bytes);
   if (rc) return rc;
-  const int structured = sc_layout(c);
+  const int structured = sc_layout(c);  // Heisenberg: checkerboard or natural order
+  const int layout = ising_layout(c);
   const ScMap m = sc_map(c);
   if (is_ising(c)) {
-    ising_export<<<copy_grid(c, n), 256, 0, c->stream>>>((int8_t*)c->d_stage, n, structured, m,
+    ising_export<<<copy_grid(c, n), 256, 0, c->stream>>>((int8_t*)c->d_stage, n, layout, m,
                                                          (const uint8_t*)c->spin[0][0], (const uint8_t*)c->spin[1][0]);
   } else if (fp64(c)) {
     Planes<double> P;
@@ -1425,9 +1465,9 @@ int vg_wolff_steps(vg_ctx* c, uint64_t n, int32_t measure, double* E, double* M)
   }
   if ((rc = ensure_stage(c, (size_t)c->n))) return rc;
   if (measure && (rc = ensure_sums(c, (size_t)std::max<uint64_t>(n, 1)))) return rc;
-  const int structured = sc_layout(c);
+  const int layout = ising_layout(c);
   const ScMap m = sc_map(c);
-  ising_export<<<copy_grid(c, c->n), 256, 0, c->stream>>>((int8_t*)c->d_stage, c->n, structured, m,
+  ising_export<<<copy_grid(c, c->n), 256, 0, c->stream>>>((int8_t*)c->d_stage, c->n, layout, m,
                                                           (const uint8_t*)c->spin[0][0],
                                                           (const uint8_t*)c->spin[1][0]);
   VG_CUDA(c, cudaGetLastError());
@@ -1452,7 +1492,7 @@ int vg_wolff_steps(vg_ctx* c, uint64_t n, int32_t measure, double* E, double* M)
     }
   }
   VG_CUDA(c, cudaMemsetAsync(c->d_flag, 0, sizeof(int), c->stream));
-  ising_import<<<copy_grid(c, c->n), 256, 0, c->stream>>>((const int8_t*)c->d_stage, c->n, structured, m,
+  ising_import<<<copy_grid(c, c->n), 256, 0, c->stream>>>((const int8_t*)c->d_stage, c->n, layout, m,
                                                           (uint8_t*)c->spin[0][0], (uint8_t*)c->spin[1][0],
                                                           c->d_flag);
   VG_CUDA(c, cudaGetLastError());

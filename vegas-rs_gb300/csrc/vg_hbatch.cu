@@ -53,13 +53,6 @@ constexpr int kPassTpb = 256;        // colour passes and measurement
 constexpr int kPassMinBlocks = 4;    // 64 registers: 32 resident warps per SM (latency-bound loads)
 constexpr int kTrackMinBlocks = 4;   // tracked passes too (partials in shared memory)
 
-// Basis positions in half lattice constants: bcc (0,0,0) (1,1,1); fcc
-// (0,0,0) (1,1,0) (1,0,1) (0,1,1) -- the order of Lattice::bcc / fcc.
-template <int NB>
-__host__ __device__ constexpr int half_pos(int b, int a) {
-  return NB == 2 ? (b == 1 ? 1 : 0) : (((b == 1 && a != 2) || (b == 2 && a != 1) || (b == 3 && a != 0)) ? 1 : 0);
-}
-
 template <typename R>
 struct HbArgs {
   R* spin;             // [rep][class][xyz][cell]

@@ -126,6 +126,24 @@ inline void set_sc_offsets(IsingScArgs& a) {
   a.zwrap = (uint32_t)(a.Lz - 1) * a.plane;
 }
 
+// Basis positions in half lattice constants: bcc (0,0,0) (1,1,1); fcc
+// (0,0,0) (1,1,0) (1,0,1) (0,1,1) -- the order of Lattice::bcc / fcc.  The
+// neighbours of basis b on basis q sit in the cells c + sum over the axes a
+// where the two positions differ of {0, +1 if b is at the half position on
+// a else -1} e_a.
+template <int NB>
+__host__ __device__ constexpr int half_pos(int b, int a) {
+  return NB == 2 ? (b == 1 ? 1 : 0) : (((b == 1 && a != 2) || (b == 2 && a != 1) || (b == 3 && a != 0)) ? 1 : 0);
+}
+
+struct IsingSubArgs {         // bcc / fcc: one uint8 0/1 array per sublattice, [class][cell]
+  uint8_t* base;              // class q at base + q * ncell, cell = (z ny + y) nx + x
+  uint32_t ncell, groups;     // cells per class, 16-cell runs per class (nx a multiple of 16)
+  int nx, ny, nz, z;          // z: coordination (8 or 12)
+  int pbx, pby, pbz;
+  FastDiv fnx, fny;
+};
+
 struct IsingGenArgs {         // any lattice: natural order uint8 0/1 + ELL
   uint8_t* spin;
   const int32_t* sites;       // class entry -> site
@@ -215,6 +233,9 @@ cudaError_t launch_site_energies(bool ising, const void* spins, int64_t n, int z
 template <typename R>
 cudaError_t launch_heis_delta(const double* spins, const double* prop, int64_t n, int z, const int32_t* nbr,
                               const double* jnat, const HeisParams<R>& P, double* out, cudaStream_t s);
+// One colour (sublattice) pass of a bcc / fcc Ising lattice.
+cudaError_t launch_ising_sub(const IsingSubArgs& a, int nb, const IsingTable& tab, RngKey key, int colour,
+                             int proposal, bool update, long long* part, int grid, int tpb, cudaStream_t s);
 size_t ising_resident_smem(const IsingScArgs& a);
 cudaError_t launch_ising_resident(const IsingScArgs& a, const IsingTable& tab, RngKey key, int proposal,
                                   uint32_t n_sweeps, double* sums, int tpb, cudaStream_t s);

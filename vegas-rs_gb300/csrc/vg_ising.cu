@@ -768,6 +768,149 @@ __global__ void __launch_bounds__(256) ising_bond_kernel(const IsingGenArgs a, c
   }
 }
 
+// ------------------------------------------------------------ sublattice
+// bcc / fcc Ising with one array per sublattice (the greedy colouring's
+// classes; entry = cell index): a thread takes a run of 16 cells along x of
+// class CLS.  Its neighbours on class Q are the runs of Q at the cells
+// c + {0, d} e_a along the axes a where the two basis positions differ:
+// whole 16-byte rows along y and z, and along x the same row shifted by one
+// cell (its 16 bytes and the byte at the run's edge).  Up counts and
+// existing-neighbour counts (open axes drop bonds) index the threshold table
+// as in the generic kernel, and entry j draws byte j & 15 of group j >> 4:
+// results equal the generic path's.
+template <int NB, int CLS, bool MEASURE, bool UPDATE, int PROP>
+__global__ void __launch_bounds__(256) ising_sub_kernel(const IsingSubArgs a, const IsingTable tab, const RngKey key,
+                                                        long long* __restrict__ part) {
+  constexpr int ZC = NB == 2 ? 8 : 12;  // coordination
+  constexpr int W = 2 * ZC + 1;
+  constexpr int dx = half_pos<NB>(CLS, 0) ? 1 : -1, dy = half_pos<NB>(CLS, 1) ? 1 : -1,
+                dz = half_pos<NB>(CLS, 2) ? 1 : -1;
+  constexpr int edge = dx < 0 ? 0 : 15;      // the entry whose x neighbour lies outside the run
+  constexpr int ZL = (NB == 2 ? 8 : 4) * CLS;  // bonds to lower classes per entry
+  __shared__ unsigned long long s_thr[2 * W];
+  for (int i = threadIdx.x; i < 2 * W; i += blockDim.x) s_thr[i] = tab.thr[i];
+  __syncthreads();
+  uint8_t* __restrict__ own = a.base + (size_t)CLS * a.ncell;
+  int bond = 0, ups = 0, nacc = 0;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < a.groups; g += stride) {
+    const uint32_t cell0 = g << 4;
+    const uint32_t row = fdiv(cell0, a.fnx);
+    const int x0 = (int)(cell0 - row * (uint32_t)a.nx);
+    const int z = (int)fdiv(row, a.fny);
+    const int y = (int)row - z * a.ny;
+    int ys = y + dy, zs = z + dz, xe = dx < 0 ? x0 - 1 : x0 + 16;
+    bool yok = true, zok = true, xok = true;
+    if (ys < 0 || ys >= a.ny) {
+      ys = ys < 0 ? a.ny - 1 : 0;
+      yok = a.pby;
+    }
+    if (zs < 0 || zs >= a.nz) {
+      zs = zs < 0 ? a.nz - 1 : 0;
+      zok = a.pbz;
+    }
+    if (xe < 0 || xe >= a.nx) {
+      xe = xe < 0 ? a.nx - 1 : 0;
+      xok = a.pbx;
+    }
+    uint32_t A[4] = {0u, 0u, 0u, 0u}, Lo[4] = {0u, 0u, 0u, 0u};  // up neighbours per byte: all, lower classes
+    int miss = 0, missL = 0, emiss = 0, emissL = 0;  // dropped bonds of every entry, and of the edge entry
+#pragma unroll
+    for (int q = 0; q < NB; ++q) {
+      if (q == CLS) continue;
+      const bool Dx = half_pos<NB>(q, 0) != half_pos<NB>(CLS, 0);
+      const bool Dy = half_pos<NB>(q, 1) != half_pos<NB>(CLS, 1);
+      const bool Dz = half_pos<NB>(q, 2) != half_pos<NB>(CLS, 2);
+      const bool low = q < CLS;
+      const uint8_t* __restrict__ oq = a.base + (size_t)q * a.ncell;
+#pragma unroll
+      for (int iz = 0; iz < 2; ++iz) {
+        if (iz && !Dz) continue;
+#pragma unroll
+        for (int iy = 0; iy < 2; ++iy) {
+          if (iy && !Dy) continue;
+          const int per = Dx ? 2 : 1;  // bonds this row carries per entry
+          if ((iz && !zok) || (iy && !yok)) {
+            miss += per;
+            if (low) missL += per;
+            continue;
+          }
+          const uint32_t r = ((uint32_t)(iz ? zs : z) * (uint32_t)a.ny + (uint32_t)(iy ? ys : y)) * (uint32_t)a.nx;
+          const uint4 v = __ldg(reinterpret_cast<const uint4*>(oq + r + (uint32_t)x0));
+          const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+          uint32_t X1[4] = {0u, 0u, 0u, 0u};
+          if (Dx) {
+            uint32_t e = 0u;
+            if (xok) e = __ldg(oq + r + (uint32_t)xe);
+            else {
+              emiss += 1;
+              if (low) emissL += 1;
+            }
+            if (dx < 0) {
+              X1[0] = __byte_perm(e << 24, w[0], 0x6543);
+#pragma unroll
+              for (int i = 1; i < 4; ++i) X1[i] = __byte_perm(w[i - 1], w[i], 0x6543);
+            } else {
+#pragma unroll
+              for (int i = 0; i < 3; ++i) X1[i] = __byte_perm(w[i], w[i + 1], 0x4321);
+              X1[3] = __byte_perm(w[3], e, 0x4321);
+            }
+          }
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            const uint32_t add = w[i] + X1[i];
+            A[i] += add;
+            if (low) Lo[i] += add;
+          }
+        }
+      }
+    }
+    const uint4 Sv = *reinterpret_cast<const uint4*>(own + cell0);
+    const uint32_t S[4] = {Sv.x, Sv.y, Sv.z, Sv.w};
+    uint32_t flip = 0;
+    if (UPDATE) {
+      uint32_t cand = 0xFFFFu;
+      if (PROP == VG_PROPOSE_RANDOM) {
+        const uint4 pb =
+            philox_ks(make_uint4(g, key.sweep, (kTagIsingPropose << 24) | ((uint32_t)CLS << 8), key.replica), key.ks);
+        cand = 0u;
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+          const uint32_t up = blk_byte(pb, k) < 128u ? 1u : 0u;
+          cand |= (up != ((S[k >> 2] >> (8 * (k & 3))) & 1u) ? 1u : 0u) << k;
+        }
+      }
+      unsigned long long t[16];
+#pragma unroll
+      for (int k = 0; k < 16; ++k) {
+        const int s01 = (int)((S[k >> 2] >> (8 * (k & 3))) & 1u);
+        const int nu = (int)((A[k >> 2] >> (8 * (k & 3))) & 0xFFu);
+        const int nbe = ZC - miss - (k == edge ? emiss : 0);
+        t[k] = s_thr[s01 * W + (2 * nu - nbe) + ZC];
+      }
+      flip = decide16(t, cand, key, g, CLS) & cand;
+    }
+    uint32_t Sn[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) Sn[i] = S[i] ^ spread4(flip >> (4 * i));
+    if (flip) *reinterpret_cast<uint4*>(own + cell0) = make_uint4(Sn[0], Sn[1], Sn[2], Sn[3]);
+    if (MEASURE) {
+      nacc += __popc(flip);
+#pragma unroll
+      for (int k = 0; k < 16; ++k) {
+        const int sn = (int)((Sn[k >> 2] >> (8 * (k & 3))) & 1u);
+        ups += sn;
+        if (CLS > 0) {
+          const int nl = (int)((Lo[k >> 2] >> (8 * (k & 3))) & 0xFFu);
+          const int nlow = 2 * nl - (ZL - missL - (k == edge ? emissL : 0));
+          bond += sn ? nlow : -nlow;
+        }
+      }
+    }
+  }
+  if (MEASURE) block_sum3_store(bond, ups, nacc, part + (size_t)blockIdx.x * kNumSums);
+}
+
 // ------------------------------------------------------------ dispatch
 // Launch with programmatic stream serialization: the kernel may start while
 // its predecessor on the stream drains and waits (griddepcontrol.wait) for
@@ -895,6 +1038,35 @@ cudaError_t launch_ising_gen(const IsingGenArgs& a, const IsingTable& tab, RngKe
   if (a.z <= 6) return gen_dispatch<6>(a, tab, key, colour, proposal, update, part, grid, tpb, s);
   if (a.z <= 8) return gen_dispatch<8>(a, tab, key, colour, proposal, update, part, grid, tpb, s);
   return gen_dispatch<12>(a, tab, key, colour, proposal, update, part, grid, tpb, s);
+}
+
+template <int NB, int CLS>
+static cudaError_t sub_dispatch(const IsingSubArgs& a, const IsingTable& tab, RngKey key, int proposal, bool update,
+                                long long* part, int grid, int tpb, cudaStream_t s) {
+  const bool m = part != nullptr;
+  if (!update)
+    ising_sub_kernel<NB, CLS, true, false, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, tab, key, part);
+  else if (proposal == VG_PROPOSE_FLIP) {
+    if (m) ising_sub_kernel<NB, CLS, true, true, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, tab, key, part);
+    else ising_sub_kernel<NB, CLS, false, true, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, tab, key, part);
+  } else {
+    if (m) ising_sub_kernel<NB, CLS, true, true, VG_PROPOSE_RANDOM><<<grid, tpb, 0, s>>>(a, tab, key, part);
+    else ising_sub_kernel<NB, CLS, false, true, VG_PROPOSE_RANDOM><<<grid, tpb, 0, s>>>(a, tab, key, part);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ising_sub(const IsingSubArgs& a, int nb, const IsingTable& tab, RngKey key, int colour,
+                             int proposal, bool update, long long* part, int grid, int tpb, cudaStream_t s) {
+  if (nb == 2)
+    return colour == 0 ? sub_dispatch<2, 0>(a, tab, key, proposal, update, part, grid, tpb, s)
+                       : sub_dispatch<2, 1>(a, tab, key, proposal, update, part, grid, tpb, s);
+  switch (colour) {
+    case 0: return sub_dispatch<4, 0>(a, tab, key, proposal, update, part, grid, tpb, s);
+    case 1: return sub_dispatch<4, 1>(a, tab, key, proposal, update, part, grid, tpb, s);
+    case 2: return sub_dispatch<4, 2>(a, tab, key, proposal, update, part, grid, tpb, s);
+    default: return sub_dispatch<4, 3>(a, tab, key, proposal, update, part, grid, tpb, s);
+  }
 }
 
 }  // namespace vg
