@@ -774,22 +774,54 @@ __global__ void __launch_bounds__(256) ising_bond_kernel(const IsingGenArgs a, c
 // class CLS.  Its neighbours on class Q are the runs of Q at the cells
 // c + {0, d} e_a along the axes a where the two basis positions differ:
 // whole 16-byte rows along y and z, and along x the same row shifted by one
-// cell (its 16 bytes and the byte at the run's edge).  Up counts and
-// existing-neighbour counts (open axes drop bonds) index the threshold table
-// as in the generic kernel, and entry j draws byte j & 15 of group j >> 4:
-// results equal the generic path's.
+// cell (its 16 bytes and the byte at the run's edge).  Entry j draws byte
+// j & 15 of group j >> 4, so results equal the generic path's.
+//
+// Decisions are byte-parallel as in the sc pair kernel: every entry of a run
+// has the same number nbe of existing neighbours (open y / z boundaries drop
+// whole rows), except the edge entry when its x neighbour lies across an
+// open boundary.  A shared table per (nbe, spin) holds the thresholds' top
+// bytes for up-neighbour counts 0..15, looked up with two PRMTs per word;
+// the first random digit is compared byte-parallel and the rare ties (and
+// the odd edge entry) are decided from the full thresholds in line.
+
+// Top bytes of the thresholds of 16 entries packed 4 per word (nu = up
+// neighbours per byte, s = 0/1 spin per byte), from the 16-byte tables of
+// the two spin values.
+__device__ __forceinline__ uint32_t sub_top(uint32_t nu, uint32_t s, const uint4& t0, const uint4& t1) {
+  const uint32_t sel = nibble_selector(nu);
+  const uint32_t hm = ((nu >> 3) & 0x01010101u) * 0xFFu;
+  const uint32_t sm = s * 0xFFu;
+  const uint32_t a0 = (__byte_perm(t0.z, t0.w, sel) & hm) | (__byte_perm(t0.x, t0.y, sel) & ~hm);
+  const uint32_t a1 = (__byte_perm(t1.z, t1.w, sel) & hm) | (__byte_perm(t1.x, t1.y, sel) & ~hm);
+  return (a1 & sm) | (a0 & ~sm);
+}
+
 template <int NB, int CLS, bool MEASURE, bool UPDATE, int PROP>
-__global__ void __launch_bounds__(256) ising_sub_kernel(const IsingSubArgs a, const IsingTable tab, const RngKey key,
-                                                        long long* __restrict__ part) {
+__global__ void __launch_bounds__(256, 4) ising_sub_kernel(const IsingSubArgs a, const IsingTable tab, const RngKey key,
+                                                           long long* __restrict__ part) {
   constexpr int ZC = NB == 2 ? 8 : 12;  // coordination
   constexpr int W = 2 * ZC + 1;
   constexpr int dx = half_pos<NB>(CLS, 0) ? 1 : -1, dy = half_pos<NB>(CLS, 1) ? 1 : -1,
                 dz = half_pos<NB>(CLS, 2) ? 1 : -1;
-  constexpr int edge = dx < 0 ? 0 : 15;      // the entry whose x neighbour lies outside the run
+  constexpr int edge = dx < 0 ? 0 : 15;        // the entry whose x neighbour lies outside the run
   constexpr int ZL = (NB == 2 ? 8 : 4) * CLS;  // bonds to lower classes per entry
+  constexpr bool ALL_LOW = CLS == NB - 1;      // every neighbour class is lower
   __shared__ unsigned long long s_thr[2 * W];
+  __shared__ uint4 s_top[ZC + 1][2];           // [nbe][spin]: top byte for nu = 0..15
+  pdl_launch_dependents();
   for (int i = threadIdx.x; i < 2 * W; i += blockDim.x) s_thr[i] = tab.thr[i];
+  for (int i = threadIdx.x; i < (ZC + 1) * 32; i += blockDim.x) {
+    const int nbe = i >> 5, s01 = (i >> 4) & 1, nu = i & 15;
+    uint32_t top = 0u;
+    if (nu <= nbe) {
+      const unsigned long long t = tab.thr[s01 * W + 2 * nu - nbe + ZC];
+      top = t >= (1ull << 32) ? 0xFFu : (uint32_t)(t >> 24);
+    }
+    reinterpret_cast<uint8_t*>(&s_top[nbe][s01])[nu] = (uint8_t)top;
+  }
   __syncthreads();
+  pdl_wait();
   uint8_t* __restrict__ own = a.base + (size_t)CLS * a.ncell;
   int bond = 0, ups = 0, nacc = 0;
   const uint32_t stride = gridDim.x * blockDim.x;
@@ -821,7 +853,7 @@ __global__ void __launch_bounds__(256) ising_sub_kernel(const IsingSubArgs a, co
       const bool Dx = half_pos<NB>(q, 0) != half_pos<NB>(CLS, 0);
       const bool Dy = half_pos<NB>(q, 1) != half_pos<NB>(CLS, 1);
       const bool Dz = half_pos<NB>(q, 2) != half_pos<NB>(CLS, 2);
-      const bool low = q < CLS;
+      const bool low = q < CLS && !ALL_LOW;
       const uint8_t* __restrict__ oq = a.base + (size_t)q * a.ncell;
 #pragma unroll
       for (int iz = 0; iz < 2; ++iz) {
@@ -832,7 +864,7 @@ __global__ void __launch_bounds__(256) ising_sub_kernel(const IsingSubArgs a, co
           const int per = Dx ? 2 : 1;  // bonds this row carries per entry
           if ((iz && !zok) || (iy && !yok)) {
             miss += per;
-            if (low) missL += per;
+            if (q < CLS) missL += per;
             continue;
           }
           const uint32_t r = ((uint32_t)(iz ? zs : z) * (uint32_t)a.ny + (uint32_t)(iy ? ys : y)) * (uint32_t)a.nx;
@@ -844,7 +876,7 @@ __global__ void __launch_bounds__(256) ising_sub_kernel(const IsingSubArgs a, co
             if (xok) e = __ldg(oq + r + (uint32_t)xe);
             else {
               emiss += 1;
-              if (low) emissL += 1;
+              if (q < CLS) emissL += 1;
             }
             if (dx < 0) {
               X1[0] = __byte_perm(e << 24, w[0], 0x6543);
@@ -865,46 +897,101 @@ __global__ void __launch_bounds__(256) ising_sub_kernel(const IsingSubArgs a, co
         }
       }
     }
+    if (ALL_LOW) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) Lo[i] = A[i];
+    }
     const uint4 Sv = *reinterpret_cast<const uint4*>(own + cell0);
     const uint32_t S[4] = {Sv.x, Sv.y, Sv.z, Sv.w};
-    uint32_t flip = 0;
+    const int nbe = ZC - miss;
+    uint32_t F[4] = {0u, 0u, 0u, 0u};
     if (UPDATE) {
-      uint32_t cand = 0xFFFFu;
+      uint32_t cand[4] = {0x01010101u, 0x01010101u, 0x01010101u, 0x01010101u};
       if (PROP == VG_PROPOSE_RANDOM) {
         const uint4 pb =
             philox_ks(make_uint4(g, key.sweep, (kTagIsingPropose << 24) | ((uint32_t)CLS << 8), key.replica), key.ks);
-        cand = 0u;
+        const uint32_t w[4] = {pb.x, pb.y, pb.z, pb.w};
 #pragma unroll
-        for (int k = 0; k < 16; ++k) {
-          const uint32_t up = blk_byte(pb, k) < 128u ? 1u : 0u;
-          cand |= (up != ((S[k >> 2] >> (8 * (k & 3))) & 1u) ? 1u : 0u) << k;
+        for (int i = 0; i < 4; ++i) cand[i] = ((~w[i] >> 7) & 0x01010101u) ^ S[i];
+      }
+      const uint32_t ecand = (cand[edge >> 2] >> (8 * (edge & 3))) & 1u;
+      if (emiss) cand[edge >> 2] &= ~(0xFFu << (8 * (edge & 3)));  // decided below from its own threshold
+      const uint4 b = philox_ks(make_uint4(g, key.sweep, (kTagIsingAccept << 24) | ((uint32_t)CLS << 8), key.replica),
+                                key.ks);
+      const uint32_t R[4] = {b.x, b.y, b.z, b.w};
+      const uint4 t0 = s_top[nbe][0], t1 = s_top[nbe][1];
+      uint32_t tm = 0u;  // entries tied with their threshold on the first digit
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const uint32_t thr = sub_top(A[i], S[i], t0, t1);
+        F[i] = (bytes_gt80(thr, R[i]) >> 7) & cand[i];
+        tm |= gather4(bytes_zero(R[i] ^ thr) & cand[i]) << (4 * i);
+      }
+      if (emiss && ecand) tm |= 1u << edge;  // the edge entry starts at the first digit
+      if (tm) {
+        const uint32_t nbe_e = (uint32_t)(nbe - emiss);
+        uint32_t acc = 0u;
+        for (int d = 0; d < 4 && tm; ++d) {
+          uint4 bd = b;
+          if (d > 0)
+            bd = philox_ks(make_uint4(g, key.sweep, (kTagIsingAccept << 24) | ((uint32_t)CLS << 8) | (uint32_t)d,
+                                      key.replica),
+                           key.ks);
+          for (uint32_t m = tm; m; m &= m - 1u) {
+            const int k = __ffs(m) - 1;
+            const uint32_t s01 = byte_at(S[0], S[1], S[2], S[3], k);
+            const uint32_t nu = byte_at(A[0], A[1], A[2], A[3], k);
+            const int ne = k == edge ? (int)nbe_e : nbe;
+            const unsigned long long th = s_thr[s01 * W + 2 * (int)nu - ne + ZC];
+            const uint32_t bit = 1u << k;
+            if (th >= (1ull << 32)) {
+              acc |= bit;
+              tm &= ~bit;
+              continue;
+            }
+            const bool first = k == edge && emiss && d == 0;  // not compared byte-parallel
+            if (d == 0 && !first) continue;                 // tied on digit 0 already
+            const uint32_t ub = blk_byte(bd, k);
+            const uint32_t tb = ((uint32_t)th >> (24 - 8 * d)) & 0xFFu;
+            if (ub < tb) {
+              acc |= bit;
+              tm &= ~bit;
+            } else if (ub > tb) {
+              tm &= ~bit;
+            }
+          }
         }
-      }
-      unsigned long long t[16];
 #pragma unroll
-      for (int k = 0; k < 16; ++k) {
-        const int s01 = (int)((S[k >> 2] >> (8 * (k & 3))) & 1u);
-        const int nu = (int)((A[k >> 2] >> (8 * (k & 3))) & 0xFFu);
-        const int nbe = ZC - miss - (k == edge ? emiss : 0);
-        t[k] = s_thr[s01 * W + (2 * nu - nbe) + ZC];
+        for (int i = 0; i < 4; ++i) F[i] |= spread4(acc >> (4 * i));
       }
-      flip = decide16(t, cand, key, g, CLS) & cand;
     }
-    uint32_t Sn[4];
+    uint32_t Sn[4], anyf = 0u;
 #pragma unroll
-    for (int i = 0; i < 4; ++i) Sn[i] = S[i] ^ spread4(flip >> (4 * i));
-    if (flip) *reinterpret_cast<uint4*>(own + cell0) = make_uint4(Sn[0], Sn[1], Sn[2], Sn[3]);
+    for (int i = 0; i < 4; ++i) {
+      Sn[i] = S[i] ^ F[i];
+      anyf |= F[i];
+    }
+    if (anyf) *reinterpret_cast<uint4*>(own + cell0) = make_uint4(Sn[0], Sn[1], Sn[2], Sn[3]);
     if (MEASURE) {
-      nacc += __popc(flip);
+      unsigned su = 0u, sf = 0u;
 #pragma unroll
-      for (int k = 0; k < 16; ++k) {
-        const int sn = (int)((Sn[k >> 2] >> (8 * (k & 3))) & 1u);
-        ups += sn;
-        if (CLS > 0) {
-          const int nl = (int)((Lo[k >> 2] >> (8 * (k & 3))) & 0xFFu);
-          const int nlow = 2 * nl - (ZL - missL - (k == edge ? emissL : 0));
-          bond += sn ? nlow : -nlow;
+      for (int i = 0; i < 4; ++i) {
+        su = __dp4a(Sn[i], 0x01010101u, su);
+        sf = __dp4a(F[i], 0x01010101u, sf);
+      }
+      ups += (int)su;
+      nacc += (int)sf;
+      if (CLS > 0) {
+        // sum_k (2 s_k - 1)(2 nl_k - L_k), L_k = L but L - emissL for the edge entry
+        const int L = ZL - missL;
+        unsigned snl = 0u, nls = 0u;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          snl = __dp4a(Sn[i], Lo[i], snl);
+          nls = __dp4a(Lo[i], 0x01010101u, nls);
         }
+        const int se = (int)((Sn[edge >> 2] >> (8 * (edge & 3))) & 1u);
+        bond += 4 * (int)snl - 2 * (L * (int)su - emissL * se) - 2 * (int)nls + 16 * L - emissL;
       }
     }
   }
@@ -1044,16 +1131,13 @@ template <int NB, int CLS>
 static cudaError_t sub_dispatch(const IsingSubArgs& a, const IsingTable& tab, RngKey key, int proposal, bool update,
                                 long long* part, int grid, int tpb, cudaStream_t s) {
   const bool m = part != nullptr;
-  if (!update)
-    ising_sub_kernel<NB, CLS, true, false, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, tab, key, part);
-  else if (proposal == VG_PROPOSE_FLIP) {
-    if (m) ising_sub_kernel<NB, CLS, true, true, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, tab, key, part);
-    else ising_sub_kernel<NB, CLS, false, true, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, tab, key, part);
-  } else {
-    if (m) ising_sub_kernel<NB, CLS, true, true, VG_PROPOSE_RANDOM><<<grid, tpb, 0, s>>>(a, tab, key, part);
-    else ising_sub_kernel<NB, CLS, false, true, VG_PROPOSE_RANDOM><<<grid, tpb, 0, s>>>(a, tab, key, part);
+  if (!update) return launch_pdl(ising_sub_kernel<NB, CLS, true, false, VG_PROPOSE_FLIP>, grid, tpb, s, a, tab, key, part);
+  if (proposal == VG_PROPOSE_FLIP) {
+    if (m) return launch_pdl(ising_sub_kernel<NB, CLS, true, true, VG_PROPOSE_FLIP>, grid, tpb, s, a, tab, key, part);
+    return launch_pdl(ising_sub_kernel<NB, CLS, false, true, VG_PROPOSE_FLIP>, grid, tpb, s, a, tab, key, part);
   }
-  return cudaGetLastError();
+  if (m) return launch_pdl(ising_sub_kernel<NB, CLS, true, true, VG_PROPOSE_RANDOM>, grid, tpb, s, a, tab, key, part);
+  return launch_pdl(ising_sub_kernel<NB, CLS, false, true, VG_PROPOSE_RANDOM>, grid, tpb, s, a, tab, key, part);
 }
 
 cudaError_t launch_ising_sub(const IsingSubArgs& a, int nb, const IsingTable& tab, RngKey key, int colour,

@@ -6,6 +6,7 @@ launches with -c), after the same command has run without the profiler.
 
     python vegas-rs_gb300/profile_cases.py ising L SWEEPS      # sc L^3 Ising, checkerboard passes
     python vegas-rs_gb300/profile_cases.py ising_sizes N       # pass time for sc 64^3 .. 512^3
+    python vegas-rs_gb300/profile_cases.py sub CELL L SWEEPS   # bcc / fcc L^3-cell Ising, sublattice passes
     python vegas-rs_gb300/profile_cases.py heis L SWEEPS       # sc L^3 Heisenberg, FP32
     python vegas-rs_gb300/profile_cases.py hbatch L REPLICAS   # fcc L^3 cells x replicas, field points
     python vegas-rs_gb300/profile_cases.py msc ROUNDS          # the 256-replica multi-spin-coded batch
@@ -44,6 +45,17 @@ def ising_sizes(sweeps_at_256):
             eng.synchronize()
             us = (time.perf_counter() - t0) / n * 1e6
             print(f"sc {L}^3: pass {us / 2:.2f} us, {L ** 3 / (us * 1e3):.1f} flips/ns, grid {eng.info().grid_blocks}")
+
+
+def sub(cell, L, sweeps):
+    lat = getattr(V.Lattice, cell)(L, L, L)
+    with V.Engine(lat, V.hamiltonian(V.Exchange(1.0)), seed=1, path=V.PATH_STRUCTURED) as eng:
+        eng.init_random()
+        eng.set_thermostat(3.0)
+        t0 = time.perf_counter()
+        eng.sweeps(sweeps)
+        dt = time.perf_counter() - t0
+        print(f"ising {cell} {L}^3 cells: {sweeps} measured sweeps, {lat.n_sites * sweeps / (dt * 1e9):.1f} flips/ns (wall)")
 
 
 def heis(L, sweeps):
@@ -86,5 +98,5 @@ def msc(rounds):
 
 
 if __name__ == "__main__":
-    case, args = sys.argv[1], [int(a) for a in sys.argv[2:]]
-    {"ising": ising, "ising_sizes": ising_sizes, "heis": heis, "hbatch": hbatch, "msc": msc}[case](*args)
+    case, args = sys.argv[1], [a if a in ("bcc", "fcc") else int(a) for a in sys.argv[2:]]
+    {"ising": ising, "ising_sizes": ising_sizes, "sub": sub, "heis": heis, "hbatch": hbatch, "msc": msc}[case](*args)
