@@ -120,6 +120,27 @@ def test_sublattice_needs_x_multiple_of_16(V):
         assert eng.info().path == V.PATH_GENERIC
 
 
+@pytest.mark.parametrize("proposal", [0, 1])
+@pytest.mark.parametrize("ext,pbc", [((128, 64, 20), (1, 1, 1)), ((512, 512, 1), (1, 1, 0))])
+def test_pair_rounds_bit_exact(V, O, ext, pbc, proposal):
+    """More 16-site groups than grid threads: the pass runs two groups per
+    thread per round (a one-warp-per-SM grid)."""
+    seed, J, T, mag, n = 77, 1.0, 4.4, 0.2, 3
+    H = V.hamiltonian(V.Exchange(J), V.Zeeman())
+    with _engine(V, "sc", ext, pbc, H, seed, path=V.PATH_STRUCTURED, proposal=proposal, threads_per_block=32,
+                 blocks_per_sm=1) as eng:
+        assert eng.info().grid_blocks * 32 < ext[0] * ext[1] * ext[2] // 32
+        eng.init_random()
+        g = O.Graph(O.lattice("sc", *ext, pbc))
+        s0 = g.ising_init(seed)
+        eng.set_thermostat(T, (0.0, 0.0, 1.0), mag)
+        E, M = eng.sweeps(n)
+        ref, obs = g.ising_sweeps(s0, J, mag, T, seed, 0, n, proposal=proposal)
+        assert np.array_equal(eng.get_state(), ref)
+        np.testing.assert_allclose(E, -2 * J * obs[:, 0] + mag * obs[:, 1], rtol=0, atol=1e-9)
+        np.testing.assert_array_equal(M, np.abs(obs[:, 1]).astype(float))
+
+
 def test_resume_from_sweep_index(V):
     """(seed, sweep index) is the whole RNG state: splitting a run changes nothing."""
     H = V.hamiltonian(V.Exchange(1.0))

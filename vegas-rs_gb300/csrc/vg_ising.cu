@@ -607,9 +607,19 @@ __global__ void __launch_bounds__(256, kSc2MinBlocks) ising_sc2_kernel(const Isi
   __syncthreads();
   pdl_wait();
   int bond = 0, ups = 0, nacc = 0;
-  sc2_range<C, MEASURE, UPDATE, PROP, ALLPER>(a, fG2, tab, key, s_thr, s_q,
-                                                     blockIdx.x * blockDim.x + (threadIdx.x & ~31u), a.groups >> 1,
-                                                     gridDim.x * blockDim.x, bond, ups, nacc);
+  // A class with no more groups than the grid has threads runs one group per
+  // thread (twice the threads of pairs; 128^3: 5.4 -> 4.1 us per pass).
+  // Larger classes run pairs: dealing the pairs left over after whole rounds
+  // out as single groups, evenly over the SMs, was slower at 192^3 - 512^3
+  // (256^3: 9.8 -> 10.4 us) than letting a quarter of the blocks run one
+  // more pair round on issue slots the others have freed.
+  const uint32_t T = gridDim.x * blockDim.x;
+  const uint32_t first = blockIdx.x * blockDim.x + (threadIdx.x & ~31u);
+  if (a.groups <= T)
+    sc1_range<C, true, MEASURE, UPDATE, PROP>(a, tab, key, s_thr, s_q, first, a.groups, T, bond, ups, nacc);
+  else
+    sc2_range<C, MEASURE, UPDATE, PROP, ALLPER>(a, fG2, tab, key, s_thr, s_q, first, a.groups >> 1, T, bond, ups,
+                                                nacc);
   if (MEASURE) block_sum3_store(bond, ups, nacc, part + (size_t)blockIdx.x * kNumSums);
 }
 
