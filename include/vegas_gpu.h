@@ -56,7 +56,11 @@ enum vg_unit_cell { VG_CELL_SC = 0, VG_CELL_BCC = 1, VG_CELL_FCC = 2 };
 enum vg_proposal { VG_PROPOSE_FLIP = 0, VG_PROPOSE_RANDOM = 1 };
 /* Kernel family.  AUTO picks RESIDENT for Ising lattices of at most 8192
  * sites that admit STRUCTURED, else STRUCTURED when the lattice allows it,
- * else GENERIC.  RESIDENT keeps the checkerboard layout of STRUCTURED in one
+ * else GENERIC.  STRUCTURED: sc lattices with an even x extent (Ising: x/2 a
+ * multiple of 16) and even periodic y / z extents, as a checkerboard; bcc /
+ * fcc Ising lattices with x a multiple of 16, one array per basis
+ * sublattice.  GENERIC: any lattice, and per-bond exchange constants
+ * (vg_set_exchange_bonds).  RESIDENT keeps the checkerboard layout of STRUCTURED in one
  * thread block's shared memory and runs all sweeps of a call in one launch
  * (Ising, at most 65536 sites); results are identical across paths. */
 enum vg_path { VG_PATH_AUTO = 0, VG_PATH_GENERIC = 1, VG_PATH_STRUCTURED = 2, VG_PATH_RESIDENT = 3 };
