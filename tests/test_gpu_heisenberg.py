@@ -16,8 +16,11 @@ LATTICES = [
     ("sc", (8, 8, 8), (1, 1, 1)),        # structured checkerboard
     ("sc", (8, 6, 5), (1, 1, 0)),        # structured, open z
     ("sc", (7, 4, 4), (1, 1, 1)),        # generic (odd x)
-    ("bcc", (4, 4, 4), (1, 1, 1)),
-    ("fcc", (3, 3, 3), (1, 1, 1)),
+    ("bcc", (4, 4, 4), (1, 1, 1)),       # sublattice planes, runs of 4 cells
+    ("fcc", (3, 3, 3), (1, 1, 1)),       # sublattice planes, runs of 1 cell
+    ("bcc", (8, 4, 3), (1, 0, 1)),       # runs of 4, open y
+    ("fcc", (5, 3, 4), (0, 1, 1)),       # runs of 1, open x
+    ("fcc", (4, 2, 3), (1, 1, 0)),       # runs of 4, open z
 ]
 
 
@@ -28,11 +31,13 @@ def _params(O, J, K, axis, hz, b, Kc, T):
     return P
 
 
-def _run(V, O, cell, ext, pbc, precision, proposal, n=2, seed=21):
+def _run(V, O, cell, ext, pbc, precision, proposal, n=2, seed=21, **opts):
     J, K, axis, mag, b, T = 1.0, 0.1, (0.0, 0.0, 1.0), 0.05, (0.0, 0.6, 0.8), 0.9
     H = V.hamiltonian(V.Exchange(J), V.UniaxialAnisotropy(axis, K), V.Zeeman())
     lat = getattr(V.Lattice, cell)(*ext, pbc=tuple(bool(p) for p in pbc))
-    with V.Engine(lat, H, spin=V.SPIN_HEISENBERG, seed=seed, precision=precision, proposal=proposal) as eng:
+    with V.Engine(lat, H, spin=V.SPIN_HEISENBERG, seed=seed, precision=precision, proposal=proposal, **opts) as eng:
+        if opts:  # a grid of one warp per SM: threads walk several runs of four cells
+            assert lat.n_sites // (4 * (2 if cell == "bcc" else 4)) > eng.info().sm_count * 32
         eng.init_random()
         s0 = eng.get_state()
         eng.set_thermostat(T, b, mag)
@@ -57,6 +62,22 @@ def test_fp64_follows_oracle(V, O, cell, ext, pbc, proposal):
         np.testing.assert_allclose(sums[-1, :7], obs[-1, :7], rtol=0, atol=1e-9)
 
 
+@pytest.mark.parametrize("cell,ext,pbc", [("bcc", (32, 16, 40), (1, 1, 1)), ("fcc", (32, 24, 26), (1, 0, 1))])
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_sublattice_runs_of_four_follow_oracle(V, O, cell, ext, pbc, precision):
+    """bcc / fcc with x a multiple of 4 (float4 / double2 runs of four cells),
+    on a grid of one warp per SM so that threads walk several runs."""
+    fp64 = precision == "fp64"
+    s0, ref0, s1, ref1, sums, obs, path = _run(V, O, cell, ext, pbc, V.FP64 if fp64 else V.FP32, 1, n=1,
+                                               threads_per_block=32, blocks_per_sm=1)
+    assert path == V.PATH_STRUCTURED
+    tol = 1e-12 if fp64 else 2e-6
+    same = np.all(np.abs(s1 - ref1) < tol, axis=1)
+    assert same.mean() >= 0.999
+    if fp64 and same.all():
+        np.testing.assert_allclose(sums[-1, :7], obs[-1, :7], rtol=0, atol=1e-8)
+
+
 @pytest.mark.parametrize("cell,ext,pbc", LATTICES)
 def test_fp32_follows_oracle(V, O, cell, ext, pbc):
     s0, ref0, s1, ref1, sums, obs, _ = _run(V, O, cell, ext, pbc, V.FP32, 1, n=1)
@@ -66,6 +87,34 @@ def test_fp32_follows_oracle(V, O, cell, ext, pbc):
     assert (d < 2e-6).mean() >= 0.999
     norms = np.linalg.norm(s1, axis=1)
     assert np.abs(norms - 1).max() < 1e-6
+
+
+@pytest.mark.parametrize("cell,ext,pbc", [("bcc", (8, 6, 4), (1, 1, 1)), ("fcc", (4, 5, 3), (1, 0, 1)),
+                                          ("fcc", (3, 4, 4), (0, 1, 1))])
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_sublattice_and_generic_paths_agree(V, cell, ext, pbc, precision):
+    """bcc / fcc Heisenberg: the sublattice kernel and the ELL kernel draw the
+    same numbers; their fields differ only in FP summation order."""
+    prec = V.FP64 if precision == "fp64" else V.FP32
+    tol = 1e-12 if precision == "fp64" else 2e-6
+    H = V.hamiltonian(V.Exchange(1.0), V.UniaxialAnisotropy((0.0, 0.6, 0.8), 0.2), V.Zeeman(), V.CubicAnisotropy(0.05))
+    lat = getattr(V.Lattice, cell)(*ext, pbc=tuple(bool(p) for p in pbc))
+    out = []
+    for path in (V.PATH_STRUCTURED, V.PATH_GENERIC):
+        with V.Engine(lat, H, spin=V.SPIN_HEISENBERG, seed=9, precision=prec, path=path,
+                      proposal=V.PROPOSE_RANDOM) as eng:
+            assert eng.info().path == path
+            eng.init_random()
+            eng.set_thermostat(0.8, (0.0, 0.0, 1.0), 0.3)
+            sums = eng.sweeps_sums(3)
+            out.append((eng.get_state(), sums, eng.current_sums()))
+    same = np.all(np.abs(out[0][0] - out[1][0]) < tol, axis=1)
+    assert same.mean() >= 0.999
+    if same.all():
+        n = lat.n_sites
+        scale = np.array([12 * n, n, n, n, n, n, n, n])
+        assert np.all(np.abs(out[0][1] - out[1][1]) <= 1e-5 * scale)
+        assert np.all(np.abs(out[0][2][:7] - out[1][2][:7]) <= 1e-5 * scale[:7])
 
 
 def test_fp32_sums_match_fp64_on_same_state(V):

@@ -15,6 +15,7 @@
 // sum takes, for each site, only neighbours of lower colour, which are final
 // for the sweep when that site's pass runs, so every bond is counted once.
 #include "vg_heis_common.cuh"
+#include "vg_sublattice.cuh"
 
 namespace vg {
 
@@ -322,6 +323,115 @@ cudaError_t launch_heis_gen(const HeisGenArgs<R>& a, const HeisParams<R>& p, Rng
   return cudaGetLastError();
 }
 
+// ------------------------------------------------------------- sublattice
+// bcc / fcc: one thread per run of W cells of class CLS (the basis
+// sublattice), SoA planes [class][xyz][cell].  The field adds the classes in
+// ascending order, the lower ones first: their partial sum is the bond field
+// the class's lattice sums count (each bond once, from its higher-class end).
+// Entry j of the class is cell j, so the draws are the generic path's.
+template <typename R, int NB, int CLS, int W, bool MEASURE, bool UPDATE, int PROP>
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 2) heis_sub_kernel(const HeisSubArgs<R> a, const HeisParams<R> P,
+                                                          const RngKey key, double* __restrict__ part) {
+  R* own[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) own[c] = a.spin + (size_t)(CLS * 3 + c) * a.ncell;
+  R acc[kNumSums];
+#pragma unroll
+  for (int i = 0; i < kNumSums; ++i) acc[i] = (R)0;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < a.runs; u += stride) {
+    const int row = (int)fdiv(u, a.frow);
+    const int x0 = (int)(u - (uint32_t)row * (uint32_t)a.rpr) * W;
+    const int z = (int)fdiv((uint32_t)row, a.fny);
+    const int y = row - z * a.ny;
+    const RunNbr nb = make_nbr<NB, CLS, W>(a, x0, y, z);
+    Run<R, W> hf[3], lo[3];
+    zero_runs(hf);
+    if constexpr (CLS > 0) add_class<R, NB, CLS, 0, W>(a, a.spin, x0, y, z, nb, hf);
+    if constexpr (CLS > 1) add_class<R, NB, CLS, 1, W>(a, a.spin, x0, y, z, nb, hf);
+    if constexpr (CLS > 2) add_class<R, NB, CLS, 2, W>(a, a.spin, x0, y, z, nb, hf);
+    if (MEASURE) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) lo[c] = hf[c];
+    }
+    if constexpr (CLS < 1) add_class<R, NB, CLS, 1, W>(a, a.spin, x0, y, z, nb, hf);
+    if constexpr (NB == 4 && CLS < 2) add_class<R, NB, CLS, 2, W>(a, a.spin, x0, y, z, nb, hf);
+    if constexpr (NB == 4 && CLS < 3) add_class<R, NB, CLS, 3, W>(a, a.spin, x0, y, z, nb, hf);
+    const uint32_t j0 = (uint32_t)row * (uint32_t)a.nx + (uint32_t)x0;
+    Run<R, W> S[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) S[c] = load_run<R, W>(own[c] + j0);
+    bool changed = false;
+#pragma unroll
+    for (int k = 0; k < W; ++k) {
+      V3<R> s = {S[0].v[k], S[1].v[k], S[2].v[k]};
+      if (UPDATE) {
+        const V3<R> h = {hf[0].v[k], hf[1].v[k], hf[2].v[k]};
+        const uint4 w = philox_ks(make_uint4(j0 + (uint32_t)k, key.sweep, (kTagHeis << 24) | ((uint32_t)CLS << 8),
+                                             key.replica),
+                                  key.ks);
+        V3<R> sn;
+        if (heis_update<R, PROP>(s, h, P, w, sn)) {
+          S[0].v[k] = sn.x;
+          S[1].v[k] = sn.y;
+          S[2].v[k] = sn.z;
+          s = sn;
+          changed = true;
+          acc[7] += (R)1;
+        }
+      }
+      if (MEASURE) {
+        const V3<R> low = {lo[0].v[k], lo[1].v[k], lo[2].v[k]};
+        add_site_sums(acc, s, low, P);
+      }
+    }
+    if (changed) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) store_run<R, W>(own[c] + j0, S[c]);
+    }
+  }
+  if (MEASURE) flush_sums(acc, part);
+}
+
+template <typename R, int NB, int CLS, int W>
+static void sub_go(const HeisSubArgs<R>& a, const HeisParams<R>& p, RngKey key, int proposal, bool update,
+                   double* part, int grid, int tpb, cudaStream_t s) {
+  const bool m = part != nullptr;
+  if (!update) {
+    heis_sub_kernel<R, NB, CLS, W, true, false, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, p, key, part);
+  } else if (proposal == VG_PROPOSE_RANDOM) {
+    if (m) heis_sub_kernel<R, NB, CLS, W, true, true, VG_PROPOSE_RANDOM><<<grid, tpb, 0, s>>>(a, p, key, part);
+    else heis_sub_kernel<R, NB, CLS, W, false, true, VG_PROPOSE_RANDOM><<<grid, tpb, 0, s>>>(a, p, key, part);
+  } else {
+    if (m) heis_sub_kernel<R, NB, CLS, W, true, true, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, p, key, part);
+    else heis_sub_kernel<R, NB, CLS, W, false, true, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, p, key, part);
+  }
+}
+
+template <typename R, int W>
+static void sub_cls(const HeisSubArgs<R>& a, int nb, const HeisParams<R>& p, RngKey key, int colour, int proposal,
+                    bool update, double* part, int grid, int tpb, cudaStream_t s) {
+  if (nb == 2) {
+    if (colour == 0) sub_go<R, 2, 0, W>(a, p, key, proposal, update, part, grid, tpb, s);
+    else sub_go<R, 2, 1, W>(a, p, key, proposal, update, part, grid, tpb, s);
+    return;
+  }
+  switch (colour) {
+    case 0: sub_go<R, 4, 0, W>(a, p, key, proposal, update, part, grid, tpb, s); break;
+    case 1: sub_go<R, 4, 1, W>(a, p, key, proposal, update, part, grid, tpb, s); break;
+    case 2: sub_go<R, 4, 2, W>(a, p, key, proposal, update, part, grid, tpb, s); break;
+    default: sub_go<R, 4, 3, W>(a, p, key, proposal, update, part, grid, tpb, s); break;
+  }
+}
+
+template <typename R>
+cudaError_t launch_heis_sub(const HeisSubArgs<R>& a, int nb, int W, const HeisParams<R>& p, RngKey key, int colour,
+                            int proposal, bool update, double* part, int grid, int tpb, cudaStream_t s) {
+  if (W == 4) sub_cls<R, 4>(a, nb, p, key, colour, proposal, update, part, grid, tpb, s);
+  else sub_cls<R, 1>(a, nb, p, key, colour, proposal, update, part, grid, tpb, s);
+  return cudaGetLastError();
+}
+
 template cudaError_t launch_heis_sc<float>(const HeisScArgs<float>&, const HeisParams<float>&, RngKey, int, int, bool,
                                            double*, int, int, cudaStream_t);
 template cudaError_t launch_heis_sc<double>(const HeisScArgs<double>&, const HeisParams<double>&, RngKey, int, int,
@@ -330,5 +440,9 @@ template cudaError_t launch_heis_gen<float>(const HeisGenArgs<float>&, const Hei
                                             bool, double*, int, int, cudaStream_t);
 template cudaError_t launch_heis_gen<double>(const HeisGenArgs<double>&, const HeisParams<double>&, RngKey, int, int,
                                              bool, double*, int, int, cudaStream_t);
+template cudaError_t launch_heis_sub<float>(const HeisSubArgs<float>&, int, int, const HeisParams<float>&, RngKey, int,
+                                            int, bool, double*, int, int, cudaStream_t);
+template cudaError_t launch_heis_sub<double>(const HeisSubArgs<double>&, int, int, const HeisParams<double>&, RngKey,
+                                             int, int, bool, double*, int, int, cudaStream_t);
 
 }  // namespace vg

@@ -168,6 +168,18 @@ struct HeisScArgs {           // sc checkerboard, class-separated SoA
 };
 
 template <typename R>
+struct HeisSubArgs {          // bcc / fcc: SoA planes per sublattice, [class][xyz][cell]
+  R* spin;
+  uint32_t ncell;             // cells per class (3 x classes x ncell < 2^32)
+  int nx, ny, nz;
+  int pbx, pby, pbz;
+  uint32_t runs;              // ncell / W
+  FastDiv frow;               // run index -> row (runs per row = nx / W)
+  FastDiv fny;
+  int rpr;                    // runs per row
+};
+
+template <typename R>
 struct HeisGenArgs {          // any lattice: natural order SoA + ELL
   R* x;
   R* y;
@@ -246,6 +258,11 @@ template <typename R>
 cudaError_t launch_heis_sc(const HeisScArgs<R>& a, const HeisParams<R>& p, RngKey key, int colour,
                            int proposal, bool update, double* part, int grid, int tpb,
                            cudaStream_t s);
+// bcc / fcc sublattice pass; nb = basis size, W = cells per run (4 when nx
+// is a multiple of 4, else 1).
+template <typename R>
+cudaError_t launch_heis_sub(const HeisSubArgs<R>& a, int nb, int W, const HeisParams<R>& p, RngKey key, int colour,
+                            int proposal, bool update, double* part, int grid, int tpb, cudaStream_t s);
 template <typename R>
 cudaError_t launch_heis_gen(const HeisGenArgs<R>& a, const HeisParams<R>& p, RngKey key, int colour,
                             int proposal, bool update, double* part, int grid, int tpb,
