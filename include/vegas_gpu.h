@@ -58,8 +58,8 @@ enum vg_proposal { VG_PROPOSE_FLIP = 0, VG_PROPOSE_RANDOM = 1 };
  * sites that admit STRUCTURED, else STRUCTURED when the lattice allows it,
  * else GENERIC.  STRUCTURED: sc lattices with an even x extent (Ising: x/2 a
  * multiple of 16) and even periodic y / z extents, as a checkerboard; bcc /
- * fcc Ising lattices with x a multiple of 16, one array per basis
- * sublattice.  GENERIC: any lattice, and per-bond exchange constants
+ * fcc Ising lattices with x a multiple of 16 and every bcc / fcc Heisenberg
+ * lattice, one array (Heisenberg: three planes) per basis sublattice.  GENERIC: any lattice, and per-bond exchange constants
  * (vg_set_exchange_bonds).  RESIDENT keeps the checkerboard layout of STRUCTURED in one
  * thread block's shared memory and runs all sweeps of a call in one launch
  * (Ising, at most 65536 sites); results are identical across paths. */

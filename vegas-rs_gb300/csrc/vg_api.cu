@@ -7,9 +7,10 @@
 //    [z][y][x/2]; Ising as uint8 0/1, Heisenberg as three planes (SoA) of
 //    FP32 or FP64.  A colour pass reads all of the other class and
 //    reads+writes its own: (C+1) x payload bytes per site per sweep.
-//  * bcc / fcc Ising lattices with x a multiple of 16 also use STRUCTURED:
-//    one uint8 0/1 array per basis sublattice (the colour classes),
-//    [class][cell] with cell = (z ny + y) nx + x.
+//  * bcc / fcc Ising lattices with x a multiple of 16, and every bcc / fcc
+//    Heisenberg lattice, also use STRUCTURED: one array per basis
+//    sublattice (the colour classes), [class][cell] uint8 0/1 for Ising and
+//    [class][xyz][cell] planes for Heisenberg, cell = (z ny + y) nx + x.
 //  * every other lattice uses the GENERIC path: natural-order spins plus,
 //    per colour class of a greedy colouring, the class's site list, an ELL
 //    neighbour table [z][n_c] and a lower-colour bit mask.
