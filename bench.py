@@ -293,6 +293,40 @@ def run_cooldown_2d(V, torch, args):
             "path": {1: "generic", 2: "structured", 3: "resident"}.get(path, "?"), "cpu_baseline": cpu}
 
 
+def run_sublattice(V, torch, args):
+    """bcc 128^3 cells (4,194,304 sites), full PBC, J=1: Ising (T = 3.0,
+    flip proposals) and Heisenberg (K = 0.1 along z, B = 0.05 along z, T = 1.0,
+    sphere proposals, FP32) through the sublattice kernels, each beside the
+    same sweeps on the neighbour-table (ELL) kernels; 20 measured sweeps per
+    timing, after 5 warm-up sweeps."""
+    out = {}
+    cases = (("ising", V.SPIN_ISING, V.hamiltonian(V.Exchange(1.0)), 3.0),
+             ("heisenberg", V.SPIN_HEISENBERG,
+              V.hamiltonian(V.Exchange(1.0), V.UniaxialAnisotropy((0, 0, 1), 0.1), V.Zeeman()), 1.0))
+    lat = V.Lattice.bcc(128, 128, 128)
+    n = 20
+    for name, spin, H, T in cases:
+        row = {}
+        for key, path in (("sublattice", V.PATH_STRUCTURED), ("ell", V.PATH_GENERIC)):
+            with V.Engine(lat, H, spin=spin, seed=SEED, path=path,
+                          proposal=V.PROPOSE_RANDOM if spin == V.SPIN_HEISENBERG else V.PROPOSE_FLIP) as eng:
+                eng.init_random()
+                eng.set_thermostat(T, (0, 0, 1), 0.05 if spin == V.SPIN_HEISENBERG else 0.0)
+                eng.sweeps(5)
+                s = torch.cuda.ExternalStream(eng.stream())
+                a, c = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(s)
+                eng.sweeps_async(n, measure=True)
+                c.record(s)
+                eng.synchronize()
+                row[key] = lat.n_sites * n / (a.elapsed_time(c) * 1e6)
+        out[name] = {"value": row["sublattice"], "ell_value": row["ell"], "unit": "flips/ns",
+                     "kernel": "ising_sub_kernel" if spin == V.SPIN_ISING else "heis_sub_kernel"}
+    return {"workload": "bcc 128^3 cells (4,194,304 sites) PBC J=1, Ising T=3.0 and Heisenberg T=1.0 K=0.1 B=0.05, "
+                        "20 measured sweeps, sublattice kernels beside the neighbour-table kernels",
+            **out}
+
+
 def run_wolff(V, torch, args):
     """docs/wolff.toml's workload shape: sc 10x10x10 Ising, Wolff cluster
     steps; a bounded sample of 20,000 steps at T = 4.5 (near the critical
@@ -623,6 +657,7 @@ def main():
 
     cool = run_cooldown_2d(V, torch, args) if not args.no_heisenberg else None
     wolff = run_wolff(V, torch, args) if not args.no_heisenberg else None
+    sub = run_sublattice(V, torch, args) if not args.no_heisenberg else None
     heis = hyst = None
     if not args.no_heisenberg:
         heis = run_heisenberg(V, torch, args)
@@ -661,6 +696,7 @@ def main():
             "batched_vs_plain": (batched["value"] / value) if batched else None,
             "cooldown_2d": cool,
             "wolff": wolff,
+            "sublattice": sub,
             "heisenberg": heis,
             "hysteresis_batch": hyst,
             "clocks": clk.summary(),

@@ -76,7 +76,7 @@ __device__ __forceinline__ R heis_delta_e(const V3<R>& s, const V3<R>& p, const 
   R de = -P.J * (dx * h.x + dy * h.y + dz * h.z);
   de += P.K * (pe * pe - se * se);
   de += P.hz * (dx * P.bx + dy * P.by + dz * P.bz);
-  de -= P.Kc * (quart(p) - quart(s));
+  if (P.Kc != (R)0) de -= P.Kc * (quart(p) - quart(s));  // skipped: the same value without the two quartics
   return de;
 }
 
