@@ -8,6 +8,7 @@ launches with -c), after the same command has run without the profiler.
     python vegas-rs_gb300/profile_cases.py ising_sizes N       # pass time for sc 64^3 .. 512^3
     python vegas-rs_gb300/profile_cases.py sub CELL L SWEEPS   # bcc / fcc L^3-cell Ising, sublattice passes
     python vegas-rs_gb300/profile_cases.py heis L SWEEPS       # sc L^3 Heisenberg, FP32
+    python vegas-rs_gb300/profile_cases.py heis_sub CELL L SWEEPS  # bcc / fcc L^3-cell Heisenberg, FP32
     python vegas-rs_gb300/profile_cases.py hbatch L REPLICAS   # fcc L^3 cells x replicas, field points
     python vegas-rs_gb300/profile_cases.py msc ROUNDS          # the 256-replica multi-spin-coded batch
 """
@@ -69,6 +70,19 @@ def heis(L, sweeps):
         print(f"heisenberg sc {L}^3: {sweeps} measured sweeps, {L ** 3 * sweeps / (dt * 1e9):.1f} flips/ns (wall)")
 
 
+def heis_sub(cell, L, sweeps):
+    lat = getattr(V.Lattice, cell)(L, L, L)
+    H = V.hamiltonian(V.Exchange(1.0), V.UniaxialAnisotropy((0, 0, 1), 0.1), V.Zeeman())
+    with V.Engine(lat, H, spin=V.SPIN_HEISENBERG, seed=1, path=V.PATH_STRUCTURED) as eng:
+        eng.init_random()
+        eng.set_thermostat(1.0, (0, 0, 1), 0.05)
+        t0 = time.perf_counter()
+        eng.sweeps(sweeps)
+        dt = time.perf_counter() - t0
+        print(f"heisenberg {cell} {L}^3 cells: {sweeps} measured sweeps, "
+              f"{lat.n_sites * sweeps / (dt * 1e9):.1f} flips/ns (wall)")
+
+
 def hbatch(L, nrep):
     lat = V.Lattice.fcc(L, L, L)
     reps = [V.HeisReplica(seed=11 + r, replica=r, temperature=0.5, cubic=0.05) for r in range(nrep)]
@@ -99,4 +113,4 @@ def msc(rounds):
 
 if __name__ == "__main__":
     case, args = sys.argv[1], [a if a in ("bcc", "fcc") else int(a) for a in sys.argv[2:]]
-    {"ising": ising, "ising_sizes": ising_sizes, "sub": sub, "heis": heis, "hbatch": hbatch, "msc": msc}[case](*args)
+    {"ising": ising, "ising_sizes": ising_sizes, "sub": sub, "heis": heis, "heis_sub": heis_sub, "hbatch": hbatch, "msc": msc}[case](*args)
