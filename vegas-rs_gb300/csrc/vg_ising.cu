@@ -792,8 +792,13 @@ __global__ void __launch_bounds__(256) ising_bond_kernel(const IsingGenArgs a, c
 // whole rows), except the edge entry when its x neighbour lies across an
 // open boundary.  A shared table per (nbe, spin) holds the thresholds' top
 // bytes for up-neighbour counts 0..15, looked up with two PRMTs per word;
-// the first random digit is compared byte-parallel and the rare ties (and
-// the odd edge entry) are decided from the full thresholds in line.
+// the first random digit is compared byte-parallel.  The rare ties (and the
+// odd edge entry) go to a block queue that the whole block decides from the
+// full thresholds after its runs (a warp would otherwise diverge into one
+// more Philox block for one or two lanes in most rounds); their flips and
+// sum changes are applied then.  Entries the queue has no room for are
+// decided in line.
+constexpr int kSubQueue = 512;  // tie entries per block
 
 // Top bytes of the thresholds of 16 entries packed 4 per word (nu = up
 // neighbours per byte, s = 0/1 spin per byte), from the 16-byte tables of
@@ -819,7 +824,11 @@ __global__ void __launch_bounds__(256, 4) ising_sub_kernel(const IsingSubArgs a,
   constexpr bool ALL_LOW = CLS == NB - 1;      // every neighbour class is lower
   __shared__ unsigned long long s_thr[2 * W];
   __shared__ uint4 s_top[ZC + 1][2];           // [nbe][spin]: top byte for nu = 0..15
+  // tie queue: (group, k | s01 << 4 | first << 5 | nu << 6 | ne << 10 | nl << 14 | lk << 18)
+  __shared__ uint2 s_tq[UPDATE ? kSubQueue : 1];
+  __shared__ int s_tn;
   pdl_launch_dependents();
+  if (threadIdx.x == 0) s_tn = 0;
   for (int i = threadIdx.x; i < 2 * W; i += blockDim.x) s_thr[i] = tab.thr[i];
   for (int i = threadIdx.x; i < (ZC + 1) * 32; i += blockDim.x) {
     const int nbe = i >> 5, s01 = (i >> 4) & 1, nu = i & 15;
@@ -938,7 +947,22 @@ __global__ void __launch_bounds__(256, 4) ising_sub_kernel(const IsingSubArgs a,
         tm |= gather4(bytes_zero(R[i] ^ thr) & cand[i]) << (4 * i);
       }
       if (emiss && ecand) tm |= 1u << edge;  // the edge entry starts at the first digit
-      if (tm) {
+      for (uint32_t m = tm; m; m &= m - 1u) {
+        const int k = __ffs(m) - 1;
+        const int slot = atomicAdd(&s_tn, 1);
+        if (slot < kSubQueue) {
+          const uint32_t s01 = byte_at(S[0], S[1], S[2], S[3], k);
+          const uint32_t nu = byte_at(A[0], A[1], A[2], A[3], k);
+          const uint32_t nl = byte_at(Lo[0], Lo[1], Lo[2], Lo[3], k);
+          const bool ek = k == edge && emiss;
+          const uint32_t ne = (uint32_t)(nbe - (ek ? emiss : 0));
+          const uint32_t lk = (uint32_t)(ZL - missL - (ek ? emissL : 0));
+          s_tq[slot] = make_uint2(g, (uint32_t)k | (s01 << 4) | ((uint32_t)ek << 5) | (nu << 6) | (ne << 10) |
+                                         (nl << 14) | (lk << 18));
+          tm &= ~(1u << k);
+        }
+      }
+      if (tm) {  // no room left in the queue
         const uint32_t nbe_e = (uint32_t)(nbe - emiss);
         uint32_t acc = 0u;
         for (int d = 0; d < 4 && tm; ++d) {
@@ -1002,6 +1026,38 @@ __global__ void __launch_bounds__(256, 4) ising_sub_kernel(const IsingSubArgs a,
         }
         const int se = (int)((Sn[edge >> 2] >> (8 * (edge & 3))) & 1u);
         bond += 4 * (int)snl - 2 * (L * (int)su - emissL * se) - 2 * (int)nls + 16 * L - emissL;
+      }
+    }
+  }
+  if (UPDATE) {  // the queued entries, one per thread
+    __syncthreads();
+    const int nq = s_tn < kSubQueue ? s_tn : kSubQueue;
+    for (int i = threadIdx.x; i < nq; i += blockDim.x) {
+      const uint2 e = s_tq[i];
+      const int k = (int)(e.y & 15u);
+      const uint32_t s01 = (e.y >> 4) & 1u, first = (e.y >> 5) & 1u, nu = (e.y >> 6) & 15u, ne = (e.y >> 10) & 15u;
+      const unsigned long long th = s_thr[s01 * W + 2 * (int)nu - (int)ne + ZC];
+      bool acc = th >= (1ull << 32), done = acc;
+      for (int d = first ? 0 : 1; d < 4 && !done; ++d) {
+        const uint4 bd = philox_ks(
+            make_uint4(e.x, key.sweep, (kTagIsingAccept << 24) | ((uint32_t)CLS << 8) | (uint32_t)d, key.replica),
+            key.ks);
+        const uint32_t ub = blk_byte(bd, k), tb = ((uint32_t)th >> (24 - 8 * d)) & 0xFFu;
+        if (ub != tb) {
+          acc = ub < tb;
+          done = true;
+        }
+      }
+      if (acc) {  // U < thr; a tie on every digit (U == thr) rejects
+        own[(size_t)e.x * 16 + k] = (uint8_t)(s01 ^ 1u);
+        if (MEASURE) {
+          ups += 1 - 2 * (int)s01;
+          nacc += 1;
+          if (CLS > 0) {
+            const int nl = (int)((e.y >> 14) & 15u), lk = (int)((e.y >> 18) & 15u);
+            bond -= 2 * (2 * (int)s01 - 1) * (2 * nl - lk);
+          }
+        }
       }
     }
   }
