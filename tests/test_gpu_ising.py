@@ -111,6 +111,27 @@ def test_sublattice_and_generic_paths_agree(V, cell, ext, pbc, proposal):
     assert out[0][2] == out[1][2] and out[0][3] == out[1][3]
 
 
+def test_sublattice_tie_queue_overflow_matches_generic(V):
+    """A block keeps at most 512 tied entries for after its runs and decides
+    the rest in line: with one warp per SM walking ~320 runs per thread
+    (~650 ties per block) both happen; the result equals the ELL kernel's."""
+    ext = (1024, 192, 128)
+    H = V.hamiltonian(V.Exchange(1.0), V.Zeeman())
+    out = []
+    for path, opts in ((V.PATH_STRUCTURED, dict(threads_per_block=32, blocks_per_sm=1)), (V.PATH_GENERIC, {})):
+        with _engine(V, "bcc", ext, (1, 1, 1), H, 31, path=path, **opts) as eng:
+            assert eng.info().path == path
+            if path == V.PATH_STRUCTURED:
+                groups = ext[0] * ext[1] * ext[2] // 16
+                assert groups // (eng.info().grid_blocks * 32) * 32 // 16 > 512
+            eng.init_random()
+            eng.set_thermostat(3.0, (0, 0, 1), 0.1)
+            sums = eng.sweeps_sums(2)
+            out.append((eng.get_state(), sums))
+    assert np.array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
+
+
 def test_sublattice_needs_x_multiple_of_16(V):
     H = V.hamiltonian(V.Exchange(1.0))
     with pytest.raises(V.VegasGpuError) as e:
