@@ -198,6 +198,14 @@ int vg_time_passes(vg_ctx* ctx, uint64_t n, int32_t measure, double* mean_pass_m
  * exchange constant only (no per-bond constants). */
 int vg_wolff_steps(vg_ctx* ctx, uint64_t n_steps, int32_t measure, double* E, double* M);
 
+/* Self-test of the bounded waits of the grid barrier vg_wolff_steps uses on
+ * large lattices (no reference counterpart): one barrier over four blocks of
+ * a cooperative launch on the context's device and stream.  With
+ * skip_block in [0, 4) that block never arrives and the others' waits run
+ * out after 2 s: VG_ERR_TIMEOUT.  Otherwise VG_OK.  The context stays
+ * usable either way. */
+int vg_selftest_grid_barrier(vg_ctx* ctx, int32_t skip_block);
+
 /* Per-bond exchange constants: Exchange's CSR with arbitrary J_ij
  * (src/energy.rs:169-206) instead of one constant for every bond.
  * J[i * z + k] is the constant of the bond from site i to its k-th

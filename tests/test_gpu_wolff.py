@@ -156,3 +156,37 @@ def test_cli_runs_the_wolff_input(tmp_path):
     # ordered at T = 1: energy per spin near the ground state of the Compound total (-6)
     assert rows[-1][2] / 1000 < -5.5 and rows[-1][4] / 1000 > 0.95
     assert (tmp_path / "obs.parquet").exists()
+
+
+def test_grid_barrier_wait_runs_out_and_context_stays_usable(V):
+    """A grid barrier one block never reaches: the others' bounded waits end
+    after 2 s with VG_ERR_TIMEOUT (no fault, no hang); the same context then
+    completes a barrier and runs multi-block Wolff steps bit-exactly."""
+    import time
+
+    lib = V.lib()
+    with V.Engine(V.Lattice.sc(8, 8, 8), V.hamiltonian(V.Exchange(1.0)), seed=3) as eng:
+        assert lib.vg_selftest_grid_barrier(eng._h, -1) == 0
+        t0 = time.perf_counter()
+        assert lib.vg_selftest_grid_barrier(eng._h, 2) == 3  # VG_ERR_TIMEOUT
+        assert 1.5 < time.perf_counter() - t0 < 30.0
+        assert b"ran out" in lib.vg_last_error(eng._h)
+        assert lib.vg_selftest_grid_barrier(eng._h, -1) == 0
+        eng.init_random()
+        eng.set_thermostat(4.5)
+        eng.sweeps(2)
+
+
+def test_grid_wolff_after_barrier_self_test(V, O):
+    """The self-test's barrier block does not stand in for the multi-block
+    kernel's other buffers: a grid Wolff run on the same context is exact."""
+    lat = V.Lattice.sc(96, 96, 96)
+    with V.Engine(lat, V.hamiltonian(V.Exchange(1.0)), seed=12) as eng:
+        assert V.lib().vg_selftest_grid_barrier(eng._h, 1) == 3
+        eng.init_random()
+        s0 = eng.get_state()
+        eng.set_thermostat(4.5)
+        eng.wolff_steps(3)
+        g = O.Graph(O.lattice("sc", 96, 96, 96))
+        ref, _ = g.wolff_steps(s0, 1.0, 4.5, 12, 0, 3)
+        assert np.array_equal(eng.get_state(), ref)

@@ -1491,10 +1491,8 @@ int vg_wolff_steps(vg_ctx* c, uint64_t n, int32_t measure, double* E, double* M)
   const bool mid = c->n > kWolffMaxSites && c->n <= kWolffMidSites;
   const bool grid = c->n > kWolffMidSites;
   if ((mid || grid) && !c->d_wq && (rc = dalloc(c, (void**)&c->d_wq, sizeof(int32_t) * (size_t)c->n))) return rc;
-  if (grid && !c->d_wgrid) {
-    if ((rc = dalloc(c, (void**)&c->d_wmark, sizeof(uint32_t) * (size_t)c->n))) return rc;
-    if ((rc = dalloc(c, (void**)&c->d_wgrid, sizeof(WolffGrid)))) return rc;
-  }
+  if (grid && !c->d_wmark && (rc = dalloc(c, (void**)&c->d_wmark, sizeof(uint32_t) * (size_t)c->n))) return rc;
+  if (grid && !c->d_wgrid && (rc = dalloc(c, (void**)&c->d_wgrid, sizeof(WolffGrid)))) return rc;
   // bond probability 1 - exp(-2 J / T) as a threshold on a 32-bit word (src/integrator.rs:199-203)
   const double J = c->ham.has_exchange ? c->ham.exchange : 0.0;
   const double T = clamp_temperature(c->T);
@@ -1548,6 +1546,21 @@ int vg_wolff_steps(vg_ctx* c, uint64_t n, int32_t measure, double* E, double* M)
     finish_sums(c, raw + t * kNumSums, &s);
     energy_of(c, &s, E ? E + t : nullptr, M ? M + t : nullptr);
   }
+  return VG_OK;
+}
+
+int vg_selftest_grid_barrier(vg_ctx* c, int32_t skip_block) {
+  if (!c) return VG_ERR_INVALID_ARG;
+  VG_CUDA(c, cudaSetDevice(c->device));
+  int rc;
+  if (!c->d_wgrid && (rc = dalloc(c, (void**)&c->d_wgrid, sizeof(WolffGrid)))) return rc;
+  const int skip = skip_block >= 0 && skip_block < 4 ? skip_block : -1;
+  const cudaError_t e = launch_wolff_barrier_probe(c->d_wgrid, 4, skip, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "barrier self-test launch");
+  unsigned int aborted = 0;
+  VG_CUDA(c, cudaMemcpyAsync(&aborted, &c->d_wgrid->abort_flag, sizeof(aborted), cudaMemcpyDeviceToHost, c->stream));
+  VG_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (aborted) return fail(c, VG_ERR_TIMEOUT, "grid barrier self-test: a wait ran out (2 s)");
   return VG_OK;
 }
 

@@ -227,6 +227,10 @@ struct WolffGrid {
   unsigned long long cut;             // this step's sum of boundary spins (two's complement)
   unsigned long long bond0, ups0;     // sums of the incoming state
 };
+// One grid barrier over `blocks` blocks of 32 threads (a cooperative launch)
+// where block `skip` (none if skip < 0) never arrives; g->abort_flag tells
+// whether a wait ran out.
+cudaError_t launch_wolff_barrier_probe(WolffGrid* g, int blocks, int skip, cudaStream_t s);
 cudaError_t launch_ising_wolff_grid(int8_t* spins, int n, int z, const int32_t* nbr, const uint8_t* occ,
                                     unsigned long long thr, RngKey key, uint32_t n_steps, double* sums,
                                     uint32_t* mark, int32_t* q, WolffGrid* g, int sm_count, cudaStream_t s);

@@ -457,7 +457,24 @@ __global__ void __launch_bounds__(1024) ising_wolff_mid_kernel(int8_t* __restric
   for (int i = threadIdx.x; i < n; i += blockDim.x) spins[i] = (int8_t)spin_of(i);
 }
 
+// Self-test of the barrier's bounded wait: block `skip` (none for skip < 0)
+// never arrives, so the other blocks' waits run out after 2 s and set
+// g->abort_flag; with every block arriving the barrier completes.  The wait
+// ends either way: nothing here spins without a limit.
+__global__ void wolff_barrier_probe_kernel(WolffGrid* g, int skip) {
+  if ((int)blockIdx.x == skip) return;
+  grid_barrier(g, nullptr, nullptr);
+}
+
 }  // namespace
+
+cudaError_t launch_wolff_barrier_probe(WolffGrid* g, int blocks, int skip, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(g, 0, sizeof(WolffGrid), s);
+  if (e != cudaSuccess) return e;
+  void* args[] = {&g, &skip};
+  return cudaLaunchCooperativeKernel((const void*)wolff_barrier_probe_kernel, dim3((unsigned)blocks), dim3(32), args,
+                                     0, s);
+}
 
 size_t ising_wolff_smem(int n) { return (size_t)n * 9; }
 

@@ -151,6 +151,7 @@ SIGNATURES = {
                                              C.c_uint32, C.c_uint64, C.c_uint64, C.c_void_p, C.c_void_p,
                                              C.c_void_p, C.c_void_p]),
     "vg_wolff_steps": (C.c_int, [C.c_void_p, C.c_uint64, C.c_int32, P(C.c_double), P(C.c_double)]),
+    "vg_selftest_grid_barrier": (C.c_int, [C.c_void_p, C.c_int32]),
     "vg_set_exchange_bonds": (C.c_int, [C.c_void_p, P(C.c_double), C.c_int64]),
     "vg_site_energies": (C.c_int, [C.c_void_p, P(C.c_double), C.c_int64]),
     "vg_delta_energies": (C.c_int, [C.c_void_p, P(C.c_double), P(C.c_double), C.c_int64]),
