@@ -75,8 +75,6 @@ struct MscDev {
   uint32_t pad;
 };
 
-__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;"); }
-__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
 // (b2 b1 b0) = number of set lanes among the inputs, per lane
 __device__ __forceinline__ void count6(uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t a4, uint32_t a5,
@@ -552,21 +550,6 @@ void bdestroy(vg_batch* b) {
   delete b;
 }
 
-template <typename... P, typename... A>
-cudaError_t launch_pdl(void (*kern)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, A&&... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = grid;
-  cfg.blockDim = block;
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = s;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, kern, std::forward<A>(args)...);
-}
-
 using MscPassFn = void (*)(const MscSeg*, const int2*, const uint32_t*, const MscDev*, uint32_t, KeySchedule, int);
 
 template <int C, int TPB>
@@ -611,9 +594,9 @@ int enqueue_round(vg_batch* b) {
   const dim3 tpb((unsigned)b->tune.threads_per_block);
   for (int t = 0; t < b->every; ++t) {
     const int jsign = b->J > 0.0 ? 1 : b->J < 0.0 ? -1 : 0;
-    VG_BCUDA(b, launch_pdl(p0, dim3(nb), tpb, 0, b->stream, (const MscSeg*)b->d_segs, (const int2*)b->d_blocks,
+    VG_BCUDA(b, launch_pdl_ex(p0, dim3(nb), tpb, 0, b->stream, (const MscSeg*)b->d_segs, (const int2*)b->d_blocks,
                            (const uint32_t*)b->d_tabs, (const MscDev*)b->d_dev, (uint32_t)t, b->ks, jsign));
-    VG_BCUDA(b, launch_pdl(p1, dim3(nb), tpb, 0, b->stream, (const MscSeg*)b->d_segs, (const int2*)b->d_blocks,
+    VG_BCUDA(b, launch_pdl_ex(p1, dim3(nb), tpb, 0, b->stream, (const MscSeg*)b->d_segs, (const int2*)b->d_blocks,
                            (const uint32_t*)b->d_tabs, (const MscDev*)b->d_dev, (uint32_t)t, b->ks, jsign));
   }
   msc_measure<<<nb, 256, 0, b->stream>>>(b->d_segs, b->d_blocks,

@@ -32,6 +32,8 @@ __global__ void __launch_bounds__(256) heis_sc_kernel(const HeisScArgs<R> a, con
   R acc[kNumSums];
 #pragma unroll
   for (int i = 0; i < kNumSums; ++i) acc[i] = (R)0;
+  pdl_launch_dependents();
+  pdl_wait();
   const uint32_t stride = gridDim.x * blockDim.x;
   for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < a.n_c; j += stride) {
     const int row = (int)fdiv(j, a.fHx);
@@ -99,6 +101,8 @@ __global__ void __launch_bounds__(256) heis_sc4_kernel(const HeisScArgs<R> a, co
   R acc[kNumSums];
 #pragma unroll
   for (int i = 0; i < kNumSums; ++i) acc[i] = (R)0;
+  pdl_launch_dependents();
+  pdl_wait();
   const uint32_t n4 = a.n_c >> 2;
   const uint32_t stride = gridDim.x * blockDim.x;
   for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n4; q += stride) {
@@ -203,6 +207,8 @@ __global__ void __launch_bounds__(256) heis_gen_kernel(const HeisGenArgs<R> a, c
   R acc[kNumSums];
 #pragma unroll
   for (int i = 0; i < kNumSums; ++i) acc[i] = (R)0;
+  pdl_launch_dependents();
+  pdl_wait();
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < a.n_c; j += stride) {
     const int i = __ldg(a.sites + j);
@@ -250,13 +256,13 @@ static void sc_go(const HeisScArgs<R>& a, const HeisParams<R>& p, RngKey key, in
                   int grid, int tpb, cudaStream_t s) {
   const bool m = part != nullptr;
   if (!update) {
-    heis_sc_kernel<R, C, ALLPER, true, false, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, p, key, part);
+    launch_pdl(heis_sc_kernel<R, C, ALLPER, true, false, VG_PROPOSE_FLIP>, grid, tpb, s, a, p, key, part);
   } else if (proposal == VG_PROPOSE_RANDOM) {
-    if (m) heis_sc_kernel<R, C, ALLPER, true, true, VG_PROPOSE_RANDOM><<<grid, tpb, 0, s>>>(a, p, key, part);
-    else heis_sc_kernel<R, C, ALLPER, false, true, VG_PROPOSE_RANDOM><<<grid, tpb, 0, s>>>(a, p, key, part);
+    if (m) launch_pdl(heis_sc_kernel<R, C, ALLPER, true, true, VG_PROPOSE_RANDOM>, grid, tpb, s, a, p, key, part);
+    else launch_pdl(heis_sc_kernel<R, C, ALLPER, false, true, VG_PROPOSE_RANDOM>, grid, tpb, s, a, p, key, part);
   } else {
-    if (m) heis_sc_kernel<R, C, ALLPER, true, true, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, p, key, part);
-    else heis_sc_kernel<R, C, ALLPER, false, true, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, p, key, part);
+    if (m) launch_pdl(heis_sc_kernel<R, C, ALLPER, true, true, VG_PROPOSE_FLIP>, grid, tpb, s, a, p, key, part);
+    else launch_pdl(heis_sc_kernel<R, C, ALLPER, false, true, VG_PROPOSE_FLIP>, grid, tpb, s, a, p, key, part);
   }
 }
 
@@ -265,13 +271,13 @@ static void sc4_go(const HeisScArgs<R>& a, const HeisParams<R>& p, RngKey key, i
                    int grid, int tpb, cudaStream_t s) {
   const bool m = part != nullptr;
   if (!update) {
-    heis_sc4_kernel<R, C, ALLPER, true, false, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, p, key, part);
+    launch_pdl(heis_sc4_kernel<R, C, ALLPER, true, false, VG_PROPOSE_FLIP>, grid, tpb, s, a, p, key, part);
   } else if (proposal == VG_PROPOSE_RANDOM) {
-    if (m) heis_sc4_kernel<R, C, ALLPER, true, true, VG_PROPOSE_RANDOM><<<grid, tpb, 0, s>>>(a, p, key, part);
-    else heis_sc4_kernel<R, C, ALLPER, false, true, VG_PROPOSE_RANDOM><<<grid, tpb, 0, s>>>(a, p, key, part);
+    if (m) launch_pdl(heis_sc4_kernel<R, C, ALLPER, true, true, VG_PROPOSE_RANDOM>, grid, tpb, s, a, p, key, part);
+    else launch_pdl(heis_sc4_kernel<R, C, ALLPER, false, true, VG_PROPOSE_RANDOM>, grid, tpb, s, a, p, key, part);
   } else {
-    if (m) heis_sc4_kernel<R, C, ALLPER, true, true, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, p, key, part);
-    else heis_sc4_kernel<R, C, ALLPER, false, true, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, p, key, part);
+    if (m) launch_pdl(heis_sc4_kernel<R, C, ALLPER, true, true, VG_PROPOSE_FLIP>, grid, tpb, s, a, p, key, part);
+    else launch_pdl(heis_sc4_kernel<R, C, ALLPER, false, true, VG_PROPOSE_FLIP>, grid, tpb, s, a, p, key, part);
   }
 }
 
@@ -304,13 +310,13 @@ static void gen_go(const HeisGenArgs<R>& a, const HeisParams<R>& p, RngKey key, 
                    double* part, int grid, int tpb, cudaStream_t s) {
   const bool m = part != nullptr;
   if (!update) {
-    heis_gen_kernel<R, ZT, true, false, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, p, key, colour, part);
+    launch_pdl(heis_gen_kernel<R, ZT, true, false, VG_PROPOSE_FLIP>, grid, tpb, s, a, p, key, colour, part);
   } else if (proposal == VG_PROPOSE_RANDOM) {
-    if (m) heis_gen_kernel<R, ZT, true, true, VG_PROPOSE_RANDOM><<<grid, tpb, 0, s>>>(a, p, key, colour, part);
-    else heis_gen_kernel<R, ZT, false, true, VG_PROPOSE_RANDOM><<<grid, tpb, 0, s>>>(a, p, key, colour, part);
+    if (m) launch_pdl(heis_gen_kernel<R, ZT, true, true, VG_PROPOSE_RANDOM>, grid, tpb, s, a, p, key, colour, part);
+    else launch_pdl(heis_gen_kernel<R, ZT, false, true, VG_PROPOSE_RANDOM>, grid, tpb, s, a, p, key, colour, part);
   } else {
-    if (m) heis_gen_kernel<R, ZT, true, true, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, p, key, colour, part);
-    else heis_gen_kernel<R, ZT, false, true, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, p, key, colour, part);
+    if (m) launch_pdl(heis_gen_kernel<R, ZT, true, true, VG_PROPOSE_FLIP>, grid, tpb, s, a, p, key, colour, part);
+    else launch_pdl(heis_gen_kernel<R, ZT, false, true, VG_PROPOSE_FLIP>, grid, tpb, s, a, p, key, colour, part);
   }
 }
 
@@ -338,6 +344,8 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 2) heis_sub_kernel(c
   R acc[kNumSums];
 #pragma unroll
   for (int i = 0; i < kNumSums; ++i) acc[i] = (R)0;
+  pdl_launch_dependents();
+  pdl_wait();
   const uint32_t stride = gridDim.x * blockDim.x;
   for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < a.runs; u += stride) {
     const int row = (int)fdiv(u, a.frow);
@@ -398,13 +406,13 @@ static void sub_go(const HeisSubArgs<R>& a, const HeisParams<R>& p, RngKey key, 
                    double* part, int grid, int tpb, cudaStream_t s) {
   const bool m = part != nullptr;
   if (!update) {
-    heis_sub_kernel<R, NB, CLS, W, true, false, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, p, key, part);
+    launch_pdl(heis_sub_kernel<R, NB, CLS, W, true, false, VG_PROPOSE_FLIP>, grid, tpb, s, a, p, key, part);
   } else if (proposal == VG_PROPOSE_RANDOM) {
-    if (m) heis_sub_kernel<R, NB, CLS, W, true, true, VG_PROPOSE_RANDOM><<<grid, tpb, 0, s>>>(a, p, key, part);
-    else heis_sub_kernel<R, NB, CLS, W, false, true, VG_PROPOSE_RANDOM><<<grid, tpb, 0, s>>>(a, p, key, part);
+    if (m) launch_pdl(heis_sub_kernel<R, NB, CLS, W, true, true, VG_PROPOSE_RANDOM>, grid, tpb, s, a, p, key, part);
+    else launch_pdl(heis_sub_kernel<R, NB, CLS, W, false, true, VG_PROPOSE_RANDOM>, grid, tpb, s, a, p, key, part);
   } else {
-    if (m) heis_sub_kernel<R, NB, CLS, W, true, true, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, p, key, part);
-    else heis_sub_kernel<R, NB, CLS, W, false, true, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, p, key, part);
+    if (m) launch_pdl(heis_sub_kernel<R, NB, CLS, W, true, true, VG_PROPOSE_FLIP>, grid, tpb, s, a, p, key, part);
+    else launch_pdl(heis_sub_kernel<R, NB, CLS, W, false, true, VG_PROPOSE_FLIP>, grid, tpb, s, a, p, key, part);
   }
 }
 

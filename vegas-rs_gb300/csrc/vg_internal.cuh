@@ -5,9 +5,39 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <utility>
+
 #include "vegas_gpu.h"
 
 namespace vg {
+
+// Programmatic dependent launch: a colour pass lets the next one launch
+// while it drains, and every pass waits for its predecessor's writes
+// (griddepcontrol.wait) before touching spins or partial sums.  Both are
+// no-ops for kernels launched without the PDL attribute.
+__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+// Launch with programmatic stream serialization (kernels that call pdl_wait
+// before reading what their predecessor wrote).
+template <typename... P, typename... A>
+cudaError_t launch_pdl_ex(void (*kern)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, A&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, std::forward<A>(args)...);
+}
+template <typename... P, typename... A>
+cudaError_t launch_pdl(void (*kern)(P...), int grid, int tpb, cudaStream_t s, A&&... args) {
+  return launch_pdl_ex(kern, dim3(grid), dim3(tpb), 0, s, std::forward<A>(args)...);
+}
 
 constexpr int kMaxZ = 12;          // fcc coordination
 constexpr int kMaxColours = 16;

@@ -122,13 +122,6 @@ __device__ __forceinline__ void block_sum3_store(int a, int b, int c, long long*
   }
 }
 
-// Programmatic dependent launch: let the next colour pass launch while this
-// one drains, and make every pass wait for its predecessor's writes before
-// touching spins.  Both are no-ops for kernels launched without the PDL
-// attribute.
-__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;"); }
-__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
-
 // Resolution of ties deferred to whole warps: a queued site (group gid,
 // site k, spin s, up-neighbour count nu) tied with its threshold on digit 0;
 // digits 1..3 decide it exactly as the in-line rule would.  Returns whether
@@ -1065,24 +1058,6 @@ __global__ void __launch_bounds__(256, 4) ising_sub_kernel(const IsingSubArgs a,
 }
 
 // ------------------------------------------------------------ dispatch
-// Launch with programmatic stream serialization: the kernel may start while
-// its predecessor on the stream drains and waits (griddepcontrol.wait) for
-// that predecessor's completion before reading spins.
-template <typename... P, typename... A>
-static cudaError_t launch_pdl(void (*kern)(P...), int grid, int tpb, cudaStream_t s, A&&... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(grid);
-  cfg.blockDim = dim3(tpb);
-  cfg.dynamicSmemBytes = 0;
-  cfg.stream = s;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, kern, std::forward<A>(args)...);
-}
-
 template <int C, bool UNIFORM>
 static cudaError_t sc_dispatch(const IsingScArgs& a, const IsingTable& tab, RngKey key, int proposal, bool update,
                                long long* part, int grid, int tpb, cudaStream_t s) {
