@@ -669,8 +669,10 @@ __global__ void __launch_bounds__(256, 4) ising_gen_kernel(const IsingGenArgs a,
   __shared__ unsigned long long s_thr[2 * W];
   const int z = a.z;
   const int Wz = 2 * z + 1;
+  pdl_launch_dependents();
   for (int i = threadIdx.x; i < 2 * Wz; i += blockDim.x) s_thr[i] = tab.thr[i];
   __syncthreads();
+  pdl_wait();
 
   int bond = 0, ups = 0, nacc = 0;  // per thread: a few entries of at most +-z each
   const long long stride = (long long)gridDim.x * blockDim.x;
@@ -718,6 +720,8 @@ __global__ void __launch_bounds__(256, 4) ising_gen_kernel(const IsingGenArgs a,
 template <int ZT, bool MEASURE, bool UPDATE, int PROP>
 __global__ void __launch_bounds__(256) ising_bond_kernel(const IsingGenArgs a, const RngKey key, const int colour,
                                                          double* __restrict__ part) {
+  pdl_launch_dependents();
+  pdl_wait();
   double bond = 0.0, ups = 0.0, nacc = 0.0;
   const int z = a.z;
   const long long stride = (long long)gridDim.x * blockDim.x;
@@ -1128,13 +1132,13 @@ static cudaError_t gen_dispatch(const IsingGenArgs& a, const IsingTable& tab, Rn
                                 bool update, long long* part, int grid, int tpb, cudaStream_t s) {
   const bool m = part != nullptr;
   if (!update) {
-    ising_gen_kernel<ZT, true, false, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, tab, key, colour, part);
+    launch_pdl(ising_gen_kernel<ZT, true, false, VG_PROPOSE_FLIP>, grid, tpb, s, a, tab, key, colour, part);
   } else if (proposal == VG_PROPOSE_FLIP) {
-    if (m) ising_gen_kernel<ZT, true, true, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, tab, key, colour, part);
-    else ising_gen_kernel<ZT, false, true, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, tab, key, colour, part);
+    if (m) launch_pdl(ising_gen_kernel<ZT, true, true, VG_PROPOSE_FLIP>, grid, tpb, s, a, tab, key, colour, part);
+    else launch_pdl(ising_gen_kernel<ZT, false, true, VG_PROPOSE_FLIP>, grid, tpb, s, a, tab, key, colour, part);
   } else {
-    if (m) ising_gen_kernel<ZT, true, true, VG_PROPOSE_RANDOM><<<grid, tpb, 0, s>>>(a, tab, key, colour, part);
-    else ising_gen_kernel<ZT, false, true, VG_PROPOSE_RANDOM><<<grid, tpb, 0, s>>>(a, tab, key, colour, part);
+    if (m) launch_pdl(ising_gen_kernel<ZT, true, true, VG_PROPOSE_RANDOM>, grid, tpb, s, a, tab, key, colour, part);
+    else launch_pdl(ising_gen_kernel<ZT, false, true, VG_PROPOSE_RANDOM>, grid, tpb, s, a, tab, key, colour, part);
   }
   return cudaGetLastError();
 }
@@ -1144,13 +1148,13 @@ static cudaError_t bond_dispatch(const IsingGenArgs& a, RngKey key, int colour, 
                                  double* part, int grid, int tpb, cudaStream_t s) {
   const bool m = part != nullptr;
   if (!update) {
-    ising_bond_kernel<ZT, true, false, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, key, colour, part);
+    launch_pdl(ising_bond_kernel<ZT, true, false, VG_PROPOSE_FLIP>, grid, tpb, s, a, key, colour, part);
   } else if (proposal == VG_PROPOSE_FLIP) {
-    if (m) ising_bond_kernel<ZT, true, true, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, key, colour, part);
-    else ising_bond_kernel<ZT, false, true, VG_PROPOSE_FLIP><<<grid, tpb, 0, s>>>(a, key, colour, part);
+    if (m) launch_pdl(ising_bond_kernel<ZT, true, true, VG_PROPOSE_FLIP>, grid, tpb, s, a, key, colour, part);
+    else launch_pdl(ising_bond_kernel<ZT, false, true, VG_PROPOSE_FLIP>, grid, tpb, s, a, key, colour, part);
   } else {
-    if (m) ising_bond_kernel<ZT, true, true, VG_PROPOSE_RANDOM><<<grid, tpb, 0, s>>>(a, key, colour, part);
-    else ising_bond_kernel<ZT, false, true, VG_PROPOSE_RANDOM><<<grid, tpb, 0, s>>>(a, key, colour, part);
+    if (m) launch_pdl(ising_bond_kernel<ZT, true, true, VG_PROPOSE_RANDOM>, grid, tpb, s, a, key, colour, part);
+    else launch_pdl(ising_bond_kernel<ZT, false, true, VG_PROPOSE_RANDOM>, grid, tpb, s, a, key, colour, part);
   }
   return cudaGetLastError();
 }
