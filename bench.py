@@ -429,7 +429,9 @@ def run_heisenberg(V, torch, args):
             ms = sum(a.elapsed_time(c) for a, c in ev)
             pass_ms, _ = eng.time_passes(20, measure=False)
             key = "fp32" if prec == V.FP32 else "fp64"
-            out[key] = {"value": lat.n_sites * sweeps * steps / (ms * 1e6), "pass_ms": pass_ms}
+            # average pass over the timed sweeps (as the headline), and one pass timed alone
+            out[key] = {"value": lat.n_sites * sweeps * steps / (ms * 1e6), "pass_ms": ms / (steps * sweeps * 2),
+                        "pass_ms_isolated": pass_ms}
             if prec == V.FP32:
                 st = eng.get_state().reshape(n_l, n_l, n_l, 3)
                 got = eng.current_sums()
@@ -455,7 +457,8 @@ def run_heisenberg(V, torch, args):
             "value": out["fp32"]["value"], "unit": "flips/ns", "sweeps_per_step": sweeps,
             "fp64_value": out["fp64"]["value"], "bytes_per_flip": 36.0,
             "roofline": {"achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                         "pass_ms": out["fp32"]["pass_ms"], "kernel": "heis_sc4_kernel (one colour pass)"},
+                         "pass_ms": out["fp32"]["pass_ms"], "pass_ms_isolated": out["fp32"]["pass_ms_isolated"],
+                         "kernel": "heis_sc4_kernel (one colour pass, measured sweeps)"},
             "sum_rel_err_vs_fp64_recompute": out["sum_rel_err"]}
 
 
