@@ -96,12 +96,9 @@ __device__ __forceinline__ uint32_t byte_at(uint32_t w0, uint32_t w1, uint32_t w
 __device__ __forceinline__ void block_sum3_store(int a, int b, int c, long long* out) {
   __shared__ int red[3][32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    a += __shfl_down_sync(0xffffffffu, a, o);
-    b += __shfl_down_sync(0xffffffffu, b, o);
-    c += __shfl_down_sync(0xffffffffu, c, o);
-  }
+  a = __reduce_add_sync(0xffffffffu, a);
+  b = __reduce_add_sync(0xffffffffu, b);
+  c = __reduce_add_sync(0xffffffffu, c);
   if (lane == 0) {
     red[0][warp] = a;
     red[1][warp] = b;

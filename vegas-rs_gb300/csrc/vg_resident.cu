@@ -174,13 +174,11 @@ __global__ void __launch_bounds__(MAXT) ising_resident_kernel(IsingScArgs a, Isi
       }
       if (C == 0) __syncthreads();
     }
-    // sweep sums: per warp, then over the warps by warp 0
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      bond += __shfl_down_sync(0xffffffffu, bond, o);
-      ups += __shfl_down_sync(0xffffffffu, ups, o);
-      nacc += __shfl_down_sync(0xffffffffu, nacc, o);
-    }
+    // sweep sums: per warp (one warp-reduce instruction each), then over the
+    // warps by warp 0, off the next pass's path
+    bond = __reduce_add_sync(0xffffffffu, bond);
+    ups = __reduce_add_sync(0xffffffffu, ups);
+    nacc = __reduce_add_sync(0xffffffffu, nacc);
     int (*red)[32] = s_red[t & 1];
     if (lane == 0) {
       red[0][warp] = bond;
@@ -191,12 +189,9 @@ __global__ void __launch_bounds__(MAXT) ising_resident_kernel(IsingScArgs a, Isi
     if (warp == 0 && sums) {
       int b = lane < nwarp ? red[0][lane] : 0, u = lane < nwarp ? red[1][lane] : 0,
           c = lane < nwarp ? red[2][lane] : 0;
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        b += __shfl_down_sync(0xffffffffu, b, o);
-        u += __shfl_down_sync(0xffffffffu, u, o);
-        c += __shfl_down_sync(0xffffffffu, c, o);
-      }
+      b = __reduce_add_sync(0xffffffffu, b);
+      u = __reduce_add_sync(0xffffffffu, u);
+      c = __reduce_add_sync(0xffffffffu, c);
       if (lane == 0) {
         double* o = sums + (size_t)t * kNumSums;
         o[0] = (double)b;
