@@ -67,11 +67,8 @@ __global__ void __launch_bounds__(1024) ising_wolff_kernel(int8_t* __restrict__ 
         if (j > i) b += si * s[j];
       }
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      b += __shfl_down_sync(0xffffffffu, b, o);
-      u += __shfl_down_sync(0xffffffffu, u, o);
-    }
+    b = __reduce_add_sync(0xffffffffu, b);
+    u = __reduce_add_sync(0xffffffffu, u);
     if (lane == 0) {
       s_red[0][warp] = b;
       s_red[1][warp] = u;
@@ -127,8 +124,7 @@ __global__ void __launch_bounds__(1024) ising_wolff_kernel(int8_t* __restrict__ 
       if (k == 0) s[site] = (int8_t)(-ref);
     }
     if (sums) {
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) cut += __shfl_down_sync(0xffffffffu, cut, o);
+      cut = __reduce_add_sync(0xffffffffu, cut);
       if (lane == 0 && cut) atomicAdd(&s_cut, cut);
     }
     __syncthreads();
@@ -245,11 +241,8 @@ __global__ void __launch_bounds__(kWolffGridTpb) ising_wolff_grid_kernel(
         if (j > i) b += si * spins[j];
       }
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      b += __shfl_down_sync(0xffffffffu, b, o);
-      u += __shfl_down_sync(0xffffffffu, u, o);
-    }
+    b = __reduce_add_sync(0xffffffffu, b);
+    u = __reduce_add_sync(0xffffffffu, u);
     if (lane == 0) {
       atomicAdd(&g->bond0, (unsigned long long)(long long)b);
       atomicAdd(&g->ups0, (unsigned long long)(long long)u);
@@ -314,8 +307,7 @@ __global__ void __launch_bounds__(kWolffGridTpb) ising_wolff_grid_kernel(
       if (k == 0) spins[site] = (int8_t)(-ref);
     }
     if (sums) {
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) cut += __shfl_down_sync(0xffffffffu, cut, o);
+      cut = __reduce_add_sync(0xffffffffu, cut);
       if (lane == 0 && cut) atomicAdd(&g->cut, (unsigned long long)(long long)cut);
     }
     if (!grid_barrier(g, nullptr, nullptr)) return;
@@ -372,11 +364,8 @@ __global__ void __launch_bounds__(1024) ising_wolff_mid_kernel(int8_t* __restric
         if (j > i) b += si * spin_of(j);
       }
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      b += __shfl_down_sync(0xffffffffu, b, o);
-      u += __shfl_down_sync(0xffffffffu, u, o);
-    }
+    b = __reduce_add_sync(0xffffffffu, b);
+    u = __reduce_add_sync(0xffffffffu, u);
     if (lane == 0) {
       s_red[0][warp] = b;
       s_red[1][warp] = u;
@@ -432,8 +421,7 @@ __global__ void __launch_bounds__(1024) ising_wolff_mid_kernel(int8_t* __restric
       if (k == 0) atomicXor(&up[site >> 5], 1u << (site & 31));
     }
     if (sums) {
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) cut += __shfl_down_sync(0xffffffffu, cut, o);
+      cut = __reduce_add_sync(0xffffffffu, cut);
       if (lane == 0 && cut) atomicAdd(&s_cut, cut);
     }
     __syncthreads();
