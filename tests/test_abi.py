@@ -45,6 +45,25 @@ def test_lattice_tables_match_oracle(V, O, cell, ext, pbc):
     assert nc == g.ncolours and np.array_equal(col, g.colour)
 
 
+@pytest.mark.parametrize("cell,nb", [("bcc", 2), ("fcc", 4)])
+def test_bcc_fcc_colour_classes_are_the_sublattices(V, O, cell, nb):
+    """The sublattice kernels take class q = basis sublattice q and class
+    entry = cell index; that is the greedy colouring's assignment (and so
+    the generic path's draws) for any extents and boundaries, including
+    extents 1 and 2 where periodic images repeat a neighbour."""
+    rng = np.random.default_rng(11)
+    shapes = [(16, 1, 1), (16, 2, 1), (2, 2, 2), (1, 3, 5)] + [tuple(int(v) for v in rng.integers(1, 7, size=3))
+                                                               for _ in range(12)]
+    for k, ext in enumerate(shapes):
+        pbc = tuple(bool((k >> a) & 1) for a in range(3))
+        lat = getattr(V.Lattice, cell)(*ext, pbc=pbc)
+        col, nc = lat.colouring()
+        assert nc == nb, (ext, pbc)
+        assert np.array_equal(col, np.arange(lat.n_sites) % nb), (ext, pbc)
+        g = O.Graph(O.lattice(cell, *ext, tuple(int(p) for p in pbc)))
+        assert np.array_equal(g.colour, col), (ext, pbc)
+
+
 def test_periodic_extent_one_is_rejected(V):
     with pytest.raises(V.VegasGpuError) as e:
         V.Lattice.sc(4, 4, 1, pbc=(True, True, True)).neighbours()
