@@ -64,6 +64,49 @@ def test_bcc_fcc_colour_classes_are_the_sublattices(V, O, cell, nb):
         assert np.array_equal(g.colour, col), (ext, pbc)
 
 
+def _half(cell, b, a):
+    """Whether basis site b sits at the half-cell position on axis a."""
+    if cell == "bcc":
+        return b == 1
+    return (b == 1 and a != 2) or (b == 2 and a != 1) or (b == 3 and a != 0)
+
+
+@pytest.mark.parametrize("cell,nb", [("bcc", 2), ("fcc", 4)])
+def test_sublattice_stencil_equals_neighbour_table(O, cell, nb):
+    """The sublattice kernels' stencil: the neighbours of basis b on basis q
+    are the cells c + sum over the axes where the two basis positions differ
+    of {0, d_b} e_a (d_b = +1 if b sits at the half position, else -1),
+    wrapped on periodic axes and dropped across open ones; as multisets it
+    equals the oracle's neighbour table."""
+    rng = np.random.default_rng(5)
+    for k in range(10):
+        ext = tuple(int(v) for v in rng.integers(1, 6, size=3))
+        pbc = tuple((k >> a) & 1 for a in range(3))
+        g = O.Graph(O.lattice(cell, *ext, pbc))
+        table = g.nbr.reshape(g.n, g.zmax)
+        nx, ny, nz = ext
+        for i in range(g.n):
+            b, c = i % nb, i // nb
+            x, y, z = c % nx, (c // nx) % ny, c // (nx * ny)
+            got = []
+            for q in range(nb):
+                if q == b:
+                    continue
+                axes = [a for a in range(3) if _half(cell, q, a) != _half(cell, b, a)]
+                for m in range(1 << len(axes)):
+                    pos, ok = [x, y, z], True
+                    for t, a in enumerate(axes):
+                        if (m >> t) & 1:
+                            pos[a] += 1 if _half(cell, b, a) else -1
+                            if not 0 <= pos[a] < ext[a]:
+                                ok = ok and bool(pbc[a])
+                                pos[a] %= ext[a]
+                    if ok:
+                        got.append(((pos[2] * ny + pos[1]) * nx + pos[0]) * nb + q)
+            want = [int(j) for j in table[i] if j >= 0]
+            assert sorted(got) == sorted(want), (ext, pbc, i)
+
+
 def test_periodic_extent_one_is_rejected(V):
     with pytest.raises(V.VegasGpuError) as e:
         V.Lattice.sc(4, 4, 1, pbc=(True, True, True)).neighbours()
