@@ -174,7 +174,16 @@ def hamiltonian(*terms) -> _abi.HamiltonianDesc:
 
 # ------------------------------------------------------------------ engine
 class Engine:
-    """A device-resident lattice state driven by the GPU Metropolis integrator."""
+    """A device-resident lattice state driven by the GPU Metropolis integrator.
+
+    `path` picks the kernel family (PATH_AUTO chooses): PATH_STRUCTURED runs
+    implicit neighbour stencils -- sc checkerboard classes, and one array per
+    basis sublattice for bcc / fcc (Ising when x is a multiple of 16,
+    Heisenberg always); PATH_GENERIC runs neighbour tables on any lattice and
+    is the one per-bond exchange constants need; PATH_RESIDENT keeps a small
+    sc Ising lattice in one block's shared memory.  All paths draw the same
+    random numbers for the same site, sweep and seed.
+    """
 
     def __init__(self, lattice: Lattice, ham: _abi.HamiltonianDesc, spin: int = SPIN_ISING, seed: int = 0,
                  proposal: Optional[int] = None, path: int = PATH_AUTO, precision: int = FP32, replica: int = 0,
