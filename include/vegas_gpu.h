@@ -404,16 +404,24 @@ int vg_hbatch_time_passes(vg_hbatch* batch, uint32_t n_sweeps, double* ms_per_sw
  * loops where an allocation could synchronise the device.  The caller owns
  * every buffer: class0 / class1 are the two checkerboard classes on the
  * device (uint8 0 = Down / 1 = Up, sites with (x+y+z)&1 == c, row-major
- * [z][y][x/2]) and sums_out (may be NULL) receives n_sweeps vg_sums rows
- * (field along +z).  zeeman is the per-site Zeeman coefficient (sign * |B| *
- * orientation).  Work is enqueued on cuda_stream (NULL = default stream);
- * results are valid once that stream has been synchronised.  Draws and
- * results equal vg_sweeps on a context with the same seed and replica at
- * sweep index sweep0.  The per-block partial sums live in a 2 MiB array
- * inside the library (at most 2048 thread blocks per colour pass; larger
- * launches are rejected with VG_ERR_UNSUPPORTED); every call shares it, so
- * calls that overlap on the GPU race.  The first call on a device looks up
- * the array's address: make it before any stream capture. */
+ * [z][y][x/2]) and sums_out (may be NULL) receives n_sweeps vg_sums rows.
+ * zeeman is the per-site Zeeman coefficient (sign * |B| * orientation, the
+ * field's z orientation folded in), so the rows cannot know the orientation:
+ * their zeeman member is the sum of s.z (mz), which a context reports for a
+ * field along +z; for a field along -z the context's zeeman member is -mz,
+ * and callers forming energies multiply by the orientation themselves.  Work
+ * is enqueued on cuda_stream (NULL = default stream); results are valid once
+ * that stream has been synchronised.  Draws, spins and every other member of
+ * the rows equal vg_sweeps on a context with the same seed and replica at
+ * sweep index sweep0 (sweep0 + n_sweeps <= 2^32).  The per-block partial
+ * sums live in a 2 MiB array inside the library (at most 2048 thread blocks
+ * per colour pass; larger launches are rejected with VG_ERR_UNSUPPORTED);
+ * every call shares it, so calls that overlap on the GPU race.  The first
+ * call on a device looks up the array's address and keeps it for the rest of
+ * the process: make it before any stream capture.  A device reset
+ * (cudaDeviceReset, or the primary context being destroyed) moves the array
+ * and the library cannot look it up again, so a process that resets a device
+ * must not call this entry point on it afterwards. */
 int vg_ising_sc_sweeps_noalloc(const vg_lattice_desc* lattice, double exchange, double zeeman, double temperature,
                                uint64_t seed, uint32_t replica, uint64_t sweep0, uint64_t n_sweeps,
                                uint8_t* class0, uint8_t* class1, double* sums_out, void* cuda_stream);

@@ -71,10 +71,13 @@ def test_fp64_batch_matches_oracle(V, O, cell, ext, pbc):
                 np.abs(s0[r] - g.heis_init(rep.seed, rep.replica).reshape(-1, 3)).max() < 1e-12
             want_s, want = _oracle_run(O, olat, rep, s0[r].reshape(-1), fields, relax, measure, zsign, axis, baxis)
             got_s = hb.get_replica(r)
+            # FP64 against FP64: a decision can differ only where u equals
+            # exp(-dE/T) to rounding (about 1e-16 per attempt), so every spin
+            # must agree and the per-point sums are always compared
             same = np.all(np.abs(got_s - want_s.reshape(-1, 3)) < SPIN_TOL, axis=1)
-            assert same.mean() > 0.999, f"replica {r}: {same.mean():.4f} of spins agree"
-            if same.all():
-                np.testing.assert_allclose(sums[:, r, :], want, rtol=REL_FP64, atol=1e-8)
+            assert same.all(), f"replica {r}: {int((~same).sum())} of {same.size} spins differ"
+            np.testing.assert_allclose(sums[:, r, :], want, rtol=REL_FP64, atol=1e-8,
+                                       err_msg=f"per-point sums of replica {r}")
 
 
 def test_init_random_matches_single_lattice_contexts(V):

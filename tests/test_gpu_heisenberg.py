@@ -144,7 +144,7 @@ def test_norms_do_not_drift(V):
 
 
 def test_reference_known_answers_on_gpu(V):
-    """The reference's energy unit tests (src/energy.rs:530-605) through the GPU totals."""
+    """The reference's energy unit tests (src/energy.rs:300-375) through the GPU totals."""
     import json
     import os
 

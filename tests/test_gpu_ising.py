@@ -178,6 +178,33 @@ def test_resume_from_sweep_index(V):
         assert np.array_equal(a.get_state(), b.get_state())
 
 
+def test_sweep_index_stays_32_bit(V, O):
+    """The sweep index is the 32-bit Philox counter word: the last index a run
+    may use is 2^32 - 1 and runs that would pass it are refused (the state
+    and the index stay as they were)."""
+    H = V.hamiltonian(V.Exchange(1.0))
+    with _engine(V, "sc", (32, 8, 8), (1, 1, 1), H, 8) as eng:
+        eng.init_random()
+        eng.set_thermostat(4.5)
+        with pytest.raises(V.VegasGpuError) as e:
+            eng.sweep_index = 1 << 32
+        assert e.value.status == 1
+        last = (1 << 32) - 2
+        eng.sweep_index = last
+        s0 = eng.get_state()
+        with pytest.raises(V.VegasGpuError) as e:
+            eng.sweeps(3)
+        assert e.value.status == 1 and "2^32" in str(e.value)
+        assert eng.sweep_index == last and np.array_equal(eng.get_state(), s0)
+        eng.sweeps(2, measure=False)  # sweeps 2^32 - 2 and 2^32 - 1
+        g = O.Graph(O.lattice("sc", 32, 8, 8))
+        ref, _ = g.ising_sweeps(s0, 1.0, 0.0, 4.5, 8, last, 2)
+        assert np.array_equal(eng.get_state(), ref)
+        assert eng.sweep_index == 1 << 32
+        with pytest.raises(V.VegasGpuError):
+            eng.sweeps(1)
+
+
 def test_set_get_roundtrip_and_observables(V, O):
     lat = ("sc", (32, 6, 4), (1, 1, 1))
     rng = np.random.default_rng(1)

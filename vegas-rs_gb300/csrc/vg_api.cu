@@ -96,6 +96,13 @@ int cuda_fail(vg_ctx* c, cudaError_t e, const char* what) {
   return fail(c, code, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+// Sweeps [c->sweep, c->sweep + n) must have 32-bit indices.
+int check_sweeps(vg_ctx* c, uint64_t n) {
+  if (sweep_range_ok(c->sweep, n)) return VG_OK;
+  return fail(c, VG_ERR_INVALID_ARG, "sweep index " + std::to_string(c->sweep) + " + " + std::to_string(n) +
+                                         " sweeps passes 2^32 (the 32-bit sweep word of the Philox counter)");
+}
+
 #define VG_CUDA(c, expr)                                    \
   do {                                                      \
     cudaError_t _e = (expr);                                \
@@ -467,54 +474,11 @@ double zeeman_coef(const vg_ctx* c) {
 
 // Ising thresholds: accept iff U < thr (see vg_ising.cu)
 IsingTable ising_table(const vg_ctx* c) {
-  IsingTable t;
-  std::memset(&t, 0, sizeof(t));
   const double J = c->ham.has_exchange ? c->ham.exchange : 0.0;
   const double o = c->bhat[2] >= 0.0 ? 1.0 : -1.0;  // Field<IsingSpin> orientation Up / Down
-  const double hz = zeeman_coef(c) * o;
-  const double T = clamp_temperature(c->T);
-  const int z = c->z, W = 2 * z + 1;
-  for (int s01 = 0; s01 < 2; ++s01)
-    for (int ns = -z; ns <= z; ++ns) {
-      const double s = s01 ? 1.0 : -1.0;
-      const double e_old = -J * s * (double)ns + hz * s;
-      const double e_new = -J * (-s) * (double)ns + hz * (-s);
-      const double de = e_new - e_old;
-      unsigned long long thr;
-      if (de <= 0.0) {
-        thr = 1ull << 32;
-      } else {
-        const double x = std::ceil(std::exp(-de / T) * 4294967296.0);
-        thr = x >= 4294967296.0 ? (1ull << 32) : x <= 0.0 ? 0ull : (unsigned long long)x;
-      }
-      t.thr[s01 * W + ns + z] = thr;
-    }
-  // byte tables for lattices whose sites all have the same neighbour count
-  t.zeff = -1;
-  if (sc_layout(c)) {
-    const int ext[3] = {c->lat.nx, c->lat.ny, c->lat.nz};
-    const int per[3] = {c->lat.pbc_x, c->lat.pbc_y, c->lat.pbc_z};
-    int zeff = 0;
-    bool uniform = true;
-    for (int a = 0; a < 3; ++a) {
-      if (per[a]) zeff += 2;
-      else if (ext[a] > 1) uniform = false;
-    }
-    if (uniform) {
-      t.zeff = zeff;
-      uint8_t top[2][8] = {};
-      for (int s01 = 0; s01 < 2; ++s01)
-        for (int nu = 0; nu <= zeff; ++nu) {
-          const unsigned long long thr = t.thr[s01 * W + 2 * nu - zeff + z];
-          top[s01][nu] = thr >= (1ull << 32) ? 0xFF : (uint8_t)(thr >> 24);
-        }
-      for (int s01 = 0; s01 < 2; ++s01)
-        for (int h = 0; h < 2; ++h)
-          t.top[s01][h] = (uint32_t)top[s01][4 * h] | ((uint32_t)top[s01][4 * h + 1] << 8) |
-                          ((uint32_t)top[s01][4 * h + 2] << 16) | ((uint32_t)top[s01][4 * h + 3] << 24);
-    }
-  }
-  return t;
+  const int ext[3] = {c->lat.nx, c->lat.ny, c->lat.nz};
+  const int per[3] = {c->lat.pbc_x, c->lat.pbc_y, c->lat.pbc_z};
+  return make_ising_table(J, zeeman_coef(c) * o, clamp_temperature(c->T), c->z, sc_layout(c), ext, per);
 }
 
 template <typename R>
@@ -692,6 +656,7 @@ int launch_reduce(vg_ctx* c, int sweeps, double* out) {
 // Enqueue n sweeps; with measure, per-sweep raw sums land in d_sums[0..n).
 int enqueue(vg_ctx* c, uint64_t n, bool measure) {
   int rc;
+  if ((rc = check_sweeps(c, n))) return rc;
   if (c->path == VG_PATH_RESIDENT) {  // all n sweeps in one launch
     if (measure && (rc = ensure_sums(c, (size_t)std::max<uint64_t>(n, 1)))) return rc;
     const IsingScArgs a = ising_sc_args(c);
@@ -1312,6 +1277,8 @@ int vg_set_thermostat(vg_ctx* c, double T, const double b[3], double mag) {
 
 int vg_set_sweep_index(vg_ctx* c, uint64_t s) {
   if (!c) return VG_ERR_INVALID_ARG;
+  if (s >= kSweepLimit)
+    return fail(c, VG_ERR_INVALID_ARG, "sweep index " + std::to_string(s) + " does not fit the 32-bit sweep word");
   c->sweep = s;
   return VG_OK;
 }
@@ -1373,6 +1340,7 @@ int vg_time_passes(vg_ctx* c, uint64_t n, int32_t measure, double* pass_ms, doub
   if (!c || n == 0) return VG_ERR_INVALID_ARG;
   VG_CUDA(c, cudaSetDevice(c->device));
   int rc;
+  if ((rc = check_sweeps(c, n))) return rc;
   if (measure) {
     if ((rc = ensure_sums(c, (size_t)n))) return rc;
     if ((rc = ensure_part(c, rows_per_sweep(c) * kChunk))) return rc;
@@ -1491,6 +1459,7 @@ int vg_wolff_steps(vg_ctx* c, uint64_t n, int32_t measure, double* E, double* M)
   if (c->bonds) return fail(c, VG_ERR_UNSUPPORTED, "Wolff steps use the uniform exchange constant");
   VG_CUDA(c, cudaSetDevice(c->device));
   int rc;
+  if ((rc = check_sweeps(c, n))) return rc;
   if ((rc = ensure_natural_nbr(c))) return rc;
   const bool mid = c->n > kWolffMaxSites && c->n <= kWolffMidSites;
   const bool grid = c->n > kWolffMidSites;

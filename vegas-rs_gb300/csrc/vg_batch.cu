@@ -868,6 +868,8 @@ int vg_batch_init_random(vg_batch* b) {
 
 int vg_batch_run_async(vg_batch* b, uint64_t rounds) {
   if (!b) return VG_ERR_INVALID_ARG;
+  if (rounds > kSweepLimit || !sweep_range_ok(b->sweep, rounds * (uint64_t)b->every))
+    return bfail(b, VG_ERR_INVALID_ARG, "the run passes sweep index 2^32 (the 32-bit sweep word of the Philox counter)");
   VG_BCUDA(b, cudaSetDevice(b->device));
   int rc = ensure_ring(b, std::max<uint64_t>(rounds, 1));
   if (rc) return rc;

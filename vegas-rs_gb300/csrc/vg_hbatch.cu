@@ -782,6 +782,8 @@ int vg_hbatch_run_async(vg_hbatch* b, const double* fields, int32_t n_points, ui
   if (relax + measure == 0 || relax + measure < relax) return hfail(b, VG_ERR_INVALID_ARG, "a field point needs sweeps");
   for (int i = 0; i < n_points; ++i)
     if (!std::isfinite(fields[i])) return hfail(b, VG_ERR_INVALID_ARG, "field values must be finite");
+  if (!sweep_range_ok(b->sweep, (uint64_t)n_points * ((uint64_t)relax + measure)))
+    return hfail(b, VG_ERR_INVALID_ARG, "the run passes sweep index 2^32 (the 32-bit sweep word of the Philox counter)");
   VG_HCUDA(b, cudaSetDevice(b->device));
   int rc;
   // Buffers baked into the captured graph: growing one drops the graph.
@@ -868,6 +870,8 @@ int vg_hbatch_point_sums(vg_hbatch* b, double* out, int64_t cap) {
 
 int vg_hbatch_time_passes(vg_hbatch* b, uint32_t n, double* ms) {
   if (!b || !ms || n == 0) return VG_ERR_INVALID_ARG;
+  if (!sweep_range_ok(b->sweep, n))
+    return hfail(b, VG_ERR_INVALID_ARG, "the run passes sweep index 2^32 (the 32-bit sweep word of the Philox counter)");
   VG_HCUDA(b, cudaSetDevice(b->device));
   const HbField zero{0.0, 0.f, 0.f};
   const HbDev d0{(uint32_t)b->sweep, 0};

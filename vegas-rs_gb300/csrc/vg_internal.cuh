@@ -5,6 +5,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cmath>
+#include <cstring>
+
 #include <utility>
 
 #include "vegas_gpu.h"
@@ -43,6 +46,12 @@ constexpr int kMaxZ = 12;          // fcc coordination
 constexpr int kMaxColours = 16;
 constexpr int kIsingGroup = 16;    // class entries sharing one Philox block
 constexpr int kNumSums = 8;        // members of vg_sums
+// The sweep index is Philox counter word 1 (32 bits): a run may use sweep
+// indices up to 2^32 - 1, and entry points refuse runs that would go past.
+constexpr unsigned long long kSweepLimit = 1ull << 32;
+inline bool sweep_range_ok(unsigned long long first, unsigned long long n) {
+  return first < kSweepLimit && n <= kSweepLimit - first;
+}
 
 // Draw-stream tags (bits 24..31 of Philox counter word 2).
 enum : uint32_t {
@@ -131,6 +140,57 @@ struct IsingTable {
   uint32_t top[2][2];
   int zeff;
 };
+
+// The acceptance table of the reference's rule (dE < 0 accepts, otherwise
+// accept iff u < exp(-dE/T), src/integrator.rs:113-137) for the Ising site
+// energy E_i(s) = -J s nsum + hz s (src/energy.rs:147-152, :194-206) with z
+// neighbours at most, built in FP64 on the host: thr = ceil(exp(-dE/T) 2^32),
+// 2^32 where the move always accepts.  sc: the lattice uses the checkerboard
+// kernels, whose byte tables need every site to have the same number of
+// existing neighbours (each axis periodic, or open with extent 1); zeeman
+// sign, |B| and the field orientation are folded into hz by the caller.
+inline IsingTable make_ising_table(double J, double hz, double T, int z, bool sc, const int ext[3],
+                                   const int per[3]) {
+  IsingTable t;
+  std::memset(&t, 0, sizeof(t));
+  const int W = 2 * z + 1;
+  for (int s01 = 0; s01 < 2; ++s01)
+    for (int ns = -z; ns <= z; ++ns) {
+      const double s = s01 ? 1.0 : -1.0;
+      const double e_old = -J * s * (double)ns + hz * s;
+      const double e_new = -J * (-s) * (double)ns + hz * (-s);
+      const double de = e_new - e_old;
+      unsigned long long thr;
+      if (de <= 0.0) {
+        thr = 1ull << 32;
+      } else {
+        const double x = std::ceil(std::exp(-de / T) * 4294967296.0);
+        thr = x >= 4294967296.0 ? (1ull << 32) : x <= 0.0 ? 0ull : (unsigned long long)x;
+      }
+      t.thr[s01 * W + ns + z] = thr;
+    }
+  t.zeff = -1;
+  if (!sc) return t;
+  int zeff = 0;
+  bool uniform = true;
+  for (int a = 0; a < 3; ++a) {
+    if (per[a]) zeff += 2;
+    else if (ext[a] > 1) uniform = false;
+  }
+  if (!uniform) return t;
+  t.zeff = zeff;
+  uint8_t top[2][8] = {};
+  for (int s01 = 0; s01 < 2; ++s01)
+    for (int nu = 0; nu <= zeff; ++nu) {
+      const unsigned long long thr = t.thr[s01 * W + 2 * nu - zeff + z];
+      top[s01][nu] = thr >= (1ull << 32) ? 0xFF : (uint8_t)(thr >> 24);
+    }
+  for (int s01 = 0; s01 < 2; ++s01)
+    for (int h = 0; h < 2; ++h)
+      t.top[s01][h] = (uint32_t)top[s01][4 * h] | ((uint32_t)top[s01][4 * h + 1] << 8) |
+                      ((uint32_t)top[s01][4 * h + 2] << 16) | ((uint32_t)top[s01][4 * h + 3] << 24);
+  return t;
+}
 
 struct RngKey {
   uint32_t k0, k1, replica, sweep;

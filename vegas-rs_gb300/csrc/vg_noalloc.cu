@@ -13,7 +13,10 @@
 //
 // Set-up: the first call on a device looks up the array's device address
 // (cudaGetSymbolAddress) with that device current and caches it; make that
-// first call before any stream capture.  All calls share the one array and
+// first call before any stream capture.  The cached address belongs to the
+// device's primary context: after a device reset it is stale and there is no
+// way to look it up again, so the entry point must not be used on a device
+// the process has reset.  All calls share the one array and
 // each colour pass overwrites every row it later reads, so nothing has to be
 // cleared between calls -- but calls whose work overlaps on the GPU (two
 // streams, or two host threads) race on the array and must be serialised by
@@ -49,7 +52,8 @@ int fail(int code, const char* msg) {
 }
 
 // Per-sweep rows -> finished sums (bond, N, mz, N, 0, 0, mz, accepted), the
-// layout of vg_sums with the field along +z.
+// layout of vg_sums; the zeeman member is mz whatever the field's
+// orientation (the caller folded it into the coefficient).
 __global__ void noalloc_finish(const long long* __restrict__ rows, int rows_per_sweep, long long n_sites,
                                double* __restrict__ out) {
   __shared__ long long s[3][256];
@@ -84,51 +88,6 @@ __global__ void noalloc_finish(const long long* __restrict__ rows, int rows_per_
   }
 }
 
-// Acceptance table of the reference rule (accept if dE < 0, else iff
-// u < exp(-dE/T)) for E_i(s) = -J s nsum + hz s, with the byte tables used
-// when every site has the same number of neighbours.
-IsingTable build_table(const vg_lattice_desc& L, double J, double hz, double T) {
-  IsingTable t;
-  std::memset(&t, 0, sizeof(t));
-  const int z = 6, W = 2 * z + 1;
-  for (int s01 = 0; s01 < 2; ++s01)
-    for (int ns = -z; ns <= z; ++ns) {
-      const double s = s01 ? 1.0 : -1.0;
-      const double de = (-J * (-s) * (double)ns + hz * (-s)) - (-J * s * (double)ns + hz * s);
-      unsigned long long thr;
-      if (de <= 0.0) {
-        thr = 1ull << 32;
-      } else {
-        const double x = std::ceil(std::exp(-de / T) * 4294967296.0);
-        thr = x >= 4294967296.0 ? (1ull << 32) : x <= 0.0 ? 0ull : (unsigned long long)x;
-      }
-      t.thr[s01 * W + ns + z] = thr;
-    }
-  const int ext[3] = {L.nx, L.ny, L.nz};
-  const int per[3] = {L.pbc_x, L.pbc_y, L.pbc_z};
-  int zeff = 0;
-  bool uniform = true;
-  for (int a = 0; a < 3; ++a) {
-    if (per[a]) zeff += 2;
-    else if (ext[a] > 1) uniform = false;
-  }
-  t.zeff = -1;
-  if (uniform) {
-    t.zeff = zeff;
-    uint8_t top[2][8] = {};
-    for (int s01 = 0; s01 < 2; ++s01)
-      for (int nu = 0; nu <= zeff; ++nu) {
-        const unsigned long long thr = t.thr[s01 * W + 2 * nu - zeff + z];
-        top[s01][nu] = thr >= (1ull << 32) ? 0xFF : (uint8_t)(thr >> 24);
-      }
-    for (int s01 = 0; s01 < 2; ++s01)
-      for (int h = 0; h < 2; ++h)
-        t.top[s01][h] = (uint32_t)top[s01][4 * h] | ((uint32_t)top[s01][4 * h + 1] << 8) |
-                        ((uint32_t)top[s01][4 * h + 2] << 16) | ((uint32_t)top[s01][4 * h + 3] << 24);
-  }
-  return t;
-}
-
 }  // namespace
 
 extern "C" int vg_ising_sc_sweeps_noalloc(const vg_lattice_desc* L, double exchange, double zeeman,
@@ -143,6 +102,8 @@ extern "C" int vg_ising_sc_sweeps_noalloc(const vg_lattice_desc* L, double excha
   if ((double)L->nx * L->ny * L->nz > 2147483647.0) return fail(VG_ERR_UNSUPPORTED, "lattice has more than 2^31-1 sites");
   if (std::isnan(temperature) || !std::isfinite(exchange) || !std::isfinite(zeeman))
     return fail(VG_ERR_INVALID_ARG, "temperature, exchange and field must be numbers");
+  if (!sweep_range_ok(sweep0, n_sweeps))
+    return fail(VG_ERR_INVALID_ARG, "sweep0 + n_sweeps passes 2^32 (the 32-bit sweep word of the Philox counter)");
   const double eps = 2.220446049250313e-16;
   const double T = temperature < eps ? eps : temperature;
 
@@ -184,7 +145,9 @@ extern "C" int vg_ising_sc_sweeps_noalloc(const vg_lattice_desc* L, double excha
     return fail(VG_ERR_UNSUPPORTED, "no-alloc sweeps: the launch needs more partial-sum rows than the 2 MiB "
                                     "scratch array holds (at most 2048 thread blocks per colour pass)");
 
-  const IsingTable tab = build_table(*L, exchange, zeeman, T);
+  const int ext[3] = {L->nx, L->ny, L->nz};
+  const int per[3] = {L->pbc_x, L->pbc_y, L->pbc_z};
+  const IsingTable tab = make_ising_table(exchange, zeeman, T, 6, true, ext, per);
   cudaStream_t s = (cudaStream_t)cuda_stream;
   const long long n_sites = (long long)L->nx * L->ny * L->nz;
   for (uint64_t t0 = 0; t0 < n_sweeps; t0 += kNoAllocChunk) {
