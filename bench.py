@@ -175,17 +175,24 @@ def run_reference(args, rank):
     H = O.Hamiltonian(has_exchange=1, J=1.0, compound=0)
     lat = O.lattice("sc", L, L, L)
     # each step is one measured reference sweep of a 256^3 lattice on every
-    # host core (about five seconds); the warm-up sweeps run untimed first
+    # host core (about five seconds) at the temperature the GPU arm's step of
+    # the same index runs: the CoolDown(5.5, 3.5, 0.1) ladder, one
+    # temperature per step, the chains carrying their state along it; the
+    # warm-up sweeps run untimed first
     steps = max(1, args.steps)
     warm = max(0, args.warmup)
-    flips, dt = O.ref_parallel(lat, 0, H, 4.5, steps, threads, seed=SEED, measure=True, warmup=warm)
+    temps = ladder()
+    sched = [temps[(warm + k) % len(temps)] for k in range(steps)]
+    flips, dt = O.ref_parallel_ladder(lat, 0, H, sched, 1, threads, seed=SEED, measure=True, warmup=warm)
     v = flips / (dt * 1e9)
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "flips/ns", "n_gpus": args.gpus,
         "steps": steps, "warmup": warm, "ms_per_step": dt * 1e3 / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "ising-sc-256^3-pbc-J1-h0 (reference random-site Metropolis, CLI measurement)",
-                   "lattice": [L, L, L], "threads": threads},
+                   "lattice": [L, L, L], "threads": threads,
+                   "temperatures": "CoolDown(5.5, 3.5, 0.1) ladder, one per step (the GPU arm's steps)",
+                   "step_temperatures": sched},
         "cpu_baseline": {"value": v, "unit": "flips/ns", "cores": threads, "kind": "port",
                          "sample": f"{steps} measured sweeps per core, one 256^3 lattice per core"},
         "e2e": {"value": v, "unit": "flips/ns", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},

@@ -121,6 +121,10 @@ def lib():
         L.vo_ref_parallel.argtypes = [P(Lattice), C.c_int32, C.c_int32, P(Hamiltonian), C.c_double, C.c_double,
                                       C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, P(C.c_double)]
         L.vo_ref_parallel.restype = C.c_int64
+        L.vo_ref_parallel_ladder.argtypes = [P(Lattice), C.c_int32, C.c_int32, P(Hamiltonian), P(C.c_double),
+                                             C.c_int32, C.c_double, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                             C.c_uint64, P(C.c_double)]
+        L.vo_ref_parallel_ladder.restype = C.c_int64
         L.vo_cooldown_temperatures.argtypes = [C.c_double, C.c_double, C.c_double, P(C.c_double), C.c_int32]
         L.vo_cooldown_temperatures.restype = C.c_int32
         L.vo_hysteresis_fields.argtypes = [C.c_double, C.c_double, P(C.c_double), C.c_int32]
@@ -381,4 +385,17 @@ def ref_parallel(lat: Lattice, kind, H: Hamiltonian, T, nsweeps, nthreads, seed=
     sec = C.c_double()
     flips = int(lib().vo_ref_parallel(C.byref(lat), kind, proposal, C.byref(H), T, bmag, warmup, nsweeps,
                                       int(measure), nthreads, seed, C.byref(sec)))
+    return flips, sec.value
+
+
+def ref_parallel_ladder(lat: Lattice, kind, H: Hamiltonian, temps, sweeps_per_temp, nthreads, seed=1,
+                        proposal=PROPOSE_FLIP, measure=True, bmag=0.0, warmup=0):
+    """Independent reference chains, one per thread, each walking `temps`
+    (`warmup` untimed sweeps at temps[0], then `sweeps_per_temp` timed sweeps
+    per temperature, state carried over); returns (flips, seconds)."""
+    t = np.ascontiguousarray(temps, dtype=np.float64)
+    sec = C.c_double()
+    flips = int(lib().vo_ref_parallel_ladder(C.byref(lat), kind, proposal, C.byref(H), _p(t, C.c_double), t.size,
+                                             bmag, warmup, sweeps_per_temp, int(measure), nthreads, seed,
+                                             C.byref(sec)))
     return flips, sec.value

@@ -12,6 +12,7 @@
 
 #include <math.h>
 #include <pthread.h>
+#include <unistd.h>
 #include <stdlib.h>
 #include <string.h>
 #include <time.h>
@@ -794,7 +795,9 @@ typedef struct {
   const vo_lattice* lat;
   int32_t kind, proposal, nsweeps, measure, nwarm;
   const vo_hamiltonian* H;
-  double T, bmag;
+  const double* temps; /* nsweeps measured sweeps at each of ntemps temperatures */
+  int32_t ntemps;
+  double bmag;
   uint64_t seed;
   int64_t flips;
   pthread_barrier_t* start;
@@ -826,18 +829,19 @@ static void* par_worker(void* arg) {
   }
   double* obs = (double*)malloc(sizeof(double) * 2 * (size_t)(J->nsweeps > 0 ? J->nsweeps : 1));
   double b[3] = {0, 0, 1};
-  if (J->nwarm > 0) { /* untimed warm-up sweeps */
+  if (J->nwarm > 0) { /* untimed warm-up sweeps at the first temperature */
     double* wo = (double*)malloc(sizeof(double) * 2 * (size_t)J->nwarm);
-    vo_ref_sweeps(n, z, nbr, J->kind, J->proposal, si, sf, J->H, J->T, b, J->bmag, &rng, J->nwarm, J->measure, 1,
-                  wo);
+    vo_ref_sweeps(n, z, nbr, J->kind, J->proposal, si, sf, J->H, J->temps[0], b, J->bmag, &rng, J->nwarm,
+                  J->measure, 1, wo);
     free(wo);
   }
   pthread_barrier_wait(J->start); /* all chains set up: time the sweeps only */
   double t0 = now_s();
-  vo_ref_sweeps(n, z, nbr, J->kind, J->proposal, si, sf, J->H, J->T, b, J->bmag, &rng, J->nsweeps, J->measure, 1,
-                obs);
+  for (int32_t k = 0; k < J->ntemps; ++k) /* the chain carries its state from temperature to temperature */
+    vo_ref_sweeps(n, z, nbr, J->kind, J->proposal, si, sf, J->H, J->temps[k], b, J->bmag, &rng, J->nsweeps,
+                  J->measure, 1, obs);
   J->seconds = now_s() - t0;
-  J->flips = n * (int64_t)J->nsweeps;
+  J->flips = n * (int64_t)J->nsweeps * J->ntemps;
   free(obs);
   free(si);
   free(sf);
@@ -848,13 +852,24 @@ static void* par_worker(void* arg) {
 int64_t vo_ref_parallel(const vo_lattice* lat, int32_t kind, int32_t proposal, const vo_hamiltonian* H,
                         double T, double bmag, int32_t nwarm, int32_t nsweeps, int32_t measure, int32_t nthreads,
                         uint64_t seed, double* seconds) {
+  return vo_ref_parallel_ladder(lat, kind, proposal, H, &T, 1, bmag, nwarm, nsweeps, measure, nthreads, seed,
+                                seconds);
+}
+
+int64_t vo_ref_parallel_ladder(const vo_lattice* lat, int32_t kind, int32_t proposal, const vo_hamiltonian* H,
+                               const double* temps, int32_t ntemps, double bmag, int32_t nwarm,
+                               int32_t sweeps_per_temp, int32_t measure, int32_t nthreads, uint64_t seed,
+                               double* seconds) {
+  const int32_t nsweeps = sweeps_per_temp;
   if (nthreads < 1) nthreads = 1;
+  if (ntemps < 1) return 0;
   pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)nthreads);
   par_job* jobs = (par_job*)malloc(sizeof(par_job) * (size_t)nthreads);
   pthread_barrier_t start;
   pthread_barrier_init(&start, NULL, (unsigned)nthreads);
   for (int k = 0; k < nthreads; ++k) {
-    par_job j = {lat, kind, proposal, nsweeps, measure, nwarm, H, T, bmag, seed + 7919ull * (uint64_t)k, 0, &start, 0.0};
+    par_job j = {lat, kind, proposal, nsweeps, measure, nwarm, H, temps, ntemps, bmag, seed + 7919ull * (uint64_t)k,
+                 0, &start, 0.0};
     jobs[k] = j;
     pthread_create(&th[k], NULL, par_worker, &jobs[k]);
   }
@@ -895,14 +910,86 @@ void vo_msc_init(vo_msc_group* g, uint64_t seed) {
   }
 }
 
-static uint32_t msc_uniform(uint64_t seed, uint32_t word, uint32_t sweep, int colour, int64_t j, uint32_t lane) {
-  uint32_t u = 0;
+/* Decision of "U < th" for lane `lane` of the 32-replica word `word` at class
+ * entry j: U's bit 31-p is bit `lane` of plane p, plane p is word p & 3 of
+ * the Philox block p >> 2 (drawn once per word and kept in blk / have, so
+ * the 32 lanes of a word share their blocks).  Planes are compared most
+ * significant first, and only until they differ, which gives exactly
+ * U < th. */
+static int msc_accept(uint64_t seed, uint32_t word, uint32_t sweep, int colour, int64_t j, uint32_t lane,
+                      uint64_t th, uint32_t blk[8][4], int have[8]) {
   for (int p = 0; p < 32; ++p) {
-    uint32_t w[4];
-    draw(seed, (uint32_t)j, sweep, ((uint32_t)VO_TAG_MSC << 24) | ((uint32_t)colour << 8) | (uint32_t)(p >> 2), word, w);
-    u |= ((w[p & 3] >> lane) & 1u) << (31 - p);
+    const int b = p >> 2;
+    if (!have[b]) {
+      draw(seed, (uint32_t)j, sweep, ((uint32_t)VO_TAG_MSC << 24) | ((uint32_t)colour << 8) | (uint32_t)b, word,
+           blk[b]);
+      have[b] = 1;
+    }
+    const uint32_t ub = (blk[b][p & 3] >> lane) & 1u;
+    const uint32_t tb = (uint32_t)(th >> (31 - p)) & 1u;
+    if (ub != tb) return ub < tb;
   }
-  return u;
+  return 0; /* U == th */
+}
+
+/* One colour pass of one replica group over the class entries of colour c,
+ * the sites split across host threads (sites of one colour share no bond). */
+typedef struct {
+  vo_msc_group* g;
+  int64_t n, lo, hi;
+  const int32_t* nbr;
+  const int32_t* colour;
+  const int64_t* rank;
+  const uint64_t* thr;
+  int z, c;
+  uint64_t seed;
+  uint32_t sweep;
+} msc_pass_job;
+
+static void* msc_pass_worker(void* arg) {
+  const msc_pass_job* J = (const msc_pass_job*)arg;
+  vo_msc_group* g = J->g;
+  for (int64_t i = J->lo; i < J->hi; ++i) {
+    if (J->colour[i] != J->c) continue;
+    for (int32_t w0 = 0; w0 < g->n_rep; w0 += 32) {
+      uint32_t blk[8][4];
+      int have[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+      for (int32_t r = w0; r < w0 + 32; ++r) {
+        int8_t* sp = g->spins + (int64_t)r * J->n;
+        int na = 0;
+        for (int k = 0; k < 6; ++k) {
+          const int32_t q = J->nbr[i * 6 + k];
+          if (q >= 0 && sp[q] != sp[i]) ++na;
+        }
+        const uint64_t th = J->thr[(size_t)g->tau[r] * (J->z + 1) + na];
+        const int acc = th >= (1ull << 32) ? 1
+                                           : msc_accept(J->seed, g->seg_base + (uint32_t)(r / 32), J->sweep, J->c,
+                                                        J->rank[i], (uint32_t)(r % 32), th, blk, have);
+        if (acc) sp[i] = (int8_t)(-sp[i]);
+      }
+    }
+  }
+  return NULL;
+}
+
+static int host_threads(void) {
+  long k = sysconf(_SC_NPROCESSORS_ONLN);
+  return k < 1 ? 1 : k > 32 ? 32 : (int)k;
+}
+
+static void msc_pass(vo_msc_group* g, int64_t n, const int32_t* nbr, const int32_t* colour, const int64_t* rank,
+                     const uint64_t* thr, int z, int c, uint64_t seed, uint32_t sweep) {
+  int nt = host_threads();
+  if (n < 4096) nt = 1;
+  pthread_t th[32];
+  msc_pass_job jobs[32];
+  for (int k = 0; k < nt; ++k) {
+    msc_pass_job J = {g, n, n * k / nt, n * (k + 1) / nt, nbr, colour, rank, thr, z, c, seed, sweep};
+    jobs[k] = J;
+  }
+  for (int k = 1; k < nt; ++k) pthread_create(&th[k], NULL, msc_pass_worker, &jobs[k]);
+  msc_pass_worker(&jobs[0]);
+  for (int k = 1; k < nt; ++k) pthread_join(th[k], NULL);
 }
 
 int vo_msc_run(vo_msc_group* G, int32_t ng, double J, uint64_t seed, uint32_t sweep0, uint32_t round0, int32_t every,
@@ -930,24 +1017,7 @@ int vo_msc_run(vo_msc_group* G, int32_t ng, double J, uint64_t seed, uint32_t sw
     for (int32_t rd = 0; rd < rounds; ++rd) {
       for (int32_t t = 0; t < every; ++t) {
         const uint32_t sweep = sweep0 + (uint32_t)(rd * every + t);
-        for (int c = 0; c < 2; ++c)
-          for (int64_t i = 0; i < n; ++i) {
-            if (colour[i] != c) continue;
-            for (int32_t r = 0; r < g->n_rep; ++r) {
-              int8_t* sp = g->spins + (int64_t)r * n;
-              int na = 0;
-              for (int k = 0; k < 6; ++k) {
-                const int32_t q = nbr[i * 6 + k];
-                if (q >= 0 && sp[q] != sp[i]) ++na;
-              }
-              const uint64_t th = thr[(size_t)g->tau[r] * (z + 1) + na];
-              const int acc = th >= (1ull << 32)
-                                  ? 1
-                                  : msc_uniform(seed, g->seg_base + (uint32_t)(r / 32), sweep, c, rank[i],
-                                                (uint32_t)(r % 32)) < th;
-              if (acc) sp[i] = (int8_t)(-sp[i]);
-            }
-          }
+        for (int c = 0; c < 2; ++c) msc_pass(g, n, nbr, colour, rank, thr, z, c, seed, sweep);
       }
       /* measurement: anti-aligned bonds and up spins of every replica */
       for (int32_t r = 0; r < g->n_rep; ++r) {

@@ -173,6 +173,13 @@ void vo_ref_site_energies(int64_t n, int32_t zmax, const int32_t* nbr, int32_t s
 int64_t vo_ref_parallel(const vo_lattice* lat, int32_t spin_kind, int32_t proposal,
                         const vo_hamiltonian* H, double T, double bmag, int32_t nwarm, int32_t nsweeps,
                         int32_t measure, int32_t nthreads, uint64_t seed, double* seconds);
+/* The same chains walking a temperature schedule: nwarm untimed sweeps at
+ * temps[0], then sweeps_per_temp timed sweeps at each temperature in turn,
+ * the state carried over as CoolDown::run carries it (src/program.rs:182-214). */
+int64_t vo_ref_parallel_ladder(const vo_lattice* lat, int32_t spin_kind, int32_t proposal,
+                               const vo_hamiltonian* H, const double* temps, int32_t ntemps, double bmag,
+                               int32_t nwarm, int32_t sweeps_per_temp, int32_t measure, int32_t nthreads,
+                               uint64_t seed, double* seconds);
 
 /* --------------------------------- (a) colour_cpu: batched multi-spin coding */
 /* A replica group: n_rep replicas (a multiple of 32) of one sc lattice that

@@ -189,3 +189,63 @@ def test_ref_cpu_matches_colour_oracle_statistically(O):
 
     (m1, s1), (m2, s2) = binned(e_ref), binned(e_col)
     assert abs(m1 - m2) < 3 * np.hypot(s1, s2)
+
+
+def test_msc_oracle_matches_plane_by_plane_definition(O):
+    """The batched oracle draws each 32-replica word's threshold planes once
+    and compares them most significant first; a direct restatement of the
+    draw definition (replica lane l's uniform U has bit 31-p equal to bit l of
+    plane p = word p & 3 of Philox(entry, sweep, 6 << 24 | colour << 8 | p >> 2,
+    word)) gives the same spins after two sweeps."""
+    seed, J = 77, 1.0
+    lat = O.lattice("sc", 8, 6, 1, (1, 1, 0))
+    temps = np.geomspace(1.5, 3.0, 32)
+    ref = O.MscBatch([(lat, temps)])
+    ref.init(seed)
+    g = ref.groups[0]
+    spins = g["spins"].copy()
+    ref.run(J, seed, 0, 0, 2, 1, exchange=False)
+    graph = O.Graph(lat)
+    nb, col = graph.neighbours(), graph.colour
+    rank = np.zeros(graph.n, dtype=np.int64)
+    for c in range(graph.ncolours):
+        idx = np.nonzero(col == c)[0]
+        rank[idx] = np.arange(idx.size)
+    z = 4
+    for sweep in range(2):
+        for c in range(2):
+            for i in np.nonzero(col == c)[0]:
+                planes = []
+                for r in range(32):
+                    s = spins[r]
+                    na = sum(1 for q in nb[i] if q >= 0 and s[q] != s[i])
+                    th = O.ising_threshold(J, 0.0, max(temps[r], 2.220446049250313e-16), 1, z - 2 * na)
+                    if th >= 1 << 32:
+                        acc = True
+                    else:
+                        if not planes:
+                            planes = sum((O.philox([int(rank[i]), sweep, (6 << 24) | (c << 8) | b, 0], [seed, 0])
+                                          for b in range(8)), [])
+                        u = 0
+                        for p in range(32):
+                            u |= ((planes[p] >> r) & 1) << (31 - p)
+                        acc = u < th
+                    if acc:
+                        s[i] = -s[i]
+    assert np.array_equal(spins, g["spins"])
+
+
+def test_exact_finite_torus_energy_matches_enumeration():
+    """Kaufman's finite-torus partition function (used by the Onsager checks)
+    against brute-force sums over every state of small tori."""
+    import itertools
+
+    import exact_ising2d as X
+
+    for m, n in ((3, 3), (2, 4), (4, 4)):
+        for T in (1.5, 2.269, 4.0):
+            e = np.array(list(itertools.product((-1, 1), repeat=m * n)), dtype=np.int64).reshape(-1, m, n)
+            bond = (e * np.roll(e, 1, axis=1)).sum(axis=(1, 2)) + (e * np.roll(e, 1, axis=2)).sum(axis=(1, 2))
+            w = np.exp((bond - bond.max()) / T)
+            u = -(bond * w).sum() / w.sum() / (m * n)
+            assert abs(X.energy_per_spin(T, m, n) - u) < 1e-10, (m, n, T)
