@@ -62,8 +62,13 @@ enum vg_proposal { VG_PROPOSE_FLIP = 0, VG_PROPOSE_RANDOM = 1 };
  * lattice, one array (Heisenberg: three planes) per basis sublattice.  GENERIC: any lattice, and per-bond exchange constants
  * (vg_set_exchange_bonds).  RESIDENT keeps the checkerboard layout of STRUCTURED in one
  * thread block's shared memory and runs all sweeps of a call in one launch
- * (Ising, at most 65536 sites); results are identical across paths. */
-enum vg_path { VG_PATH_AUTO = 0, VG_PATH_GENERIC = 1, VG_PATH_STRUCTURED = 2, VG_PATH_RESIDENT = 3 };
+ * (Ising, at most 65536 sites).  TILED (Ising sc, periodic on every axis,
+ * x a multiple of 32, even y and z >= 4) runs each sweep as one launch:
+ * both colour passes on shared-memory tiles with halos, reading the class
+ * arrays and writing a second pair, so the context holds twice the spins;
+ * AUTO takes it for lattices of at least 64 x-rows (y x z) per SM.  Results
+ * are identical across paths. */
+enum vg_path { VG_PATH_AUTO = 0, VG_PATH_GENERIC = 1, VG_PATH_STRUCTURED = 2, VG_PATH_RESIDENT = 3, VG_PATH_TILED = 4 };
 enum vg_precision { VG_FP32 = 0, VG_FP64 = 1 };
 
 /* Lattice::sc/bcc/fcc(1.0).expand(nx, ny, nz) with drop_x/y/z on the open

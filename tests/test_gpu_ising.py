@@ -295,3 +295,54 @@ def test_one_call_equals_single_sweep_calls(V, ext, pbc, proposal):
             out.append((eng.get_state(), sums))
     assert np.array_equal(out[0][0], out[1][0])
     np.testing.assert_array_equal(out[0][1], out[1][1])
+
+
+TILED = [  # extents (all periodic), proposal, sweeps (odd counts end with one two-pass sweep)
+    ((32, 4, 4), 0, 6),
+    ((64, 8, 6), 1, 5),
+    ((96, 18, 6), 0, 7),      # 3 groups per row
+    ((128, 10, 12), 1, 4),
+    ((1024, 40, 36), 0, 3),   # 512-byte rows: several tiles per SM (more than one wave)
+]
+
+
+@pytest.mark.parametrize("ext,proposal,n", TILED)
+def test_tiled_sweeps_bit_exact(V, O, ext, proposal, n):
+    """One launch per sweep over shared-memory tiles with halos: the same
+    spins and per-sweep sums as the colour-order oracle and as the two-pass
+    checkerboard kernels, with a field Down and both proposals."""
+    seed, J, T, mag = 4321, 1.0, 3.7, 0.3
+    H = V.hamiltonian(V.Exchange(J), V.Zeeman())
+    out = {}
+    for path in (V.PATH_TILED, V.PATH_STRUCTURED):
+        with _engine(V, "sc", ext, (1, 1, 1), H, seed, path=path, proposal=proposal) as eng:
+            assert eng.info().path == path
+            eng.init_random()
+            s0 = eng.get_state()
+            eng.set_thermostat(T, (0.0, 0.0, -1.0), mag)
+            sums = eng.sweeps_sums(n)
+            E, M = eng.sweeps(2)
+            out[path] = (eng.get_state(), sums, E, M, eng.sweep_index)
+    a, b = out[V.PATH_TILED], out[V.PATH_STRUCTURED]
+    assert np.array_equal(a[0], b[0])
+    np.testing.assert_array_equal(a[1], b[1])
+    np.testing.assert_array_equal(a[2], b[2])
+    np.testing.assert_array_equal(a[3], b[3])
+    assert a[4] == b[4] == n + 2
+    g = O.Graph(O.lattice("sc", *ext))
+    ref, obs = g.ising_sweeps(s0, J, -mag, T, seed, 0, n + 2, proposal=proposal)
+    assert np.array_equal(a[0], ref)
+    np.testing.assert_array_equal(a[1][:, 0], obs[:n, 0].astype(float))
+    np.testing.assert_array_equal(a[1][:, 6], obs[:n, 1].astype(float))
+
+
+def test_tiled_path_selection(V):
+    H = V.hamiltonian(V.Exchange(1.0))
+    with _engine(V, "sc", (256, 128, 128), (1, 1, 1), H, 1) as eng:
+        assert eng.info().path == V.PATH_TILED  # AUTO: at least 64 rows per SM
+    with _engine(V, "sc", (64, 16, 16), (1, 1, 1), H, 1) as eng:
+        assert eng.info().path != V.PATH_TILED
+    for ext, pbc in (((64, 8, 6), (1, 1, 0)), ((16, 8, 8), (1, 1, 1)), ((64, 2, 8), (1, 1, 1))):
+        with pytest.raises(V.VegasGpuError) as e:
+            _engine(V, "sc", ext, pbc, H, 1, path=V.PATH_TILED)
+        assert e.value.status == 5

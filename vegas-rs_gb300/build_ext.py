@@ -22,7 +22,7 @@ INCLUDE = os.path.join(REPO, "include")
 LIB = os.path.join(PKG, "libvegas_gpu.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["vg_api.cu", "vg_ising.cu", "vg_heis.cu", "vg_noalloc.cu", "vg_batch.cu", "vg_resident.cu", "vg_hbatch.cu", "vg_wolff.cu", "vg_energy.cu"]
+CUDA_SOURCES = ["vg_api.cu", "vg_ising.cu", "vg_heis.cu", "vg_noalloc.cu", "vg_batch.cu", "vg_resident.cu", "vg_hbatch.cu", "vg_wolff.cu", "vg_energy.cu", "vg_tiled.cu"]
 HOST_PROGRAMS = {  # binary name -> source under host/
     "vegas_gpu_cli": "vegas_gpu_cli.cpp",
     "host_selftest": "host_selftest.cpp",

@@ -49,6 +49,10 @@ struct vg_ctx {
   double bmag = 0.0;
   // spins
   void* spin[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
+  // tiled path: the second buffer of the class-array pair a sweep writes
+  // into, and the tiling of the y-z plane of rows
+  uint8_t* tile_buf[2] = {nullptr, nullptr};
+  IsingTileArgs tile{};
   // generic path tables
   std::vector<int64_t> class_size;
   int32_t* d_sites[kMaxColours] = {};
@@ -387,11 +391,14 @@ __global__ void reduce_rows<long long>(const long long* __restrict__ part, long 
 
 // ------------------------------------------------------------ host helpers
 constexpr int kChunk = 64;  // sweeps per reduction launch
+// PATH_AUTO takes the tiled sweep kernel from this many rows (y x z) per SM
+constexpr long long kTileAutoRowsPerSm = 64;
 
 bool is_ising(const vg_ctx* c) { return c->opt.spin_kind == VG_SPIN_ISING; }
 // the checkerboard class layout (structured grid kernels or the resident kernel)
 bool sc_layout(const vg_ctx* c) {
-  return (c->path == VG_PATH_STRUCTURED || c->path == VG_PATH_RESIDENT) && c->lat.cell == VG_CELL_SC;
+  return (c->path == VG_PATH_STRUCTURED || c->path == VG_PATH_RESIDENT || c->path == VG_PATH_TILED) &&
+         c->lat.cell == VG_CELL_SC;
 }
 // bcc / fcc Ising with one array per sublattice (the structured path of those cells)
 bool sub_layout(const vg_ctx* c) { return c->path == VG_PATH_STRUCTURED && c->lat.cell != VG_CELL_SC; }
@@ -641,9 +648,10 @@ int launch_pass(vg_ctx* c, int colour, bool update, uint64_t sweep, void* part_r
 }
 
 size_t rows_per_sweep(const vg_ctx* c) { return (size_t)c->ncol * (size_t)c->grid; }
+// blocks (one partial row each) of a tiled sweep; 0 off the tiled path
+int tile_count(const vg_ctx* c) { return c->path == VG_PATH_TILED ? c->tile.nyt * c->tile.nzt : 0; }
 
-int launch_reduce(vg_ctx* c, int sweeps, double* out) {
-  const long long rows = (long long)rows_per_sweep(c);
+int launch_reduce(vg_ctx* c, int sweeps, double* out, long long rows) {
   if (is_ising(c) && !c->bonds)
     reduce_rows<long long><<<sweeps, 256, 0, c->stream>>>((const long long*)c->d_part, rows, out);
   else
@@ -673,10 +681,37 @@ int enqueue(vg_ctx* c, uint64_t n, bool measure) {
   }
   if (measure) {
     if ((rc = ensure_sums(c, (size_t)std::max<uint64_t>(n, 1)))) return rc;
-    if ((rc = ensure_part(c, rows_per_sweep(c) * kChunk))) return rc;
+    if ((rc = ensure_part(c, std::max<size_t>(rows_per_sweep(c), (size_t)tile_count(c)) * kChunk))) return rc;
+  }
+  uint64_t done = 0;
+  if (c->path == VG_PATH_TILED) {
+    // whole sweeps, one launch each, alternating between the class arrays
+    // and the second buffer: an even count ends in the class arrays; an odd
+    // last sweep runs as two colour passes in place (identical draws)
+    const uint64_t even = n & ~1ull;
+    const IsingTable tab = ising_table(c);
+    const size_t rows = (size_t)tile_count(c);
+    for (uint64_t t0 = 0; t0 < even; t0 += kChunk) {
+      const int m = (int)std::min<uint64_t>(kChunk, even - t0);
+      for (int t = 0; t < m; ++t) {
+        IsingTileArgs a = c->tile;
+        uint8_t* base[2] = {(uint8_t*)c->spin[0][0], (uint8_t*)c->spin[1][0]};
+        const bool odd = ((t0 + (uint64_t)t) & 1ull) != 0;
+        for (int k = 0; k < 2; ++k) {
+          a.in[k] = odd ? c->tile_buf[k] : base[k];
+          a.out[k] = odd ? base[k] : c->tile_buf[k];
+        }
+        long long* part = measure ? (long long*)c->d_part + (size_t)t * rows * kNumSums : nullptr;
+        const cudaError_t e = launch_ising_tile_sweep(a, tab, rng_key(c, c->sweep + t0 + t), c->opt.proposal, part,
+                                                      c->stream);
+        if (e != cudaSuccess) return cuda_fail(c, e, "tiled sweep launch");
+      }
+      if (measure && (rc = launch_reduce(c, m, c->d_sums + t0 * kNumSums, (long long)rows))) return rc;
+    }
+    done = even;
   }
   const size_t rps = rows_per_sweep(c);
-  for (uint64_t t0 = 0; t0 < n; t0 += kChunk) {
+  for (uint64_t t0 = done; t0 < n; t0 += kChunk) {
     const int m = (int)std::min<uint64_t>(kChunk, n - t0);
     for (int t = 0; t < m; ++t) {
       for (int col = 0; col < c->ncol; ++col) {
@@ -685,7 +720,7 @@ int enqueue(vg_ctx* c, uint64_t n, bool measure) {
         if ((rc = launch_pass(c, col, true, c->sweep + t0 + t, row))) return rc;
       }
     }
-    if (measure && (rc = launch_reduce(c, m, c->d_sums + t0 * kNumSums))) return rc;
+    if (measure && (rc = launch_reduce(c, m, c->d_sums + t0 * kNumSums, (long long)rps))) return rc;
   }
   c->sweep += n;
   if (measure) c->last_batch = n;
@@ -826,6 +861,8 @@ void destroy(vg_ctx* c) {
   for (int k = 0; k < 2; ++k)
     for (int a = 0; a < 3; ++a)
       if (c->spin[k][a]) cudaFree(c->spin[k][a]);
+  for (int k = 0; k < 2; ++k)
+    if (c->tile_buf[k]) cudaFree(c->tile_buf[k]);
   for (int k = 0; k < kMaxColours; ++k) {
     if (c->d_sites[k]) cudaFree(c->d_sites[k]);
     if (c->d_nbr[k]) cudaFree(c->d_nbr[k]);
@@ -938,7 +975,7 @@ int vg_ctx_create_ex(const vg_lattice_desc* lat, const vg_hamiltonian_desc* ham,
     return fail(nullptr, VG_ERR_INVALID_ARG, "unknown proposal");
   if (opt->precision != VG_FP32 && opt->precision != VG_FP64)
     return fail(nullptr, VG_ERR_INVALID_ARG, "unknown precision");
-  if (opt->path < VG_PATH_AUTO || opt->path > VG_PATH_RESIDENT) return fail(nullptr, VG_ERR_INVALID_ARG, "unknown path");
+  if (opt->path < VG_PATH_AUTO || opt->path > VG_PATH_TILED) return fail(nullptr, VG_ERR_INVALID_ARG, "unknown path");
   if (opt->threads_per_block && (opt->threads_per_block % 32 || opt->threads_per_block > 256 ||
                                  opt->threads_per_block < 32))
     return fail(nullptr, VG_ERR_INVALID_ARG, "threads_per_block must be a multiple of 32 in [32, 256]");
@@ -1002,9 +1039,42 @@ int vg_ctx_create_ex(const vg_lattice_desc* lat, const vg_hamiltonian_desc* ham,
     return fail(nullptr, VG_ERR_UNSUPPORTED, "the resident path needs an Ising lattice of at most 65536 sites "
                                              "that admits the checkerboard layout");
   }
+  // the tiled sweep kernel: Ising on a fully periodic checkerboard lattice
+  // whose rows fit a tiling of shared memory
+  IsingTileArgs plan{};
+  const bool tile_ok = sc_ok && opt->spin_kind == VG_SPIN_ISING && lat->pbc_x && lat->pbc_y && lat->pbc_z &&
+                       lat->ny >= 4 && lat->nz >= 4 &&
+                       ising_tile_plan(lat->nx / 2, lat->ny, lat->nz, c->sm_count, &plan);
+  if (opt->path == VG_PATH_TILED && !tile_ok) {
+    destroy(c);
+    return fail(nullptr, VG_ERR_UNSUPPORTED, "the tiled path needs an Ising sc lattice, periodic on every axis, with "
+                                             "x a multiple of 32, even y and z of at least 4");
+  }
+  const bool tile_auto = tile_ok && (long long)lat->ny * lat->nz >= kTileAutoRowsPerSm * (long long)c->sm_count;
   if (opt->path == VG_PATH_GENERIC || !(sc_ok || sub_ok)) c->path = VG_PATH_GENERIC;
   else if (opt->path == VG_PATH_RESIDENT || (opt->path == VG_PATH_AUTO && res_ok && g.n <= 8192)) c->path = VG_PATH_RESIDENT;
+  else if (opt->path == VG_PATH_TILED || (opt->path == VG_PATH_AUTO && tile_auto)) c->path = VG_PATH_TILED;
   else c->path = VG_PATH_STRUCTURED;
+  if (c->path == VG_PATH_TILED) {
+    plan.Hx = lat->nx / 2;
+    plan.Ly = lat->ny;
+    plan.Lz = lat->nz;
+    plan.G = plan.Hx / kIsingGroup;
+    plan.fG = make_fastdiv((uint32_t)plan.G);
+    c->tile = plan;
+    e = ising_tile_prepare();
+    if (e != cudaSuccess) {
+      int r = cuda_fail(nullptr, e, "tiled sweep kernel set-up");
+      destroy(c);
+      return r;
+    }
+    for (int k = 0; k < 2 && !rc; ++k) rc = dalloc(c, (void**)&c->tile_buf[k], (size_t)(g.n / 2));
+    if (rc) {
+      g_err = c->err;
+      destroy(c);
+      return rc;
+    }
+  }
 
   if (sc_layout(c)) {
     c->ncol = 2;
@@ -1385,7 +1455,7 @@ int vg_current_sums(vg_ctx* c, vg_sums* out) {
     char* row = (char*)c->d_part + (size_t)col * c->grid * kNumSums * 8;
     if ((rc = launch_pass(c, col, false, c->sweep, row))) return rc;
   }
-  if ((rc = launch_reduce(c, 1, c->d_sums))) return rc;
+  if ((rc = launch_reduce(c, 1, c->d_sums, (long long)rows_per_sweep(c)))) return rc;
   double* raw = nullptr;
   if ((rc = read_raw(c, 1, &raw))) return rc;
   finish_sums(c, raw, out);

@@ -246,6 +246,19 @@ struct IsingGenArgs {         // any lattice: natural order uint8 0/1 + ELL
   double T;                   // per-bond path: temperature (clamped)
 };
 
+// One Ising sweep per launch on a fully periodic sc checkerboard lattice
+// (vg_tiled.cu): both classes of a tile of whole x rows staged in shared
+// memory with halos; a sweep reads the class arrays `in` and writes `out`.
+struct IsingTileArgs {
+  const uint8_t* in[2];
+  uint8_t* out[2];
+  int Hx, Ly, Lz, G;          // Hx = Lx/2 bytes per class row, G = Hx/16
+  int nyt, nzt;               // tiles along y and z (grid = nyt x nzt blocks)
+  int TYm, TZm;               // the largest tile's extents (shared-memory layout)
+  FastDiv fG;
+};
+constexpr size_t kTileSmemMax = 200 * 1024;  // dynamic shared memory per block
+
 template <typename R>
 struct HeisScArgs {           // sc checkerboard, class-separated SoA
   R* x[2];
@@ -343,6 +356,14 @@ cudaError_t launch_heis_delta(const double* spins, const double* prop, int64_t n
 cudaError_t launch_ising_sub(const IsingSubArgs& a, int nb, const IsingTable& tab, RngKey key, int colour,
                              int proposal, bool update, long long* part, int grid, int tpb, cudaStream_t s);
 size_t ising_resident_smem(const IsingScArgs& a);
+// The tiled sweep kernel: its tiling for a lattice (false if none fits), its
+// dynamic shared memory, the per-device opt-in, and one sweep (part: one row
+// of sums per tile, or null).
+bool ising_tile_plan(int Hx, int Ly, int Lz, int sm_count, IsingTileArgs* a);
+size_t ising_tile_smem(int Hx, int TYm, int TZm);
+cudaError_t ising_tile_prepare();
+cudaError_t launch_ising_tile_sweep(const IsingTileArgs& a, const IsingTable& tab, RngKey key, int proposal,
+                                    long long* part, cudaStream_t s);
 cudaError_t launch_ising_resident(const IsingScArgs& a, const IsingTable& tab, RngKey key, int proposal,
                                   uint32_t n_sweeps, double* sums, int tpb, cudaStream_t s);
 cudaError_t launch_ising_gen(const IsingGenArgs& a, const IsingTable& tab, RngKey key, int colour,

@@ -23,13 +23,13 @@ from typing import Optional, Sequence, Tuple
 import numpy as np
 
 from . import _abi
-from ._abi import (CELL_BCC, CELL_FCC, CELL_SC, FP32, FP64, PATH_AUTO, PATH_GENERIC, PATH_RESIDENT, PATH_STRUCTURED,
+from ._abi import (CELL_BCC, CELL_FCC, CELL_SC, FP32, FP64, PATH_AUTO, PATH_GENERIC, PATH_RESIDENT, PATH_STRUCTURED, PATH_TILED,
                    PROPOSE_FLIP, PROPOSE_RANDOM, SPIN_HEISENBERG, SPIN_ISING, Sums, VegasGpuError)
 
 __all__ = [
     "Lattice", "Exchange", "UniaxialAnisotropy", "Zeeman", "Gauge", "CubicAnisotropy", "hamiltonian",
     "Engine", "Sums", "VegasGpuError", "lib", "SPIN_ISING", "SPIN_HEISENBERG", "PROPOSE_FLIP",
-    "PROPOSE_RANDOM", "PATH_AUTO", "PATH_GENERIC", "PATH_STRUCTURED", "PATH_RESIDENT", "FP32", "FP64", "Batch",
+    "PROPOSE_RANDOM", "PATH_AUTO", "PATH_GENERIC", "PATH_STRUCTURED", "PATH_RESIDENT", "PATH_TILED", "FP32", "FP64", "Batch",
     "HeisReplica", "HysteresisBatch", "hysteresis_fields", "loop_area", "coercive_fields",
 ]
 
@@ -181,8 +181,10 @@ class Engine:
     basis sublattice for bcc / fcc (Ising when x is a multiple of 16,
     Heisenberg always); PATH_GENERIC runs neighbour tables on any lattice and
     is the one per-bond exchange constants need; PATH_RESIDENT keeps a small
-    sc Ising lattice in one block's shared memory.  All paths draw the same
-    random numbers for the same site, sweep and seed.
+    sc Ising lattice in one block's shared memory; PATH_TILED runs each sweep
+    of a fully periodic sc Ising lattice as one launch over shared-memory
+    tiles with halos.  All paths draw the same random numbers for the same
+    site, sweep and seed.
     """
 
     def __init__(self, lattice: Lattice, ham: _abi.HamiltonianDesc, spin: int = SPIN_ISING, seed: int = 0,

@@ -15,7 +15,7 @@ VG_OK, VG_ERR_INVALID_ARG, VG_ERR_CUDA, VG_ERR_TIMEOUT, VG_ERR_OOM, VG_ERR_UNSUP
 SPIN_ISING, SPIN_HEISENBERG = 0, 1
 CELL_SC, CELL_BCC, CELL_FCC = 0, 1, 2
 PROPOSE_FLIP, PROPOSE_RANDOM = 0, 1
-PATH_AUTO, PATH_GENERIC, PATH_STRUCTURED, PATH_RESIDENT = 0, 1, 2, 3
+PATH_AUTO, PATH_GENERIC, PATH_STRUCTURED, PATH_RESIDENT, PATH_TILED = 0, 1, 2, 3, 4
 FP32, FP64 = 0, 1
 
 
