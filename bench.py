@@ -71,9 +71,9 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def read_profile_traffic():
-    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary."""
-    path = os.path.join(REPO, "profiles", "ising_sc_pass_256cubed.md")
+def read_profile_traffic(name):
+    """Per-launch DRAM bytes of the dominant kernel from its committed ncu summary."""
+    path = os.path.join(REPO, "profiles", name)
     try:
         for line in open(path):
             if line.startswith("traffic_bytes_per_launch:"):
@@ -199,6 +199,37 @@ def run_reference(args, rank):
         "gpu_launches": 0,
     }
     print(json.dumps(line), flush=True)
+
+
+def run_two_pass(V, torch, args, n_l, flush):
+    """The same workload on the two-pass checkerboard kernels (one launch per
+    colour pass, neighbour rows from L2): the path the tiled kernel replaces,
+    timed with the same step protocol for comparison."""
+    N = n_l ** 3
+    temps = ladder()
+    with V.Engine(V.Lattice.sc(n_l, n_l, n_l), V.hamiltonian(V.Exchange(1.0)), spin=V.SPIN_ISING, seed=SEED,
+                  path=V.PATH_STRUCTURED) as eng:
+        eng.init_random()
+        s = torch.cuda.ExternalStream(eng.stream())
+        for k in range(3):
+            eng.set_thermostat(temps[k])
+            eng.sweeps_async(SWEEPS_PER_STEP, measure=True)
+        eng.synchronize()
+        steps = 5
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for k, (a, c) in enumerate(ev):
+            with torch.cuda.stream(s):
+                flush.fill_(1.0)
+            eng.set_thermostat(temps[(3 + k) % len(temps)])
+            a.record(s)
+            eng.sweeps_async(SWEEPS_PER_STEP, measure=True)
+            c.record(s)
+        eng.synchronize()
+        ms = sum(a.elapsed_time(c) for a, c in ev)
+    v = float(N) * SWEEPS_PER_STEP * steps / (ms * 1e6)
+    peak, _ = peaks()
+    return {"value": v, "unit": "flips/ns", "kernel": "ising_sc2_kernel (one colour pass per launch)",
+            "roofline_frac": v * BYTES_PER_FLIP / peak, "steps": steps}
 
 
 def run_batched(V, torch, args):
@@ -600,7 +631,9 @@ def main():
 
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     stops = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    launches_per_step = SWEEPS_PER_STEP * info.n_colours + (SWEEPS_PER_STEP + 63) // 64
+    tiled = info.path == V.PATH_TILED
+    # one launch per sweep (tiled) or per colour pass, plus the sum reductions
+    launches_per_step = SWEEPS_PER_STEP * (1 if tiled else info.n_colours) + (SWEEPS_PER_STEP + 63) // 64
     with Clocks(local_rank) as clk:
         clk.mark_start()
         wall0 = time.perf_counter()
@@ -628,13 +661,19 @@ def main():
     # step is SWEEPS_PER_STEP x n_colours passes plus a few sum reductions,
     # which are charged to the passes); an isolated per-launch timing is
     # reported beside it.
-    passes = SWEEPS_PER_STEP * info.n_colours * args.steps
+    passes = SWEEPS_PER_STEP * (1 if tiled else info.n_colours) * args.steps
     pass_ms = dev_ms / passes
     iso_pass_ms, sweep_ms = eng.time_passes(50, measure=True)
-    alg_bytes_per_launch = 1.5 * N  # read both classes (N bytes), write one class (N/2)
+    # algorithmic bytes: (C + 1) x 1 byte per site and sweep, C = 2 colour
+    # passes -- a colour pass reads both classes (N) and writes one (N/2); a
+    # tiled launch is one sweep (3 N), whatever its real traffic (the tiles
+    # read each class once and write each once, 2 N plus halos)
+    alg_bytes_per_launch = (3.0 if tiled else 1.5) * N
     achieved = alg_bytes_per_launch / (pass_ms * 1e-3) / 1e9
     peak, peak_kind = peaks()
-    traffic = read_profile_traffic()
+    traffic = read_profile_traffic("ising_tile_sweep_256cubed.md" if tiled else "ising_sc_pass_256cubed.md")
+    kernel = ("ising_tile_sweep_kernel (one sweep: both colour passes on shared-memory tiles)" if tiled
+              else "ising_sc2_kernel (one colour pass)")
 
     # end to end through the C ABI with host buffers
     import ctypes as C
@@ -660,6 +699,8 @@ def main():
     e2e_value = float(N) * SWEEPS_PER_STEP * e2e_steps * world / (e2e_s * 1e9)
     lib.vg_host_free(hbuf)
     lib.vg_host_free(obuf)
+
+    two_pass = run_two_pass(V, torch, args, n_l, flush) if tiled else None
 
     batched = None
     if not args.no_batched:
@@ -691,17 +732,18 @@ def main():
                        "l2": "flushed between steps (256 MiB write, outside the events); the 16.8 MB lattice is "
                              "L2-resident within a step",
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                       "path": {1: "generic", 2: "structured"}.get(info.path, "?")},
+                       "path": {1: "generic", 2: "structured", 4: "tiled"}.get(info.path, "?")},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
-                         "kernel": "ising_sc2_kernel (one colour pass)", "pass_ms": pass_ms,
-                         "pass_ms_isolated_events": iso_pass_ms,
+                         "kernel": kernel, "launch_ms": pass_ms,
+                         "launch_ms_isolated_events": iso_pass_ms,
                          "alg_bytes_per_launch": alg_bytes_per_launch, "peak_kind": peak_kind,
                          "note": "frac > 1 means the lattice is served from L2"},
             "e2e": {"value": e2e_value, "unit": "flips/ns", "h2d_bytes_per_step": N,
                     "d2h_bytes_per_step": N + 16 * SWEEPS_PER_STEP},
             "gpu_launches": launches_per_step * args.steps,
             "cpu_baseline": cpu,
+            "two_pass": two_pass,
             "batched": batched,
             "batched_vs_plain": (batched["value"] / value) if batched else None,
             "cooldown_2d": cool,

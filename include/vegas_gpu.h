@@ -184,9 +184,11 @@ int vg_sweeps_async(vg_ctx* ctx, uint64_t n, int32_t measure);
 int vg_read_sums(vg_ctx* ctx, uint64_t count, vg_sums* out);
 int vg_synchronize(vg_ctx* ctx);
 
-/* Run n sweeps with a CUDA event pair around every colour pass on the
- * context stream; returns the mean pass duration and the mean sweep
- * duration (ms).  The sweeps are real work (the sweep index advances). */
+/* Run n sweeps with a CUDA event pair around every launch on the context
+ * stream; returns the mean launch duration and the mean sweep duration (ms).
+ * A launch is one colour pass, or on the tiled path one whole sweep (there n
+ * is rounded up to an even count).  The sweeps are real work (the sweep
+ * index advances). */
 int vg_time_passes(vg_ctx* ctx, uint64_t n, int32_t measure, double* mean_pass_ms, double* mean_sweep_ms);
 
 /* Wolff cluster steps (WolffIntegrator::step, src/integrator.rs:140-230) of

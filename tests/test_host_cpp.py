@@ -42,6 +42,10 @@ def test_parquet_writer_is_read_by_arrow(tmp_path):
     assert not (tmp_path / "demo.parquet.tmp").exists()
     f = pq.ParquetFile(str(tmp_path / "demo.parquet"))
     assert f.metadata.num_rows == 2500 and f.metadata.num_row_groups == 3
+    # pages compressed with SNAPPY, as the reference writes them (src/output.rs:48)
+    for g in range(3):
+        for k in range(8):
+            assert f.metadata.row_group(g).column(k).compression == "SNAPPY"
     t = f.read()
     assert t.schema.names == ["relax", "stage", "step", "n", "temperature", "field", "energy", "magnetization"]
     assert [t.schema.field(k).type for k in range(8)] == [pa.bool_(), pa.uint64(), pa.uint64(), pa.uint64(),

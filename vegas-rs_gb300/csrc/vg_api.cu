@@ -1410,21 +1410,41 @@ int vg_time_passes(vg_ctx* c, uint64_t n, int32_t measure, double* pass_ms, doub
   if (!c || n == 0) return VG_ERR_INVALID_ARG;
   VG_CUDA(c, cudaSetDevice(c->device));
   int rc;
-  if ((rc = check_sweeps(c, n))) return rc;
   if (measure) {
-    if ((rc = ensure_sums(c, (size_t)n))) return rc;
+    if ((rc = ensure_sums(c, (size_t)n + 1))) return rc;
     if ((rc = ensure_part(c, rows_per_sweep(c) * kChunk))) return rc;
   }
-  std::vector<cudaEvent_t> ev((size_t)n * c->ncol * 2);
+  // a launch is one colour pass, or on the tiled path one whole sweep (an
+  // even number of them, so that the state ends in the class arrays)
+  const bool tiled = c->path == VG_PATH_TILED;
+  if (tiled) n = (n + 1) & ~1ull;
+  if ((rc = check_sweeps(c, n))) return rc;
+  const int per_sweep = tiled ? 1 : c->ncol;
+  if (tiled && measure && (rc = ensure_part(c, (size_t)tile_count(c) * kChunk))) return rc;
+  std::vector<cudaEvent_t> ev((size_t)n * per_sweep * 2);
   for (auto& e : ev) VG_CUDA(c, cudaEventCreate(&e));
   const size_t rps = rows_per_sweep(c);
+  const IsingTable tab = is_ising(c) ? ising_table(c) : IsingTable{};
   for (uint64_t t = 0; t < n; ++t) {
-    for (int col = 0; col < c->ncol; ++col) {
-      char* row = nullptr;
-      if (measure) row = (char*)c->d_part + ((size_t)(t % kChunk) * rps + (size_t)col * c->grid) * kNumSums * 8;
-      const size_t k = ((size_t)t * c->ncol + col) * 2;
+    for (int col = 0; col < per_sweep; ++col) {
+      const size_t k = ((size_t)t * per_sweep + col) * 2;
       VG_CUDA(c, cudaEventRecord(ev[k], c->stream));
-      if ((rc = launch_pass(c, col, true, c->sweep + t, row))) return rc;
+      if (tiled) {
+        IsingTileArgs a = c->tile;
+        uint8_t* base[2] = {(uint8_t*)c->spin[0][0], (uint8_t*)c->spin[1][0]};
+        for (int q = 0; q < 2; ++q) {
+          a.in[q] = (t & 1) ? c->tile_buf[q] : base[q];
+          a.out[q] = (t & 1) ? base[q] : c->tile_buf[q];
+        }
+        long long* part = measure ? (long long*)c->d_part + (size_t)(t % kChunk) * tile_count(c) * kNumSums : nullptr;
+        const cudaError_t e = launch_ising_tile_sweep(a, tab, rng_key(c, c->sweep + t), c->opt.proposal, part,
+                                                      c->stream);
+        if (e != cudaSuccess) return cuda_fail(c, e, "tiled sweep launch");
+      } else {
+        char* row = nullptr;
+        if (measure) row = (char*)c->d_part + ((size_t)(t % kChunk) * rps + (size_t)col * c->grid) * kNumSums * 8;
+        if ((rc = launch_pass(c, col, true, c->sweep + t, row))) return rc;
+      }
       VG_CUDA(c, cudaEventRecord(ev[k + 1], c->stream));
     }
   }
@@ -1440,7 +1460,7 @@ int vg_time_passes(vg_ctx* c, uint64_t n, int32_t measure, double* pass_ms, doub
   span = whole;
   for (auto& e : ev) cudaEventDestroy(e);
   c->sweep += n;
-  if (pass_ms) *pass_ms = tot / (double)(n * c->ncol);
+  if (pass_ms) *pass_ms = tot / (double)(n * per_sweep);
   if (sweep_ms) *sweep_ms = span / (double)n;
   return VG_OK;
 }

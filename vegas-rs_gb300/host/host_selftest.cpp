@@ -55,7 +55,52 @@ static int count_lines(const std::string& s) {
   return n;
 }
 
+static void snappy_checks() {
+  // round trips of the page compressor over its element kinds: literals of
+  // every length class, short and long copies, overlapping runs, far offsets
+  std::vector<std::vector<uint8_t>> cases;
+  cases.push_back({});
+  cases.push_back({42});
+  std::vector<uint8_t> run(100000, 7);
+  cases.push_back(run);
+  std::vector<uint8_t> text;
+  for (int i = 0; i < 5000; ++i) {
+    const char* w = (i % 7 == 0) ? "magnetization " : (i % 3 == 0) ? "energy " : "step ";
+    text.insert(text.end(), w, w + std::strlen(w));
+  }
+  cases.push_back(text);
+  uint64_t x = 88172645463325252ull;
+  std::vector<uint8_t> noise(300000);
+  for (auto& b : noise) {
+    x ^= x << 13;
+    x ^= x >> 7;
+    x ^= x << 17;
+    b = (uint8_t)x;
+  }
+  cases.push_back(noise);
+  std::vector<uint8_t> far = noise;  // a repeat 100 KB back: four-byte offsets
+  far.insert(far.end(), noise.begin(), noise.begin() + 70000);
+  cases.push_back(far);
+  std::vector<uint8_t> doubles;  // PLAIN float64 / uint64 columns as the observables write them
+  for (int i = 0; i < 20000; ++i) {
+    const double d = -1.0 * (i / 7);
+    const uint64_t u = (uint64_t)(i / 3);
+    const uint8_t* p = reinterpret_cast<const uint8_t*>(&d);
+    doubles.insert(doubles.end(), p, p + 8);
+    const uint8_t* q = reinterpret_cast<const uint8_t*>(&u);
+    doubles.insert(doubles.end(), q, q + 8);
+  }
+  cases.push_back(doubles);
+  for (const auto& c : cases) {
+    const std::vector<uint8_t> z = snappy::compress(c);
+    CHECK(snappy::decompress(z.data(), z.size()) == c);
+  }
+  CHECK(snappy::compress(run).size() < run.size() / 20);
+  CHECK(snappy::compress(doubles).size() < doubles.size() / 2);
+}
+
 static void cpu_checks() {
+  snappy_checks();
   // CoolDown / HysteresisLoop schedules (src/program.rs:202-211, :302-332)
   CHECK(CoolDown(4.0, 0.1, 0.1).temperatures().size() == 39);
   CHECK(CoolDown(5.5, 3.5, 0.1).temperatures().size() == 21);

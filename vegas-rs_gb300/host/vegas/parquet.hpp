@@ -6,8 +6,8 @@
 // written to "<path>.parquet.tmp" (Path::with_extension) and renamed over the
 // destination when the writer is dropped.  This writer produces files with
 // the same schema, column order and row grouping: PLAIN-encoded values in
-// one data page per column chunk, no compression (the reference uses
-// SNAPPY; readers decode either), and the file metadata in Thrift's compact
+// one data page per column chunk, compressed with SNAPPY as the
+// reference's pages are (snappy.hpp), and the file metadata in Thrift's compact
 // protocol as the Parquet format specifies (parquet.thrift: FileMetaData,
 // SchemaElement, RowGroup, ColumnChunk, ColumnMetaData, PageHeader,
 // DataPageHeader).
@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "error.hpp"
+#include "snappy.hpp"
 
 namespace vegas {
 namespace parquet {
@@ -188,9 +189,9 @@ class Writer {
         m.elem_i32(0);  // PLAIN
         m.field_list(3, kBinary, 1);
         m.elem_string(cols_[k].name);
-        m.field_i32(4, 0);  // UNCOMPRESSED
+        m.field_i32(4, 1);  // SNAPPY
         m.field_i64(5, (int64_t)g.rows);
-        m.field_i64(6, ch.size);
+        m.field_i64(6, ch.uncompressed);
         m.field_i64(7, ch.size);
         m.field_i64(9, ch.offset);  // data_page_offset
         m.end_struct();
@@ -215,7 +216,7 @@ class Writer {
 
  private:
   struct Chunk {
-    int64_t offset, size;
+    int64_t offset, size, uncompressed;  // size: page header + compressed values, as written
   };
   struct Group {
     size_t rows;
@@ -242,11 +243,12 @@ class Writer {
       } else {
         values.swap(c.data);
       }
+      const std::vector<uint8_t> packed = snappy::compress(values);
       Compact h;  // PageHeader
       h.begin_struct();
       h.field_i32(1, 0);  // DATA_PAGE
-      h.field_i32(2, (int32_t)values.size());
-      h.field_i32(3, (int32_t)values.size());
+      h.field_i32(2, (int32_t)values.size());  // uncompressed_page_size
+      h.field_i32(3, (int32_t)packed.size());  // compressed_page_size
       h.field_struct(5);  // DataPageHeader
       h.field_i32(1, (int32_t)rows_);
       h.field_i32(2, 0);  // PLAIN
@@ -256,8 +258,8 @@ class Writer {
       h.end_struct();
       const int64_t start = offset_;
       put(h.out.data(), h.out.size());
-      if (!values.empty()) put(values.data(), values.size());
-      g.chunks.push_back(Chunk{start, offset_ - start});
+      put(packed.data(), packed.size());
+      g.chunks.push_back(Chunk{start, offset_ - start, (int64_t)(h.out.size() + values.size())});
       c.data.clear();
     }
     total_rows_ += rows_;

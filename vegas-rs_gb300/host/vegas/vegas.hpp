@@ -21,5 +21,6 @@
 #include "lattice.hpp"
 #include "machine.hpp"
 #include "program.hpp"
+#include "snappy.hpp"
 #include "state.hpp"
 #include "thermostat.hpp"
