@@ -63,7 +63,7 @@ enum vg_proposal { VG_PROPOSE_FLIP = 0, VG_PROPOSE_RANDOM = 1 };
  * (vg_set_exchange_bonds).  RESIDENT keeps the checkerboard layout of STRUCTURED in one
  * thread block's shared memory and runs all sweeps of a call in one launch
  * (Ising, at most 65536 sites).  TILED (Ising sc, periodic on every axis,
- * x a multiple of 32, even y and z >= 4) runs each sweep as one launch:
+ * x a multiple of 64, even y and z >= 4) runs each sweep as one launch:
  * both colour passes on shared-memory tiles with halos, reading the class
  * arrays and writing a second pair, so the context holds twice the spins;
  * AUTO takes it for lattices of at least 64 x-rows (y x z) per SM.  Results

@@ -298,9 +298,9 @@ def test_one_call_equals_single_sweep_calls(V, ext, pbc, proposal):
 
 
 TILED = [  # extents (all periodic), proposal, sweeps (odd counts end with one two-pass sweep)
-    ((32, 4, 4), 0, 6),
+    ((64, 4, 4), 0, 6),       # tile boxes wrap onto themselves in y and z
     ((64, 8, 6), 1, 5),
-    ((96, 18, 6), 0, 7),      # 3 groups per row
+    ((192, 18, 6), 0, 7),     # 6 groups (3 pairs) per row
     ((128, 10, 12), 1, 4),
     ((1024, 40, 36), 0, 3),   # 512-byte rows: several tiles per SM (more than one wave)
 ]
@@ -342,7 +342,8 @@ def test_tiled_path_selection(V):
         assert eng.info().path == V.PATH_TILED  # AUTO: at least 64 rows per SM
     with _engine(V, "sc", (64, 16, 16), (1, 1, 1), H, 1) as eng:
         assert eng.info().path != V.PATH_TILED
-    for ext, pbc in (((64, 8, 6), (1, 1, 0)), ((16, 8, 8), (1, 1, 1)), ((64, 2, 8), (1, 1, 1))):
+    for ext, pbc in (((64, 8, 6), (1, 1, 0)), ((32, 8, 8), (1, 1, 1)), ((96, 8, 8), (1, 1, 1)),
+                     ((64, 2, 8), (1, 1, 1))):
         with pytest.raises(V.VegasGpuError) as e:
             _engine(V, "sc", ext, pbc, H, 1, path=V.PATH_TILED)
         assert e.value.status == 5

@@ -100,3 +100,51 @@ def test_cli_run_and_bench(tmp_path):
     assert (tmp_path / "obs.parquet").exists() and not (tmp_path / "obs.parquet.tmp").exists()
     r = subprocess.run([_bin("vegas_gpu_cli"), "bench", "potts", "8"], capture_output=True, text=True, timeout=60)
     assert r.returncode == 1 and "unknown model" in r.stderr
+
+
+@pytest.mark.gpu
+def test_cli_run_matches_reference_cpu_statistically(tmp_path, O):
+    """`vegas_gpu_cli run` (src/main.rs:61-75: Input::run with the GPU
+    integrator, src/input.rs:347-367) against the reference restatement
+    ref_cpu at one CoolDown temperature: sc 32x32x1 (PBC x, y), Relax 500 at
+    T = 2.5, then CoolDown(2.5, 2.5, 0.1) -- the single temperature 2.5 --
+    with 100 relax + 2000 measured sweeps.  16 CLI runs (seeds 1..16) against
+    16 ref_cpu chains of the same schedule; the StatSensor line's <E>, C,
+    <|M|> and chi (src/instrument.rs:113-126) agree within 3 combined
+    standard errors of the run-to-run means."""
+    import numpy as np
+
+    toml = tmp_path / "in.toml"
+    toml.write_text(
+        'model = "Ising"\nalgorithm = "Metropolis"\n[sample.unitcell]\nname = "sc"\n'
+        "[sample.size]\nx = 32\ny = 32\nz = 1\n[sample.pbc]\nx = true\ny = true\nz = false\n"
+        '[[stages]]\nprogram = "Relax"\nsteps = 500\ntemperature = 2.5\n'
+        '[[stages]]\nprogram = "CoolDown"\nmax_temperature = 2.5\nmin_temperature = 2.5\ncool_rate = 0.1\n'
+        "relax = 100\nsteps = 2000\n")
+    runs = 16
+    gpu = []
+    for s in range(1, runs + 1):
+        r = subprocess.run([_bin("vegas_gpu_cli"), "run", str(toml), "-s", str(s)], capture_output=True, text=True,
+                           timeout=120)
+        assert r.returncode == 0, r.stderr
+        lines = r.stdout.strip().splitlines()
+        assert len(lines) == 1
+        gpu.append([float(x) for x in lines[0].split()])
+    gpu = np.array(gpu)
+    assert np.all(gpu[:, 0] == 2.5)
+    N, T = 1024, 2.5
+    g = O.Graph(O.lattice("sc", 32, 32, 1, (1, 1, 0)))
+    Hr = O.Hamiltonian(has_exchange=1, J=1.0, has_zeeman=1, zeeman_sign=1.0, compound=1)
+    cpu = []
+    for s in range(runs):
+        rng = O.pcg64(500 + s)
+        st, _ = g.ref_sweeps(0, g.ising_init(900 + s), Hr, T, 600, rng, measure=False, clone=False)
+        _, obs = g.ref_sweeps(0, st, Hr, T, 2000, rng, clone=False)
+        E, M = obs[:, 0], obs[:, 1]
+        # the StatSensor columns: T, |B|, <E>, Var(E)/(N T^2), <|M|>, Var(|M|)/(N T), U4
+        cpu.append([E.mean(), E.var() / (N * T * T), M.mean(), M.var() / (N * T)])
+    cpu = np.array(cpu)
+    for col, k in ((2, 0), (3, 1), (4, 2), (5, 3)):
+        a, b = gpu[:, col], cpu[:, k]
+        se = np.hypot(a.std(ddof=1), b.std(ddof=1)) / np.sqrt(runs)
+        assert abs(a.mean() - b.mean()) < 3 * se, (col, a.mean(), b.mean(), se)

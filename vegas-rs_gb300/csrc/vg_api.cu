@@ -53,6 +53,7 @@ struct vg_ctx {
   // into, and the tiling of the y-z plane of rows
   uint8_t* tile_buf[2] = {nullptr, nullptr};
   IsingTileArgs tile{};
+  int* d_tile_err = nullptr;  // raised by a tiled sweep whose staging wait ran out
   // generic path tables
   std::vector<int64_t> class_size;
   int32_t* d_sites[kMaxColours] = {};
@@ -792,6 +793,14 @@ void energy_of(const vg_ctx* c, const vg_sums* s, double* E, double* M) {
 
 int sync_stream(vg_ctx* c) {
   VG_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (c->d_tile_err) {  // a tiled sweep that gave up writes nothing: the state is not to be trusted
+    int flag = 0;
+    VG_CUDA(c, cudaMemcpy(&flag, c->d_tile_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flag) {
+      VG_CUDA(c, cudaMemset(c->d_tile_err, 0, sizeof(int)));
+      return fail(c, VG_ERR_TIMEOUT, "a tiled sweep's wait for its staged rows ran out; the state is undefined");
+    }
+  }
   return VG_OK;
 }
 
@@ -863,6 +872,7 @@ void destroy(vg_ctx* c) {
       if (c->spin[k][a]) cudaFree(c->spin[k][a]);
   for (int k = 0; k < 2; ++k)
     if (c->tile_buf[k]) cudaFree(c->tile_buf[k]);
+  if (c->d_tile_err) cudaFree(c->d_tile_err);
   for (int k = 0; k < kMaxColours; ++k) {
     if (c->d_sites[k]) cudaFree(c->d_sites[k]);
     if (c->d_nbr[k]) cudaFree(c->d_nbr[k]);
@@ -1048,7 +1058,7 @@ int vg_ctx_create_ex(const vg_lattice_desc* lat, const vg_hamiltonian_desc* ham,
   if (opt->path == VG_PATH_TILED && !tile_ok) {
     destroy(c);
     return fail(nullptr, VG_ERR_UNSUPPORTED, "the tiled path needs an Ising sc lattice, periodic on every axis, with "
-                                             "x a multiple of 32, even y and z of at least 4");
+                                             "x a multiple of 64, even y and z of at least 4");
   }
   const bool tile_auto = tile_ok && (long long)lat->ny * lat->nz >= kTileAutoRowsPerSm * (long long)c->sm_count;
   if (opt->path == VG_PATH_GENERIC || !(sc_ok || sub_ok)) c->path = VG_PATH_GENERIC;
@@ -1060,7 +1070,14 @@ int vg_ctx_create_ex(const vg_lattice_desc* lat, const vg_hamiltonian_desc* ham,
     plan.Ly = lat->ny;
     plan.Lz = lat->nz;
     plan.G = plan.Hx / kIsingGroup;
-    plan.fG = make_fastdiv((uint32_t)plan.G);
+    if ((rc = dalloc(c, (void**)&c->d_tile_err, sizeof(int))) ||
+        (e = cudaMemsetAsync(c->d_tile_err, 0, sizeof(int), c->stream)) != cudaSuccess) {
+      if (!rc) rc = cuda_fail(nullptr, e, "tiled path set-up");
+      g_err = c->err.empty() ? g_err : c->err;
+      destroy(c);
+      return rc;
+    }
+    plan.err = c->d_tile_err;
     c->tile = plan;
     e = ising_tile_prepare();
     if (e != cudaSuccess) {

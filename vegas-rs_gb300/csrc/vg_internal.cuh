@@ -252,10 +252,11 @@ struct IsingGenArgs {         // any lattice: natural order uint8 0/1 + ELL
 struct IsingTileArgs {
   const uint8_t* in[2];
   uint8_t* out[2];
-  int Hx, Ly, Lz, G;          // Hx = Lx/2 bytes per class row, G = Hx/16
+  int Hx, Ly, Lz, G;          // Hx = Lx/2 bytes per class row, G = Hx/16 (even)
   int nyt, nzt;               // tiles along y and z (grid = nyt x nzt blocks)
-  int TYm, TZm;               // the largest tile's extents (shared-memory layout)
-  FastDiv fG;
+  int TY, TZm;                // the tiles' y extent (nyt divides Ly), the largest z extent
+  FastDiv fG2, fny0, fny;     // by G/2, TY + 2 (the class-0 box), TY
+  int* err;                   // set to 1 if a block's staging wait ran out (then it writes nothing)
 };
 constexpr size_t kTileSmemMax = 200 * 1024;  // dynamic shared memory per block
 
@@ -360,7 +361,7 @@ size_t ising_resident_smem(const IsingScArgs& a);
 // dynamic shared memory, the per-device opt-in, and one sweep (part: one row
 // of sums per tile, or null).
 bool ising_tile_plan(int Hx, int Ly, int Lz, int sm_count, IsingTileArgs* a);
-size_t ising_tile_smem(int Hx, int TYm, int TZm);
+size_t ising_tile_smem(int Hx, int TY, int TZm);
 cudaError_t ising_tile_prepare();
 cudaError_t launch_ising_tile_sweep(const IsingTileArgs& a, const IsingTable& tab, RngKey key, int proposal,
                                     long long* part, cudaStream_t s);
