@@ -93,21 +93,40 @@ __device__ __forceinline__ int plane_copies(const IsingTileArgs& a, const TileGe
   return n;
 }
 
-// Stage both boxes: thread 0 registers their total bytes on the mbarrier,
-// then lane k of warp 0 issues the copies of planes k, k + 32, ...
+// The class-0 box planes [-1, -1 + P) that the first round of colour-0
+// items can touch (a round is one item per thread), and with them class-1
+// planes [-2, P): the first of the two staging chunks.
+__device__ __forceinline__ int first_chunk_planes(const IsingTileArgs& a, const TileGeom& t) {
+  const int per_plane = (a.TY + 2) * (a.G >> 1);  // colour-0 items per box plane
+  return min(t.TZ + 2, ((int)blockDim.x + per_plane - 1) / per_plane);
+}
+
+// Stage both boxes in two chunks, each completing on its own mbarrier:
+// thread 0 registers each chunk's bytes, then lane k of warp 0 issues the
+// copies of planes k, k + 32, ... (first chunk first).
 __device__ __forceinline__ void stage_boxes(const IsingTileArgs& a, const TileGeom& t, uint8_t* s1, uint8_t* s0,
                                             uint64_t* mbar) {
   const int n1 = t.TZ + 4, n0 = t.TZ + 2;
+  const int P = first_chunk_planes(a, t);
+  // chunk 0: class-1 planes [-2, P), class-0 planes [-1, -1 + P); chunk 1: the rest
+  const int c1a = P + 2, c0a = P;
   if (threadIdx.x == 0) {
-    const uint32_t bytes = (uint32_t)((a.TY + 4) * n1 + (a.TY + 2) * n0) * (uint32_t)a.Hx;
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(mbar)), "r"(bytes)
+    const uint32_t b0 = (uint32_t)((a.TY + 4) * c1a + (a.TY + 2) * c0a) * (uint32_t)a.Hx;
+    const uint32_t b1 = (uint32_t)((a.TY + 4) * (n1 - c1a) + (a.TY + 2) * (n0 - c0a)) * (uint32_t)a.Hx;
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(mbar)), "r"(b0)
+                 : "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(mbar + 1)), "r"(b1)
                  : "memory");
   }
   __syncwarp();
   if (threadIdx.x < 32) {
     for (int k = (int)threadIdx.x; k < n1 + n0; k += 32) {
-      const int c = k < n1 ? 1 : 0;
-      const int dz = c ? k - 2 : k - n1 - 1;
+      // planes in the order chunk 0 (class 1, class 0), chunk 1 (class 1, class 0)
+      int c, dz, chunk;
+      if (k < c1a) { c = 1; dz = k - 2; chunk = 0; }
+      else if (k < c1a + c0a) { c = 0; dz = k - c1a - 1; chunk = 0; }
+      else if (k < n1 + c0a) { c = 1; dz = k - c0a - 2; chunk = 1; }
+      else { c = 0; dz = k - n1 - 1; chunk = 1; }
       Copy cp[3];
       const int m = plane_copies(a, t, c, c ? -2 : -1, c ? 2 : 1, dz, cp);
       uint8_t* sm = c ? s1 : s0;
@@ -115,7 +134,7 @@ __device__ __forceinline__ void stage_boxes(const IsingTileArgs& a, const TileGe
         asm volatile(
             "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
                 smem_addr(sm + cp[j].soff)),
-            "l"(a.in[c] + cp[j].goff), "r"(cp[j].bytes), "r"(smem_addr(mbar))
+            "l"(a.in[c] + cp[j].goff), "r"(cp[j].bytes), "r"(smem_addr(mbar + chunk))
             : "memory");
     }
   }
@@ -154,14 +173,18 @@ __device__ __forceinline__ void store_tile(const IsingTileArgs& a, const TileGeo
 
 // One colour pass over the box rows [lo, TY + hi) x [lo, TZ + hi) of class C
 // (own rows in `own`, neighbour rows in `oth`, both in shared memory); a
-// thread takes a pair of groups (32 sites) of one row per item.  Measures the
+// thread takes groups q and q + G/2 of one row per item (so that the lanes of
+// a warp read consecutive 16-byte words: no bank conflicts).  Measures the
 // tile's own rows.  Decisions as the pair kernel (vg_ising.cu): uniform
-// coordination 6, byte-parallel first digit, ties queued per warp.
+// coordination 6, byte-parallel first digit, ties queued per warp.  For
+// colour 0, the first round of items waits for the first staging chunk only
+// (*staged_all is the wait for both, done once before the second round).
 template <int C, bool MEASURE, int PROP>
 __device__ __forceinline__ void tile_pass(const IsingTileArgs& a, const TileGeom& t, int lo, int hi,
                                           const FastDiv& fny, uint8_t* own, const uint8_t* oth, const IsingTable& tab,
                                           const RngKey& key, const unsigned long long* s_thr,
-                                          uint2 (*s_q)[kTileQueue], int& bond, int& ups, int& nacc) {
+                                          uint2 (*s_q)[kTileQueue], uint64_t* mbar, int& bond, int& ups,
+                                          int& nacc) {
   constexpr int Z = 6;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int ny = a.TY + hi - lo, nz = t.TZ + hi - lo;
@@ -197,8 +220,9 @@ __device__ __forceinline__ void tile_pass(const IsingTileArgs& a, const TileGeom
 
   // whole warps walk the items (the queue needs every lane at its ballots)
   for (uint32_t base = threadIdx.x & ~31u; base < items; base += blockDim.x) {
+    if (C == 0 && base >= blockDim.x && base < 2u * blockDim.x) wait_staged(mbar + 1);  // the second chunk
     const uint32_t i = base + (uint32_t)lane;
-    uint32_t tm = 0, sgrp = 0, gid0 = 0;  // tied sites: bit k -> group gid0 + (k >> 4), site k & 15
+    uint32_t tm = 0, sgrp = 0, gid0 = 0;  // tied sites: bit k -> group gid0 + (k >> 4) * G/2, site k & 15
     bool inner = false;
     uint32_t S[8], A[8];
 #pragma unroll
@@ -210,40 +234,50 @@ __device__ __forceinline__ void tile_pass(const IsingTileArgs& a, const TileGeom
       inner = dy >= 0 && dy < a.TY && dz >= 0 && dz < t.TZ;
       const int gy = wrap(t.y0 + dy, a.Ly), gz = wrap(t.z0 + dz, a.Lz);
       const int p = (gy + gz + C) & 1;  // x parity of this row's class-C sites
-      gid0 = ((uint32_t)gz * (uint32_t)a.Ly + (uint32_t)gy) * (uint32_t)a.G + 2u * q;
-      const uint32_t h0 = 32u * q;
-      const uint32_t ro = (C ? row1(a, dy, dz) : row0(a, dy, dz)) + h0;
-      sgrp = ro >> 4;
+      gid0 = ((uint32_t)gz * (uint32_t)a.Ly + (uint32_t)gy) * (uint32_t)a.G + q;
+      const uint32_t ha = 16u * q, hb = ha + 8u * (uint32_t)a.G;  // the pair: groups q and q + G/2
+      const uint32_t ro = C ? row1(a, dy, dz) : row0(a, dy, dz);
+      sgrp = (ro + ha) >> 4;
       const uint32_t ystep = (uint32_t)a.Hx, zstep = (uint32_t)((C ? a.TY + 2 : a.TY + 4) * a.Hx);
       const uint32_t rx = C ? row0(a, dy, dz) : row1(a, dy, dz);  // the other class, same row
-      const uint4 Sa = *reinterpret_cast<const uint4*>(own + ro);
-      const uint4 Sb = *reinterpret_cast<const uint4*>(own + ro + 16);
-      const uint4 Xa = *reinterpret_cast<const uint4*>(oth + rx + h0);
-      const uint4 Xb = *reinterpret_cast<const uint4*>(oth + rx + h0 + 16);
-      const uint32_t e = p == 0 ? oth[rx + (h0 == 0 ? (uint32_t)a.Hx - 1u : h0 - 1u)]
-                                : oth[rx + (h0 + 32u == (uint32_t)a.Hx ? 0u : h0 + 32u)];
+      const uint4 Sa = *reinterpret_cast<const uint4*>(own + ro + ha);
+      const uint4 Sb = *reinterpret_cast<const uint4*>(own + ro + hb);
+      const uint4 Xa = *reinterpret_cast<const uint4*>(oth + rx + ha);
+      const uint4 Xb = *reinterpret_cast<const uint4*>(oth + rx + hb);
+      // the x neighbours outside each group's 16 bytes: byte h - 1 (p = 0) or h + 16 (p = 1), cyclic in the row
+      const uint32_t Hx = (uint32_t)a.Hx;
+      const uint32_t ea = p == 0 ? oth[rx + (ha == 0 ? Hx - 1u : ha - 1u)] : oth[rx + ha + 16u];
+      const uint32_t eb = p == 0 ? oth[rx + hb - 1u] : oth[rx + (hb + 16u == Hx ? 0u : hb + 16u)];
       const uint32_t X0[8] = {Xa.x, Xa.y, Xa.z, Xa.w, Xb.x, Xb.y, Xb.z, Xb.w};
       uint32_t X1[8];
       if (p == 0) {
-        X1[0] = __byte_perm(e << 24, X0[0], 0x6543);
+        X1[0] = __byte_perm(ea << 24, X0[0], 0x6543);
+        X1[4] = __byte_perm(eb << 24, X0[4], 0x6543);
 #pragma unroll
-        for (int w = 1; w < 8; ++w) X1[w] = __byte_perm(X0[w - 1], X0[w], 0x6543);
+        for (int w = 1; w < 4; ++w) {
+          X1[w] = __byte_perm(X0[w - 1], X0[w], 0x6543);
+          X1[w + 4] = __byte_perm(X0[w + 3], X0[w + 4], 0x6543);
+        }
       } else {
 #pragma unroll
-        for (int w = 0; w < 7; ++w) X1[w] = __byte_perm(X0[w], X0[w + 1], 0x4321);
-        X1[7] = __byte_perm(X0[7], e, 0x4321);
+        for (int w = 0; w < 3; ++w) {
+          X1[w] = __byte_perm(X0[w], X0[w + 1], 0x4321);
+          X1[w + 4] = __byte_perm(X0[w + 4], X0[w + 5], 0x4321);
+        }
+        X1[3] = __byte_perm(X0[3], ea, 0x4321);
+        X1[7] = __byte_perm(X0[7], eb, 0x4321);
       }
       auto ld2 = [&](uint32_t off, uint32_t (&v)[8]) {
-        const uint4 u0 = *reinterpret_cast<const uint4*>(oth + off);
-        const uint4 u1 = *reinterpret_cast<const uint4*>(oth + off + 16);
+        const uint4 u0 = *reinterpret_cast<const uint4*>(oth + off + ha);
+        const uint4 u1 = *reinterpret_cast<const uint4*>(oth + off + hb);
         v[0] = u0.x; v[1] = u0.y; v[2] = u0.z; v[3] = u0.w;
         v[4] = u1.x; v[5] = u1.y; v[6] = u1.z; v[7] = u1.w;
       };
       uint32_t Ym[8], Yp[8], Zm[8], Zp[8];
-      ld2(rx + h0 - ystep, Ym);
-      ld2(rx + h0 + ystep, Yp);
-      ld2(rx + h0 - zstep, Zm);
-      ld2(rx + h0 + zstep, Zp);
+      ld2(rx - ystep, Ym);
+      ld2(rx + ystep, Yp);
+      ld2(rx - zstep, Zm);
+      ld2(rx + zstep, Zp);
       S[0] = Sa.x; S[1] = Sa.y; S[2] = Sa.z; S[3] = Sa.w;
       S[4] = Sb.x; S[5] = Sb.y; S[6] = Sb.z; S[7] = Sb.w;
 #pragma unroll
@@ -252,7 +286,7 @@ __device__ __forceinline__ void tile_pass(const IsingTileArgs& a, const TileGeom
       uint32_t F[8];
 #pragma unroll
       for (int g = 0; g < 2; ++g) {
-        const uint32_t gid = gid0 + (uint32_t)g;
+        const uint32_t gid = gid0 + (uint32_t)g * G2;
         uint32_t cand[4] = {0x01010101u, 0x01010101u, 0x01010101u, 0x01010101u};
         if (PROP == VG_PROPOSE_RANDOM) {
           const uint4 b = philox_ks(
@@ -288,8 +322,8 @@ __device__ __forceinline__ void tile_pass(const IsingTileArgs& a, const TileGeom
         anyf |= F[w];
       }
       if (anyf) {
-        *reinterpret_cast<uint4*>(own + ro) = make_uint4(Sn[0], Sn[1], Sn[2], Sn[3]);
-        *reinterpret_cast<uint4*>(own + ro + 16) = make_uint4(Sn[4], Sn[5], Sn[6], Sn[7]);
+        *reinterpret_cast<uint4*>(own + ro + ha) = make_uint4(Sn[0], Sn[1], Sn[2], Sn[3]);
+        *reinterpret_cast<uint4*>(own + ro + hb) = make_uint4(Sn[4], Sn[5], Sn[6], Sn[7]);
       }
       if (MEASURE && inner) {
         unsigned su = 0, sf = 0;
@@ -329,9 +363,9 @@ __device__ __forceinline__ void tile_pass(const IsingTileArgs& a, const TileGeom
         }
         const uint32_t sk = (sw >> (8 * (k & 3))) & 0xFFu;
         const uint32_t nk = (aw >> (8 * (k & 3))) & 0xFFu;
-        s_q[warp][pos] = make_uint2(gid0 + (uint32_t)(k >> 4), (uint32_t)(k & 15) | (sk << 4) | (nk << 5) |
-                                                                    ((uint32_t)inner << 8) |
-                                                                    ((sgrp + (uint32_t)(k >> 4)) << 9));
+        const uint32_t half = (uint32_t)(k >> 4) * G2;  // the pair's second group lies G/2 groups on
+        s_q[warp][pos] = make_uint2(gid0 + half, (uint32_t)(k & 15) | (sk << 4) | (nk << 5) |
+                                                     ((uint32_t)inner << 8) | ((sgrp + half) << 9));
       }
       qn += __popc(lanes);
       if (qn >= 32) drain(32);
@@ -347,7 +381,7 @@ __global__ void __launch_bounds__(kTileThreads, 1) ising_tile_sweep_kernel(const
   extern __shared__ __align__(128) uint8_t s_spin[];  // class-1 box, then class-0 box
   __shared__ unsigned long long s_thr[2 * 13];
   __shared__ uint2 s_q[kTileThreads / 32][kTileQueue];
-  __shared__ __align__(8) uint64_t s_mbar;
+  __shared__ __align__(8) uint64_t s_mbar[2];  // the two staging chunks
   __shared__ int s_ok;
   uint8_t* s1 = s_spin;
   uint8_t* s0 = s_spin + (size_t)(a.TZm + 4) * (a.TY + 4) * a.Hx;
@@ -355,29 +389,44 @@ __global__ void __launch_bounds__(kTileThreads, 1) ising_tile_sweep_kernel(const
   for (int i = threadIdx.x; i < 2 * 13; i += blockDim.x) s_thr[i] = tab.thr[i];
   const TileGeom t = tile_of(a);
   if (threadIdx.x == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(&s_mbar)) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(&s_mbar[0])) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(&s_mbar[1])) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   __syncthreads();
   pdl_wait();  // the previous sweep's writes (and its reads of our output buffer) are complete
-  stage_boxes(a, t, s1, s0, &s_mbar);
-  const bool staged = wait_staged(&s_mbar);
+  stage_boxes(a, t, s1, s0, s_mbar);
+  // the first chunk, then (inside the colour-0 pass, before its second round
+  // of items) the second; thread 0 checks both with a bound before the pass
+  // results are used
+  bool staged = wait_staged(&s_mbar[0]);
   if (threadIdx.x == 0) s_ok = staged ? 1 : 0;
   __syncthreads();
   if (!s_ok) {  // a staging wait ran out (never expected): report it, write nothing, and give the
                 // copies still in flight a second bounded wait before the block's shared memory goes
     if (threadIdx.x == 0) {
       atomicExch(a.err, 1);
-      wait_staged(&s_mbar);
+      wait_staged(&s_mbar[0]);
+      wait_staged(&s_mbar[1]);
     }
     return;
   }
   int bond = 0, ups = 0, nacc = 0;
-  tile_pass<0, MEASURE, PROP>(a, t, -1, 1, a.fny0, s0, s1, tab, key, s_thr, s_q, bond, ups, nacc);
+  tile_pass<0, MEASURE, PROP>(a, t, -1, 1, a.fny0, s0, s1, tab, key, s_thr, s_q, s_mbar, bond, ups, nacc);
+  staged = wait_staged(&s_mbar[1]);  // already complete unless the pass had a single round
+  if (threadIdx.x == 0) s_ok = staged ? 1 : 0;
+  __syncthreads();
+  if (!s_ok) {
+    if (threadIdx.x == 0) {
+      atomicExch(a.err, 1);
+      wait_staged(&s_mbar[1]);
+    }
+    return;
+  }
   asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // class 0 for the bulk store
   __syncthreads();
   store_tile(a, t, 0, s0);  // class 0 is final: its store overlaps the class-1 pass
-  tile_pass<1, MEASURE, PROP>(a, t, 0, 0, a.fny, s1, s0, tab, key, s_thr, s_q, bond, ups, nacc);
+  tile_pass<1, MEASURE, PROP>(a, t, 0, 0, a.fny, s1, s0, tab, key, s_thr, s_q, s_mbar, bond, ups, nacc);
   asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
   __syncthreads();
   store_tile(a, t, 1, s1);
