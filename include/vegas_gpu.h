@@ -66,7 +66,7 @@ enum vg_proposal { VG_PROPOSE_FLIP = 0, VG_PROPOSE_RANDOM = 1 };
  * x a multiple of 64, even y and z >= 4) runs each sweep as one launch:
  * both colour passes on shared-memory tiles with halos, reading the class
  * arrays and writing a second pair, so the context holds twice the spins;
- * AUTO takes it for lattices of at least 64 x-rows (y x z) per SM.  Results
+ * AUTO does not choose it (the two-pass kernels measured faster).  Results
  * are identical across paths. */
 enum vg_path { VG_PATH_AUTO = 0, VG_PATH_GENERIC = 1, VG_PATH_STRUCTURED = 2, VG_PATH_RESIDENT = 3, VG_PATH_TILED = 4 };
 enum vg_precision { VG_FP32 = 0, VG_FP64 = 1 };

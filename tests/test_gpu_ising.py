@@ -339,9 +339,9 @@ def test_tiled_sweeps_bit_exact(V, O, ext, proposal, n):
 def test_tiled_path_selection(V):
     H = V.hamiltonian(V.Exchange(1.0))
     with _engine(V, "sc", (256, 128, 128), (1, 1, 1), H, 1) as eng:
-        assert eng.info().path == V.PATH_TILED  # AUTO: at least 64 rows per SM
-    with _engine(V, "sc", (64, 16, 16), (1, 1, 1), H, 1) as eng:
-        assert eng.info().path != V.PATH_TILED
+        assert eng.info().path == V.PATH_STRUCTURED  # AUTO keeps the two-pass kernels
+    with _engine(V, "sc", (256, 128, 128), (1, 1, 1), H, 1, path=V.PATH_TILED) as eng:
+        assert eng.info().path == V.PATH_TILED
     for ext, pbc in (((64, 8, 6), (1, 1, 0)), ((32, 8, 8), (1, 1, 1)), ((96, 8, 8), (1, 1, 1)),
                      ((64, 2, 8), (1, 1, 1))):
         with pytest.raises(V.VegasGpuError) as e:

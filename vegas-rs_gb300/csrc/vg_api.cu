@@ -392,8 +392,6 @@ __global__ void reduce_rows<long long>(const long long* __restrict__ part, long 
 
 // ------------------------------------------------------------ host helpers
 constexpr int kChunk = 64;  // sweeps per reduction launch
-// PATH_AUTO takes the tiled sweep kernel from this many rows (y x z) per SM
-constexpr long long kTileAutoRowsPerSm = 64;
 
 bool is_ising(const vg_ctx* c) { return c->opt.spin_kind == VG_SPIN_ISING; }
 // the checkerboard class layout (structured grid kernels or the resident kernel)
@@ -1060,10 +1058,12 @@ int vg_ctx_create_ex(const vg_lattice_desc* lat, const vg_hamiltonian_desc* ham,
     return fail(nullptr, VG_ERR_UNSUPPORTED, "the tiled path needs an Ising sc lattice, periodic on every axis, with "
                                              "x a multiple of 64, even y and z of at least 4");
   }
-  const bool tile_auto = tile_ok && (long long)lat->ny * lat->nz >= kTileAutoRowsPerSm * (long long)c->sm_count;
+  // AUTO does not take it: on the GB300 it ran slower than the two-pass
+  // kernels at every size measured (sc 128^3 - 512^3; 256^3: 727-739
+  // against 792 flips/ns)
   if (opt->path == VG_PATH_GENERIC || !(sc_ok || sub_ok)) c->path = VG_PATH_GENERIC;
   else if (opt->path == VG_PATH_RESIDENT || (opt->path == VG_PATH_AUTO && res_ok && g.n <= 8192)) c->path = VG_PATH_RESIDENT;
-  else if (opt->path == VG_PATH_TILED || (opt->path == VG_PATH_AUTO && tile_auto)) c->path = VG_PATH_TILED;
+  else if (opt->path == VG_PATH_TILED) c->path = VG_PATH_TILED;
   else c->path = VG_PATH_STRUCTURED;
   if (c->path == VG_PATH_TILED) {
     plan.Hx = lat->nx / 2;
