@@ -75,6 +75,7 @@ def lib():
         L = C.CDLL(LIB_PATH)
         P = C.POINTER
         L.vo_philox4x32_10.argtypes = [P(C.c_uint32), P(C.c_uint32), P(C.c_uint32)]
+        L.vo_philox4x32_r.argtypes = [P(C.c_uint32), P(C.c_uint32), C.c_int, P(C.c_uint32)]
         L.vo_num_sites.argtypes = [P(Lattice)]
         L.vo_num_sites.restype = C.c_int64
         L.vo_coordination.argtypes = [C.c_int32]
@@ -141,12 +142,18 @@ def _p(a, ct):
     return a.ctypes.data_as(C.POINTER(ct))
 
 
-def philox(ctr, key):
+def philox(ctr, key, rounds=10):
     c = (C.c_uint32 * 4)(*ctr)
     k = (C.c_uint32 * 2)(*key)
     o = (C.c_uint32 * 4)()
-    lib().vo_philox4x32_10(c, k, o)
+    if rounds == 10:
+        lib().vo_philox4x32_10(c, k, o)
+    else:
+        lib().vo_philox4x32_r(c, k, rounds, o)
     return list(o)
+
+
+MSC_ROUNDS = 7  # Philox rounds of the batched threshold planes
 
 
 def lattice(cell="sc", nx=4, ny=4, nz=4, pbc=(True, True, True)) -> Lattice:

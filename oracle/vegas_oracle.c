@@ -21,9 +21,15 @@
 /* Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), as published with the
  * Random123 library: 10 rounds of two 32x32->64 multiplies, Weyl key bumps. */
 void vo_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+  vo_philox4x32_r(ctr, key, 10, out);
+}
+
+/* Philox4x32 with `rounds` rounds (the first rounds of the 10-round
+ * function: same multipliers and Weyl key increments). */
+void vo_philox4x32_r(const uint32_t ctr[4], const uint32_t key[2], int rounds, uint32_t out[4]) {
   uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
   uint32_t k0 = key[0], k1 = key[1];
-  for (int r = 0; r < 10; ++r) {
+  for (int r = 0; r < rounds; ++r) {
     if (r) {
       k0 += 0x9E3779B9u;
       k1 += 0xBB67AE85u;
@@ -912,7 +918,7 @@ void vo_msc_init(vo_msc_group* g, uint64_t seed) {
 
 /* Decision of "U < th" for lane `lane` of the 32-replica word `word` at class
  * entry j: U's bit 31-p is bit `lane` of plane p, plane p is word p & 3 of
- * the Philox block p >> 2 (drawn once per word and kept in blk / have, so
+ * the Philox4x32-7 block p >> 2 (drawn once per word and kept in blk / have, so
  * the 32 lanes of a word share their blocks).  Planes are compared most
  * significant first, and only until they differ, which gives exactly
  * U < th. */
@@ -921,8 +927,10 @@ static int msc_accept(uint64_t seed, uint32_t word, uint32_t sweep, int colour, 
   for (int p = 0; p < 32; ++p) {
     const int b = p >> 2;
     if (!have[b]) {
-      draw(seed, (uint32_t)j, sweep, ((uint32_t)VO_TAG_MSC << 24) | ((uint32_t)colour << 8) | (uint32_t)b, word,
-           blk[b]);
+      const uint32_t ctr[4] = {(uint32_t)j, sweep, ((uint32_t)VO_TAG_MSC << 24) | ((uint32_t)colour << 8) | (uint32_t)b,
+                               word};
+      const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+      vo_philox4x32_r(ctr, key, VO_MSC_ROUNDS, blk[b]);
       have[b] = 1;
     }
     const uint32_t ub = (blk[b][p & 3] >> lane) & 1u;

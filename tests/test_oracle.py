@@ -195,8 +195,8 @@ def test_msc_oracle_matches_plane_by_plane_definition(O):
     """The batched oracle draws each 32-replica word's threshold planes once
     and compares them most significant first; a direct restatement of the
     draw definition (replica lane l's uniform U has bit 31-p equal to bit l of
-    plane p = word p & 3 of Philox(entry, sweep, 6 << 24 | colour << 8 | p >> 2,
-    word)) gives the same spins after two sweeps."""
+    plane p = word p & 3 of Philox4x32-7(entry, sweep, 6 << 24 | colour << 8 |
+    p >> 2, word)) gives the same spins after two sweeps."""
     seed, J = 77, 1.0
     lat = O.lattice("sc", 8, 6, 1, (1, 1, 0))
     temps = np.geomspace(1.5, 3.0, 32)
@@ -224,8 +224,8 @@ def test_msc_oracle_matches_plane_by_plane_definition(O):
                         acc = True
                     else:
                         if not planes:
-                            planes = sum((O.philox([int(rank[i]), sweep, (6 << 24) | (c << 8) | b, 0], [seed, 0])
-                                          for b in range(8)), [])
+                            planes = sum((O.philox([int(rank[i]), sweep, (6 << 24) | (c << 8) | b, 0], [seed, 0],
+                                                   rounds=O.MSC_ROUNDS) for b in range(8)), [])
                         u = 0
                         for p in range(32):
                             u |= ((planes[p] >> r) & 1) << (31 - p)
@@ -249,3 +249,19 @@ def test_exact_finite_torus_energy_matches_enumeration():
             w = np.exp((bond - bond.max()) / T)
             u = -(bond * w).sum() / w.sum() / (m * n)
             assert abs(X.energy_per_spin(T, m, n) - u) < 1e-10, (m, n, T)
+
+
+def test_philox_round_count(O):
+    """The reduced-round function is the 10-round one cut short: 10 rounds
+    reproduce vo_philox4x32_10, fewer rounds give other words."""
+    ctr, key = [1, 2, 3, 4], [5, 6]
+    assert O.philox(ctr, key, rounds=10) == O.philox(ctr, key)
+    lib = O.lib()
+    import ctypes as C
+
+    c = (C.c_uint32 * 4)(*ctr)
+    k = (C.c_uint32 * 2)(*key)
+    o = (C.c_uint32 * 4)()
+    lib.vo_philox4x32_r(c, k, 10, o)
+    assert list(o) == O.philox(ctr, key)
+    assert O.philox(ctr, key, rounds=7) != O.philox(ctr, key)

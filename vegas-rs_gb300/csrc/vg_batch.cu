@@ -13,7 +13,7 @@
 //   * dE = 2 J (z - 2 n_anti); moves with dE <= 0 always accept;
 //   * the rest compare their 32-bit uniform U with their threshold
 //     thr(T_lane, n_anti) most significant bit first: plane k is a Philox
-//     word whose bit l is bit 31-k of lane l's U; the thresholds are stored
+//     word (Philox4x32-7, kMscRounds) whose bit l is bit 31-k of lane l's U; the thresholds are stored
 //     transposed (bit l of tab[q][k] = bit 31-k of lane l's threshold for the
 //     q-th drawing category).  A lane is decided at its first plane where the
 //     bits differ, so a word usually needs 6-11 planes (2-3 Philox blocks)
@@ -41,6 +41,13 @@ using namespace vg;
 namespace {
 
 constexpr uint32_t kTagMsc = 6, kTagMscInit = 7, kTagExchange = 8;
+// The threshold planes come from Philox4x32-7: Salmon et al. ("Parallel
+// random numbers: as easy as 1, 2, 3", SC'11) report Philox4x32 passing
+// TestU01's Crush batteries from 7 rounds on and take 10 as the default for a
+// safety margin of 3 rounds.  The planes are the batched pass's main cost
+// (two blocks per 32-replica word), so they use the 7-round function; initial
+// states and exchange decisions keep 10 rounds.
+constexpr int kMscRounds = 7;
 constexpr int kTabWords = 4 * 33;  // 4 drawing categories x (32 planes + always-lanes word)
 
 struct MscSeg {          // one replica word of one group
@@ -151,7 +158,8 @@ __device__ __forceinline__ uint32_t msc_plane(const WordState<ND>& w, const uint
 template <int C, int ND>
 __device__ __forceinline__ void msc_block(WordState<ND>& w, uint32_t j, uint32_t sweep, uint32_t word_id,
                                           int blkno, const uint4* s_tab, const KeySchedule& ks) {
-  const uint4 bk = philox_ks(make_uint4(j, sweep, (kTagMsc << 24) | ((uint32_t)C << 8) | (uint32_t)blkno, word_id), ks);
+  const uint4 bk =
+      philox_ks<kMscRounds>(make_uint4(j, sweep, (kTagMsc << 24) | ((uint32_t)C << 8) | (uint32_t)blkno, word_id), ks);
   const uint32_t R[4] = {bk.x, bk.y, bk.z, bk.w};
 #pragma unroll
   for (int i = 0; i < 4; ++i) {

@@ -95,9 +95,12 @@ inline KeySchedule make_key_schedule(uint32_t k0, uint32_t k1) {
   return s;
 }
 
+// ROUNDS < 10: the first ROUNDS rounds of the same schedule (Philox4x32-R).
+template <int ROUNDS = 10>
 __device__ __forceinline__ uint4 philox_ks(uint4 c, const KeySchedule& ks) {
+  static_assert(ROUNDS >= 1 && ROUNDS <= 10, "the key schedule holds 10 rounds");
 #pragma unroll
-  for (int r = 0; r < 10; ++r) {
+  for (int r = 0; r < ROUNDS; ++r) {
     const unsigned long long p0 = (unsigned long long)0xD2511F53u * c.x;
     const unsigned long long p1 = (unsigned long long)0xCD9E8D57u * c.z;
     c = make_uint4((uint32_t)(p1 >> 32) ^ c.y ^ ks.k0[r], (uint32_t)p1, (uint32_t)(p0 >> 32) ^ c.w ^ ks.k1[r],
