@@ -148,3 +148,29 @@ def test_cli_run_matches_reference_cpu_statistically(tmp_path, O):
         a, b = gpu[:, col], cpu[:, k]
         se = np.hypot(a.std(ddof=1), b.std(ddof=1)) / np.sqrt(runs)
         assert abs(a.mean() - b.mean()) < 3 * se, (col, a.mean(), b.mean(), se)
+
+
+def test_gpu_produced_observables_file_reads_back():
+    """A GPU-produced ObservableSensor file (the CLI on a GB300, made by
+    tests/golden/make_cli_observables.py) read with an independent reader:
+    the reference's schema (src/output.rs:37-46), SNAPPY pages, one row per
+    sweep of the schedule, and energy / magnetization columns equal to the
+    per-sweep E and |M| the Python engine produced for the same seed and
+    schedule through the same C ABI."""
+    pq = pytest.importorskip("pyarrow.parquet")
+    import numpy as np
+
+    golden = os.path.join(REPO, "tests", "golden")
+    f = pq.ParquetFile(os.path.join(golden, "cli_observables.parquet"))
+    ref = np.load(os.path.join(golden, "cli_observables_engine.npz"))
+    t = f.read()
+    assert t.schema.names == ["relax", "stage", "step", "n", "temperature", "field", "energy", "magnetization"]
+    assert all(f.metadata.row_group(0).column(k).compression == "SNAPPY" for k in range(8))
+    # Relax 50 at T = 3, then CoolDown(3.0, 2.0, 0.5): 3 x (20 relax + 40 measured)
+    assert t.num_rows == 50 + 3 * 60
+    assert t.column("relax").to_pylist() == [True] * 50 + ([True] * 20 + [False] * 40) * 3
+    assert t.column("stage").to_pylist() == [0] * 50 + sum(([1 + 2 * k] * 20 + [2 + 2 * k] * 40 for k in range(3)), [])
+    assert t.column("temperature").to_pylist() == [3.0] * 50 + [3.0] * 60 + [2.5] * 60 + [2.0] * 60
+    assert t.column("n").to_pylist() == [1024] * t.num_rows
+    np.testing.assert_array_equal(np.array(t.column("energy").to_pylist()), ref["energy"])
+    np.testing.assert_array_equal(np.array(t.column("magnetization").to_pylist()), ref["magnetization"])

@@ -44,9 +44,9 @@ constexpr uint32_t kTagMsc = 6, kTagMscInit = 7, kTagExchange = 8;
 // The threshold planes come from Philox4x32-7: Salmon et al. ("Parallel
 // random numbers: as easy as 1, 2, 3", SC'11) report Philox4x32 passing
 // TestU01's Crush batteries from 7 rounds on and take 10 as the default for a
-// safety margin of 3 rounds.  The planes are the batched pass's main cost
-// (two blocks per 32-replica word), so they use the 7-round function; initial
-// states and exchange decisions keep 10 rounds.
+// safety margin of 3 rounds.  The planes (two blocks per 32-replica word)
+// were about a third of the batched pass's time, so they use the 7-round
+// function; initial states and exchange decisions keep 10 rounds.
 constexpr int kMscRounds = 7;
 constexpr int kTabWords = 4 * 33;  // 4 drawing categories x (32 planes + always-lanes word)
 
