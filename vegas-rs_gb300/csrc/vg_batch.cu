@@ -302,6 +302,21 @@ __global__ void __launch_bounds__(TPB) msc_pass(const MscSeg* __restrict__ segs,
   else msc_pass_body<C, 4, TPB, WPT, WIF>(sg, (uint32_t)bl.y, own, oth, s_tab, sweep, ks, jsign, s_q);
 }
 
+// Transpose of the 32 x 32 bit matrix whose row t is lane t's word: lane l
+// gets the word whose bit t is bit l of lane t's x (five exchange stages,
+// each swapping the off-diagonal blocks of every 2j x 2j block).
+__device__ __forceinline__ uint32_t warp_columns(uint32_t x) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t m[5] = {0x0000FFFFu, 0x00FF00FFu, 0x0F0F0F0Fu, 0x33333333u, 0x55555555u};
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    const int j = 16 >> k;
+    const uint32_t y = __shfl_xor_sync(0xffffffffu, x, j);
+    x = (lane & j) ? ((x & ~m[k]) | ((y & ~m[k]) >> j)) : ((x & m[k]) | ((y & m[k]) << j));
+  }
+  return x;
+}
+
 // Per replica: anti-aligned bonds (over class-1 sites, whose neighbours are
 // all class 0) and up spins, added into obs[slot][replica][2].
 __global__ void __launch_bounds__(256) msc_measure(const MscSeg* __restrict__ segs, const int2* __restrict__ blocks,
@@ -329,17 +344,11 @@ __global__ void __launch_bounds__(256) msc_measure(const MscSeg* __restrict__ se
       u0 = s0 ^ s1;
       u1 = s0 & s1;
     }
-    for (int l = 0; l < 32; ++l) {
-      const unsigned int na = __popc(__ballot_sync(0xffffffffu, (b0 >> l) & 1u)) +
-                              2u * __popc(__ballot_sync(0xffffffffu, (b1 >> l) & 1u)) +
-                              4u * __popc(__ballot_sync(0xffffffffu, (b2 >> l) & 1u));
-      const unsigned int nu = __popc(__ballot_sync(0xffffffffu, (u0 >> l) & 1u)) +
-                              2u * __popc(__ballot_sync(0xffffffffu, (u1 >> l) & 1u));
-      if (lane == l) {
-        ca += na;
-        cu += nu;
-      }
-    }
+    // lane l counts replica l over the warp's 32 words: the columns of the
+    // 32 x 32 bit matrices (rows = the words' bit-sliced digits), then popc
+    ca += (unsigned)__popc(warp_columns(b0)) + 2u * (unsigned)__popc(warp_columns(b1)) +
+          4u * (unsigned)__popc(warp_columns(b2));
+    cu += (unsigned)__popc(warp_columns(u0)) + 2u * (unsigned)__popc(warp_columns(u1));
   }
   atomicAdd(&s_cnt[0][lane], ca);
   atomicAdd(&s_cnt[1][lane], cu);
