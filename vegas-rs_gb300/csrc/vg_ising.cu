@@ -581,16 +581,10 @@ __device__ __forceinline__ void draw1(const RngKey& key, uint32_t g, int k, int 
                   : 0u;
 }
 
-// Two class entries per thread and loop step (j and j + stride): the
-// neighbour-table gathers are two dependent round trips to L2 (table entry,
-// then the neighbour's spin) and the kernel is latency-bound, so the two
-// entries' chains are issued together.  Entries of one class share no bond,
-// so the order of their updates does not matter.
 template <int ZT, bool MEASURE, bool UPDATE, int PROP>
 __global__ void __launch_bounds__(256, 4) ising_gen_kernel(const IsingGenArgs a, const IsingTable tab, const RngKey key,
                                                         const int colour, long long* __restrict__ part) {
   constexpr int W = 2 * ZT + 1;
-  constexpr int U = 2;
   __shared__ unsigned long long s_thr[2 * W];
   const int z = a.z;
   const int Wz = 2 * z + 1;
@@ -601,55 +595,35 @@ __global__ void __launch_bounds__(256, 4) ising_gen_kernel(const IsingGenArgs a,
 
   int bond = 0, ups = 0, nacc = 0;  // per thread: a few entries of at most +-z each
   const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long j0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; j0 < a.n_c; j0 += U * stride) {
-    long long j[U];
-    bool live[U];
-    uint32_t ub0[U], up[U], lm[U];
-    int site[U], s[U], nsum[U], nlow[U];
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      j[u] = j0 + u * stride;
-      live[u] = j[u] < a.n_c;
-      ub0[u] = up[u] = lm[u] = 0u;
-      site[u] = 0;
-      nsum[u] = nlow[u] = 0;
-      if (live[u]) {
-        draw1<UPDATE, PROP>(key, (uint32_t)(j[u] >> 4), (int)(j[u] & 15), colour, ub0[u], up[u]);
-        site[u] = __ldg(a.sites + j[u]);
-        lm[u] = __ldg(a.lowmask + j[u]);
-      }
-    }
-#pragma unroll
-    for (int u = 0; u < U; ++u) s[u] = live[u] ? (int)a.spin[site[u]] : 0;
+  for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < a.n_c; j += stride) {
+    const uint32_t g = (uint32_t)(j >> 4);
+    const int k = (int)(j & 15);
+    uint32_t ub0, up;
+    draw1<UPDATE, PROP>(key, g, k, colour, ub0, up);
+    const int i = __ldg(a.sites + j);
+    const int s = a.spin[i];
+    const uint32_t lm = __ldg(a.lowmask + j);
+    int nsum = 0, nlow = 0;
 #pragma unroll
     for (int q = 0; q < ZT; ++q) {
       if (q < z) {
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-          const int t = live[u] ? __ldg(a.nbr + ((uint32_t)q * (uint32_t)a.n_c + (uint32_t)j[u])) : -1;
-          if (t >= 0) {
-            const int v = 2 * (int)a.spin[t] - 1;
-            nsum[u] += v;
-            if ((lm[u] >> q) & 1u) nlow[u] += v;
-          }
+        const int t = __ldg(a.nbr + ((uint32_t)q * (uint32_t)a.n_c + (uint32_t)j));
+        if (t >= 0) {
+          const int v = 2 * (int)a.spin[t] - 1;
+          nsum += v;
+          if ((lm >> q) & 1u) nlow += v;
         }
       }
     }
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      if (!live[u]) continue;
-      const uint32_t g = (uint32_t)(j[u] >> 4);
-      const int k = (int)(j[u] & 15);
-      bool acc = false;
-      if (UPDATE && (PROP == VG_PROPOSE_FLIP || up[u] != (uint32_t)s[u]))
-        acc = decide1(s_thr[s[u] * Wz + nsum[u] + z], ub0[u], key, g, k, colour);
-      const int sn = s[u] ^ (int)acc;
-      if (acc) a.spin[site[u]] = (uint8_t)sn;
-      if (MEASURE) {
-        ups += sn;
-        bond += sn ? nlow[u] : -nlow[u];
-        nacc += acc;
-      }
+    bool acc = false;
+    if (UPDATE && (PROP == VG_PROPOSE_FLIP || up != (uint32_t)s))
+      acc = decide1(s_thr[s * Wz + nsum + z], ub0, key, g, k, colour);
+    const int sn = s ^ (int)acc;
+    if (acc) a.spin[i] = (uint8_t)sn;
+    if (MEASURE) {
+      ups += sn;
+      bond += sn ? nlow : -nlow;
+      nacc += acc;
     }
   }
   if (MEASURE) block_sum3_store(bond, ups, nacc, part + (size_t)blockIdx.x * kNumSums);
