@@ -82,6 +82,16 @@ __device__ __forceinline__ R heis_delta_e(const V3<R>& s, const V3<R>& p, const 
 
 // Proposal and acceptance draw of one site; returns the new spin and whether
 // it was accepted.
+//
+// The FP32 kernels form the proposal's sine and cosine, its sqrt(1 - z^2)
+// and the acceptance exponential with CUDA's fast intrinsics: __sinf /
+// __cosf of x = pi (t - 1) in [-pi, pi) (sin(pi t) = -sin x, cos(pi t) =
+// -cos x; absolute error below 2^-21.4 there), w rsqrt(w) for sqrt(w)
+// (w >= 2^-23: z = (2k + 1 - 2^24) 2^-24 never reaches +-1), and __expf.
+// The proposal components then lie within 5e-7 of the FP64 kernels' (the
+// FP32 tolerance against the FP64 oracle is 2e-6), and a decision differs
+// only where u lies within a few ulp of exp(-dE / T).  The FP64 kernels
+// use sincospi, sqrt and exp.
 template <typename R, int PROP>
 __device__ __forceinline__ bool heis_update(const V3<R>& s, const V3<R>& h, const HeisParams<R>& P, const uint4& w,
                                             V3<R>& out) {
@@ -90,9 +100,17 @@ __device__ __forceinline__ bool heis_update(const V3<R>& s, const V3<R>& h, cons
     // z = (2k + 1 - 2^24) / 2^24 is exact in FP32; azimuth pi * t, t in [0, 2)
     R z, t;
     draw_zt<R>(w, z, t);
-    R sn, cs;
-    sincospi_(t, &sn, &cs);
-    const R r = sqrt_(((R)1 - z) * ((R)1 + z));
+    R sn, cs, r;
+    if constexpr (sizeof(R) == 4) {
+      const float x = 3.14159265358979f * (t - 1.0f);  // t - 1 is exact
+      sn = -__sinf(x);
+      cs = -__cosf(x);
+      const float w2 = (1.0f - z) * (1.0f + z);
+      r = w2 * rsqrtf(w2);
+    } else {
+      sincospi_(t, &sn, &cs);
+      r = sqrt_(((R)1 - z) * ((R)1 + z));
+    }
     p.x = r * cs;
     p.y = r * sn;
     p.z = z;
@@ -103,7 +121,10 @@ __device__ __forceinline__ bool heis_update(const V3<R>& s, const V3<R>& h, cons
   }
   const R de = heis_delta_e<R>(s, p, h, P);
   const R u = draw_u<R>(w);
-  const bool acc = de <= (R)0 || u < exp_(-de * P.beta);
+  R q;
+  if constexpr (sizeof(R) == 4) q = __expf(-de * P.beta);
+  else q = exp_(-de * P.beta);
+  const bool acc = de <= (R)0 || u < q;
   out = acc ? p : s;
   return acc;
 }
