@@ -298,48 +298,45 @@ __global__ void __launch_bounds__(256, UNIFORM ? 4 : 2) ising_sc_kernel(const Is
 // blocks, same tie resolution), so results are identical.  ALLPER: all axes
 // periodic, no missing rows.
 constexpr int kSc2MinBlocks = 3;  // 80 registers: the pair state stays in registers
-constexpr int kSc2Queue = kScQueue;  // per-warp tie queue
+// Ties of a pass are queued per block and decided after the block's pairs
+// (a 256^3 pass has about 36 per block); entries past the queue's end are
+// decided in line.  A per-warp queue with a ballot loop in every round of
+// pairs cost 40 % of the pass's instructions (timing builds without tie
+// handling ran 44 % faster), as nearly every warp meets a tie in every
+// round.
+constexpr int kSc2BlockQueue = 512;
+
+// S[w] and A[w] byte k & 3 of word w = k >> 2 (bit k of a pair's tie mask),
+// by selects: a dynamic index would put S and A on the stack.
+__device__ __forceinline__ void pair_site(const uint32_t (&S)[8], const uint32_t (&A)[8], int k, uint32_t& s01,
+                                          uint32_t& nu) {
+  const int wi = k >> 2;
+  uint32_t sw = 0, aw = 0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    sw = i == wi ? S[i] : sw;
+    aw = i == wi ? A[i] : aw;
+  }
+  s01 = (sw >> (8 * (k & 3))) & 0xFFu;
+  nu = (aw >> (8 * (k & 3))) & 0xFFu;
+}
 
 // The pairs base + lane for base in [first, end) step `step` (base a
 // multiple of 32 apart from `first`), adding the pass's sums to bond / ups /
-// nacc.  Every tie is resolved before returning.
+// nacc.  Ties go to the block queue s_tq / s_tn (decided by sc2_ties after
+// the block's pairs, every thread of the block taking part).
 template <int C, bool MEASURE, bool UPDATE, int PROP, bool ALLPER>
 __device__ __forceinline__ void sc2_range(const IsingScArgs& a, const FastDiv& fG2, const IsingTable& tab,
-                                          const RngKey& key, const unsigned long long* s_thr,
-                                          uint2 (*s_q)[kSc2Queue], uint32_t first, uint32_t end, uint32_t step,
-                                          int& bond, int& ups, int& nacc) {
+                                          const RngKey& key, const unsigned long long* s_thr, uint2* s_tq, int* s_tn,
+                                          uint32_t first, uint32_t end, uint32_t step, int& bond, int& ups,
+                                          int& nacc) {
   constexpr int Z = 6;
-  constexpr int kQ = kSc2Queue;
   uint8_t* __restrict__ own = a.cls[C];
   const uint8_t* __restrict__ oth = a.cls[C ^ 1];
   const uint32_t zoff = (uint32_t)(Z - tab.zeff) * 0x01010101u;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
   const int G2 = a.G >> 1;
   const uint32_t pairs = end;
-  int qn = 0;  // warp-uniform queue length
-
-  auto drain = [&](int n) {
-    __syncwarp();
-    if (lane < n) {
-      const uint2 e = s_q[warp][lane];
-      const int k = (int)(e.y & 15u);
-      const uint32_t s01 = (e.y >> 4) & 1u, nu = e.y >> 5;
-      if (resolve_tie(e.x, k, s01, nu, tab.zeff, C, s_thr, key)) {
-        own[(size_t)e.x * 16 + k] = (uint8_t)(s01 ^ 1u);
-        ups += 1 - 2 * (int)s01;
-        nacc += 1;
-        if (C == 1) bond -= 2 * (2 * (int)s01 - 1) * (2 * (int)nu - tab.zeff);
-      }
-    }
-    __syncwarp();
-    const int rest = qn - n;
-    uint2 mv = make_uint2(0, 0);
-    if (lane < rest) mv = s_q[warp][n + lane];
-    __syncwarp();
-    if (lane < rest) s_q[warp][lane] = mv;
-    __syncwarp();
-    qn = rest;
-  };
 
   for (uint32_t base = first; base < pairs; base += step) {
     const uint32_t q = base + lane;
@@ -443,6 +440,29 @@ __device__ __forceinline__ void sc2_range(const IsingScArgs& a, const FastDiv& f
             for (int i = 0; i < 4; ++i) tm |= gather4(bytes_zero(R[i] ^ thr[i]) & cand[i]) << (16 * g + 4 * i);
           }
         }
+        if (tm) {  // sites whose first digit tied with their threshold's: to the block queue
+          for (uint32_t m = tm; m; m &= m - 1u) {
+            const int k = __ffs(m) - 1;
+            const int slot = atomicAdd(s_tn, 1);
+            if (slot < kSc2BlockQueue) {
+              uint32_t s01, nu;
+              pair_site(S, A, k, s01, nu);
+              s_tq[slot] = make_uint2(2u * q + (uint32_t)(k >> 4), (uint32_t)(k & 15) | (s01 << 4) | (nu << 5));
+              tm &= ~(1u << k);
+            }
+          }
+          for (uint32_t m = tm; m; m &= m - 1u) {  // no room left in the queue: decided here
+            const int k = __ffs(m) - 1;
+            uint32_t s01, nu;
+            pair_site(S, A, k, s01, nu);
+            if (resolve_tie(2u * q + (uint32_t)(k >> 4), k & 15, s01, nu, tab.zeff, C, s_thr, key)) {
+              const uint32_t bit = 1u << (8 * (k & 3));
+#pragma unroll
+              for (int i = 0; i < 8; ++i)
+                if (i == (k >> 2)) F[i] |= bit;
+            }
+          }
+        }
       }
       uint32_t Sn[8], anyf = 0;
 #pragma unroll
@@ -479,32 +499,29 @@ __device__ __forceinline__ void sc2_range(const IsingScArgs& a, const FastDiv& f
         }
       }
     }
-    if (UPDATE) {
-      unsigned lanes = __ballot_sync(0xffffffffu, tm != 0u);
-      while (lanes) {
-        if (qn + 32 > kQ) drain(32 < qn ? 32 : qn);
-        const int pos = qn + __popc(lanes & ((1u << lane) - 1u));
-        if (tm) {
-          const int k = __ffs(tm) - 1;
-          tm &= tm - 1u;
-          const int wi = k >> 2;
-          uint32_t sw = 0, aw = 0;  // S[wi], A[wi] by selects: a dynamic index would put S, A on the stack
-#pragma unroll
-          for (int i = 0; i < 8; ++i) {
-            sw = i == wi ? S[i] : sw;
-            aw = i == wi ? A[i] : aw;
-          }
-          const uint32_t sk = (sw >> (8 * (k & 3))) & 0xFFu;
-          const uint32_t nk = (aw >> (8 * (k & 3))) & 0xFFu;
-          s_q[warp][pos] = make_uint2(2u * q + (uint32_t)(k >> 4), (uint32_t)(k & 15) | (sk << 4) | (nk << 5));
-        }
-        qn += __popc(lanes);
-        if (qn >= 32) drain(32);
-        lanes = __ballot_sync(0xffffffffu, tm != 0u);
+  }
+}
+
+// The block's queued ties (sc2_range), one per thread, after every pair of
+// the block has been stored: the flips and their changes to the sums.
+template <int C, bool MEASURE>
+__device__ __forceinline__ void sc2_ties(const IsingScArgs& a, const IsingTable& tab, const RngKey& key,
+                                         const unsigned long long* s_thr, const uint2* s_tq, int n, int& bond,
+                                         int& ups, int& nacc) {
+  uint8_t* __restrict__ own = a.cls[C];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const uint2 e = s_tq[i];
+    const int k = (int)(e.y & 15u);
+    const uint32_t s01 = (e.y >> 4) & 1u, nu = e.y >> 5;
+    if (resolve_tie(e.x, k, s01, nu, tab.zeff, C, s_thr, key)) {
+      own[(size_t)e.x * 16 + k] = (uint8_t)(s01 ^ 1u);
+      if (MEASURE) {
+        ups += 1 - 2 * (int)s01;
+        nacc += 1;
+        if (C == 1) bond -= 2 * (2 * (int)s01 - 1) * (2 * (int)nu - tab.zeff);
       }
     }
   }
-  if (UPDATE && qn > 0) drain(qn);
 }
 
 template <int C, bool MEASURE, bool UPDATE, int PROP, bool ALLPER>
@@ -513,8 +530,11 @@ __global__ void __launch_bounds__(256, kSc2MinBlocks) ising_sc2_kernel(const Isi
                                                                        long long* __restrict__ part) {
   constexpr int W = 13;
   __shared__ unsigned long long s_thr[2 * W];
-  __shared__ uint2 s_q[8][kSc2Queue];
+  __shared__ uint2 s_q[8][kScQueue];         // one group per thread: per-warp tie queues
+  __shared__ uint2 s_tq[kSc2BlockQueue];     // pairs: the block's tie queue
+  __shared__ int s_tn;
   pdl_launch_dependents();
+  if (threadIdx.x == 0) s_tn = 0;
   for (int i = threadIdx.x; i < 2 * W; i += blockDim.x) s_thr[i] = tab.thr[i];
   __syncthreads();
   pdl_wait();
@@ -527,11 +547,16 @@ __global__ void __launch_bounds__(256, kSc2MinBlocks) ising_sc2_kernel(const Isi
   // more pair round on issue slots the others have freed.
   const uint32_t T = gridDim.x * blockDim.x;
   const uint32_t first = blockIdx.x * blockDim.x + (threadIdx.x & ~31u);
-  if (a.groups <= T)
+  if (a.groups <= T) {
     sc1_range<C, true, MEASURE, UPDATE, PROP>(a, tab, key, s_thr, s_q, first, a.groups, T, bond, ups, nacc);
-  else
-    sc2_range<C, MEASURE, UPDATE, PROP, ALLPER>(a, fG2, tab, key, s_thr, s_q, first, a.groups >> 1, T, bond, ups,
-                                                nacc);
+  } else {
+    sc2_range<C, MEASURE, UPDATE, PROP, ALLPER>(a, fG2, tab, key, s_thr, s_tq, &s_tn, first, a.groups >> 1, T,
+                                                bond, ups, nacc);
+    if (UPDATE) {
+      __syncthreads();  // every pair of the block is stored
+      sc2_ties<C, MEASURE>(a, tab, key, s_thr, s_tq, min(s_tn, kSc2BlockQueue), bond, ups, nacc);
+    }
+  }
   if (MEASURE) block_sum3_store(bond, ups, nacc, part + (size_t)blockIdx.x * kNumSums);
 }
 
