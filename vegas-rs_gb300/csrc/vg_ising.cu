@@ -298,12 +298,16 @@ __global__ void __launch_bounds__(256, UNIFORM ? 4 : 2) ising_sc_kernel(const Is
 // blocks, same tie resolution), so results are identical.  ALLPER: all axes
 // periodic, no missing rows.
 constexpr int kSc2MinBlocks = 3;  // 80 registers: the pair state stays in registers
-// Ties of a pass are queued per block and decided after the block's pairs
-// (a 256^3 pass has about 36 per block); entries past the queue's end are
-// decided in line.  A per-warp queue with a ballot loop in every round of
-// pairs cost 40 % of the pass's instructions (timing builds without tie
-// handling ran 44 % faster), as nearly every warp meets a tie in every
-// round.
+// Ties on the first digit (1/256 of the candidate sites, so that a warp
+// meets one in most rounds of pairs) are queued per block and decided after
+// the block's pairs; entries past the queue's end are decided in line.
+// Timing builds put tie handling at about 30 % of the pass at 256^3 (one
+// that ignored ties ran 1,128 flips/ns against 790), and the work in the
+// pair loop, which runs in most rounds whatever the queue, dominates it:
+// a per-warp queue, this block queue, deferring whole groups to the end of
+// the block and a per-warp ring of tied groups drained 32 at a time all ran
+// between 756 and 802 flips/ns.  The kernel is latency-bound (43 % of issue
+// slots used), so serial work on a tie lengthens its warp's path.
 constexpr int kSc2BlockQueue = 512;
 
 // S[w] and A[w] byte k & 3 of word w = k >> 2 (bit k of a pair's tie mask),
