@@ -18,9 +18,10 @@
 //     q-th drawing category).  A lane is decided at its first plane where the
 //     bits differ, so a word usually needs 6-11 planes (2-3 Philox blocks)
 //     for its 32 flips, and the outcome is exactly "U < thr".
-// Every `sweeps_per_round` sweeps a measurement kernel counts anti-aligned
-// bonds and up spins per replica (warp ballots over bit-sliced counts) and an
-// exchange kernel swaps the temperatures of adjacent ladder entries with
+// The last colour-1 pass of every `sweeps_per_round` sweeps also counts
+// anti-aligned bonds and up spins per replica of the new state (bit-sliced
+// counters over the words a thread settles, turned into per-replica counts by
+// warp transposes once at the end), and an exchange kernel swaps the temperatures of adjacent ladder entries with
 // probability min(1, exp((b_i - b_j)(E_i - E_j))), then re-transposes the
 // threshold tables.  A round (passes, measurement, exchange, counter advance)
 // is captured once into a CUDA graph and replayed.
@@ -140,7 +141,54 @@ struct WordState {
   uint32_t m[ND];   // lanes in each drawing category
   uint32_t und;     // lanes still undecided
   uint32_t acc;     // lanes accepted so far
+  uint32_t b0, b1, b2, s0;  // for a measuring pass: anti-aligned count before the update, class-0 word at j
 };
+
+// Per-replica sums of a measuring pass, bit-sliced (bit l of c[k] is bit k of
+// lane l's count).  A lane settles at most its own WPT <= 8 words and one
+// queued word per drain (at most WPT + 1 drains): <= 17 words, so bonds
+// <= 102 < 2^7 and up spins <= 34 < 2^6.
+struct MscTally {
+  uint32_t bond[7];
+  uint32_t up[6];
+};
+
+// c += (x2 x1 x0), lane-wise
+template <int NP>
+__device__ __forceinline__ void slice_add(uint32_t (&c)[NP], uint32_t x0, uint32_t x1, uint32_t x2) {
+  uint32_t k = c[0] & x0;
+  c[0] ^= x0;
+  uint32_t t = c[1];
+  c[1] = t ^ x1 ^ k;
+  k = (t & x1) | (t & k) | (x1 & k);
+  t = c[2];
+  c[2] = t ^ x2 ^ k;
+  k = (t & x2) | (t & k) | (x2 & k);
+#pragma unroll
+  for (int i = 3; i < NP; ++i) {
+    t = c[i];
+    c[i] = t ^ k;
+    k &= t;
+  }
+}
+
+// A settled word into the tally: the lanes in acc flipped, so their
+// anti-aligned count n (of ZZ bonds) became ZZ - n (n and ZZ - n have the
+// same parity: b0 stays).
+template <int ZZ, int ND>
+__device__ __forceinline__ void msc_tally(MscTally& t, const WordState<ND>& w, uint32_t s) {
+  uint32_t r1, r2;
+  if (ZZ == 6) {
+    r1 = ~(w.b1 ^ w.b0);
+    r2 = ~(w.b2 | (w.b1 & w.b0));
+  } else {
+    r1 = w.b1 ^ w.b0;
+    r2 = ~(w.b2 | w.b1 | w.b0);
+  }
+  slice_add(t.bond, w.b0, (w.acc & r1) | (~w.acc & w.b1), (w.acc & r2) | (~w.acc & w.b2));
+  const uint32_t s1 = s ^ w.acc;
+  slice_add(t.up, w.s0 ^ s1, w.s0 & s1, 0u);
+}
 
 // Threshold plane k of every drawing category for the lanes in its mask
 // (s_tab: the block's table plane-major, one uint4 of categories per plane).
@@ -183,6 +231,10 @@ __device__ __forceinline__ WordState<ZZ / 2> msc_word_start(const MscSeg& sg, ui
   uint32_t b0, b1, b2;
   if (ZZ == 6) count6(a[0], a[1], a[2], a[3], a[4], a[5], b0, b1, b2);
   else count4(a[0], a[1], a[2], a[3], b0, b1, b2);
+  w.b0 = b0;
+  w.b1 = b1;
+  w.b2 = b2;
+  w.s0 = a[0] ^ s;  // the other class's word at the same index
   uint32_t draw = 0;
 #pragma unroll
   for (int q = 0; q < ND; ++q) {
@@ -196,110 +248,6 @@ __device__ __forceinline__ WordState<ZZ / 2> msc_word_start(const MscSeg& sg, ui
   msc_block<C, ND>(w, j, sweep, sg.word_id, 0, s_tab, ks);
   msc_block<C, ND>(w, j, sweep, sg.word_id, 1, s_tab, ks);
   return w;
-}
-
-// Launch shape of a pass (chosen by the autotuner, vg_batch_autotune): a
-// block of TPB threads covers TPB x WPT consecutive words of one segment;
-// each thread takes its WPT words WIF at a time (WIF = 2 interleaves two
-// independent words' Philox chains and loads).  Every shape makes the same
-// decisions for every word.
-//
-// Words still undecided after 8 planes are queued per warp and finished 32
-// at a time, so the rare long comparisons run with full warps.
-constexpr int kQueue = 64;          // per-warp queue entries
-constexpr int kQueueWords = 4 + 3;  // j, s, und, acc, m[<= 3]
-
-template <int C, int ZZ, int TPB, int WPT, int WIF>
-__device__ __forceinline__ void msc_pass_body(const MscSeg& sg, uint32_t j0, uint32_t* own, const uint32_t* oth,
-                                              const uint4* s_tab, uint32_t sweep, const KeySchedule& ks,
-                                              int jsign, uint32_t (*s_q)[kQueue][kQueueWords]) {
-  constexpr int ND = ZZ / 2;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  int qn = 0;
-  auto finish = [&](int n) {  // complete the first n queued words, one per lane
-    __syncwarp();
-    if (lane < n) {
-      const uint32_t* e = s_q[warp][lane];
-      WordState<ND> w;
-      const uint32_t j = e[0], s = e[1];
-      w.und = e[2];
-      w.acc = e[3];
-#pragma unroll
-      for (int q = 0; q < ND; ++q) w.m[q] = e[4 + q];
-#pragma unroll 1
-      for (int blkno = 2; w.und != 0u && blkno < 8; ++blkno) msc_block<C, ND>(w, j, sweep, sg.word_id, blkno, s_tab, ks);
-      if (w.acc) own[j] = s ^ w.acc;
-    }
-    __syncwarp();
-    const int rest = qn - n;
-    uint32_t tmp[ND + 4];
-    if (lane < rest)
-#pragma unroll
-      for (int i = 0; i < ND + 4; ++i) tmp[i] = s_q[warp][n + lane][i];
-    __syncwarp();
-    if (lane < rest)
-#pragma unroll
-      for (int i = 0; i < ND + 4; ++i) s_q[warp][lane][i] = tmp[i];
-    __syncwarp();
-    qn = rest;
-  };
-#pragma unroll 1
-  for (int u = 0; u < WPT; u += WIF) {
-    uint32_t j[WIF], s[WIF];
-    bool live[WIF], pend[WIF];
-    WordState<ND> w[WIF];
-#pragma unroll
-    for (int i = 0; i < WIF; ++i) {
-      j[i] = j0 + (uint32_t)((u + i) * TPB) + threadIdx.x;
-      live[i] = j[i] < sg.n_c;
-      const uint32_t jj = live[i] ? j[i] : 0u;  // dead lanes work on a valid word and discard it
-      s[i] = own[jj];
-      w[i] = msc_word_start<C, ZZ>(sg, jj, s[i], oth, s_tab, sweep, ks, jsign);
-      pend[i] = live[i] && w[i].und != 0u;
-      if (live[i] && !pend[i] && w[i].acc) own[j[i]] = s[i] ^ w[i].acc;
-    }
-#pragma unroll
-    for (int i = 0; i < WIF; ++i) {
-      const unsigned pmask = __ballot_sync(0xffffffffu, pend[i]);
-      if (pmask) {
-        if (pend[i]) {
-          uint32_t* e = s_q[warp][qn + __popc(pmask & ((1u << lane) - 1u))];
-          e[0] = j[i];
-          e[1] = s[i];
-          e[2] = w[i].und;
-          e[3] = w[i].acc;
-#pragma unroll
-          for (int q = 0; q < ND; ++q) e[4 + q] = w[i].m[q];
-        }
-        qn += __popc(pmask);
-        if (qn >= 32) finish(32);
-      }
-    }
-  }
-  if (qn > 0) finish(qn);
-}
-
-template <int C, int TPB, int WPT, int WIF>
-__global__ void __launch_bounds__(TPB) msc_pass(const MscSeg* __restrict__ segs, const int2* __restrict__ blocks,
-                                                const uint32_t* __restrict__ tabs, const MscDev* __restrict__ dev,
-                                                uint32_t t_off, KeySchedule ks, int jsign) {
-  __shared__ uint4 s_tab[33];  // plane k: the 4 categories' threshold words
-  __shared__ uint32_t s_q[TPB / 32][kQueue][kQueueWords];
-  pdl_launch_dependents();
-  const int2 bl = blocks[blockIdx.x];
-  const MscSeg sg = segs[bl.x];
-  // Tables and counters change only in the exchange / advance kernels, which
-  // complete before any pass of the next round starts; spins are read after
-  // the wait for the previous pass.
-  for (int i = threadIdx.x; i < kTabWords; i += blockDim.x)  // category-major in memory, plane-major here
-    reinterpret_cast<uint32_t*>(s_tab)[(i % 33) * 4 + i / 33] = tabs[(size_t)bl.x * kTabWords + i];
-  const uint32_t sweep = dev->sweep0 + t_off;
-  __syncthreads();
-  pdl_wait();
-  uint32_t* own = sg.cls[C];
-  const uint32_t* oth = sg.cls[C ^ 1];
-  if (sg.dim3) msc_pass_body<C, 6, TPB, WPT, WIF>(sg, (uint32_t)bl.y, own, oth, s_tab, sweep, ks, jsign, s_q);
-  else msc_pass_body<C, 4, TPB, WPT, WIF>(sg, (uint32_t)bl.y, own, oth, s_tab, sweep, ks, jsign, s_q);
 }
 
 // Transpose of the 32 x 32 bit matrix whose row t is lane t's word: lane l
@@ -317,47 +265,165 @@ __device__ __forceinline__ uint32_t warp_columns(uint32_t x) {
   return x;
 }
 
-// Per replica: anti-aligned bonds (over class-1 sites, whose neighbours are
-// all class 0) and up spins, added into obs[slot][replica][2].
-__global__ void __launch_bounds__(256) msc_measure(const MscSeg* __restrict__ segs, const int2* __restrict__ blocks,
-                                                   int words_per_block, const MscDev* __restrict__ dev,
-                                                   int total_rep, unsigned long long* __restrict__ obs) {
+// Launch shape of a pass (chosen by the autotuner, vg_batch_autotune): a
+// block of TPB threads covers TPB x WPT consecutive words of one segment;
+// each thread takes its WPT words WIF at a time (WIF = 2 interleaves two
+// independent words' Philox chains and loads).  Every shape makes the same
+// decisions for every word.
+//
+// Words still undecided after 8 planes are queued per warp and finished 32
+// at a time, so the rare long comparisons run with full warps.  MEAS: the
+// measuring pass (C = 1), which tallies every settled word and returns lane
+// l's counts for replica l in ca (anti-aligned bonds) and cu (up spins).
+constexpr int kQueue = 64;  // per-warp queue entries
+template <bool MEAS>
+__host__ __device__ constexpr int queue_words() {
+  return 4 + 3 + (MEAS ? 4 : 0);  // j, s, und, acc, m[<= 3] (+ b0, b1, b2, s0)
+}
+
+template <int C, int ZZ, int TPB, int WPT, int WIF, bool MEAS>
+__device__ __forceinline__ void msc_pass_body(const MscSeg& sg, uint32_t j0, uint32_t* own, const uint32_t* oth,
+                                              const uint4* s_tab, uint32_t sweep, const KeySchedule& ks,
+                                              int jsign, uint32_t (*s_q)[kQueue][queue_words<MEAS>()],
+                                              unsigned& ca, unsigned& cu) {
+  constexpr int ND = ZZ / 2, QW = queue_words<MEAS>();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int qn = 0;
+  MscTally tal;
+  if (MEAS) {
+#pragma unroll
+    for (int i = 0; i < 7; ++i) tal.bond[i] = 0u;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) tal.up[i] = 0u;
+  }
+  auto finish = [&](int n) {  // complete the first n queued words, one per lane
+    __syncwarp();
+    if (lane < n) {
+      const uint32_t* e = s_q[warp][lane];
+      WordState<ND> w;
+      const uint32_t j = e[0], s = e[1];
+      w.und = e[2];
+      w.acc = e[3];
+#pragma unroll
+      for (int q = 0; q < ND; ++q) w.m[q] = e[4 + q];
+      if (MEAS) {
+        w.b0 = e[7];
+        w.b1 = e[8];
+        w.b2 = e[9];
+        w.s0 = e[10];
+      }
+#pragma unroll 1
+      for (int blkno = 2; w.und != 0u && blkno < 8; ++blkno) msc_block<C, ND>(w, j, sweep, sg.word_id, blkno, s_tab, ks);
+      if (w.acc) own[j] = s ^ w.acc;
+      if (MEAS) msc_tally<ZZ>(tal, w, s);
+    }
+    __syncwarp();
+    const int rest = qn - n;
+    uint32_t tmp[QW];
+    if (lane < rest)
+#pragma unroll
+      for (int i = 0; i < QW; ++i) tmp[i] = s_q[warp][n + lane][i];
+    __syncwarp();
+    if (lane < rest)
+#pragma unroll
+      for (int i = 0; i < QW; ++i) s_q[warp][lane][i] = tmp[i];
+    __syncwarp();
+    qn = rest;
+  };
+#pragma unroll 1
+  for (int u = 0; u < WPT; u += WIF) {
+    uint32_t j[WIF], s[WIF];
+    bool live[WIF], pend[WIF];
+    WordState<ND> w[WIF];
+#pragma unroll
+    for (int i = 0; i < WIF; ++i) {
+      j[i] = j0 + (uint32_t)((u + i) * TPB) + threadIdx.x;
+      live[i] = j[i] < sg.n_c;
+      const uint32_t jj = live[i] ? j[i] : 0u;  // dead lanes work on a valid word and discard it
+      s[i] = own[jj];
+      w[i] = msc_word_start<C, ZZ>(sg, jj, s[i], oth, s_tab, sweep, ks, jsign);
+      pend[i] = live[i] && w[i].und != 0u;
+      if (live[i] && !pend[i] && w[i].acc) own[j[i]] = s[i] ^ w[i].acc;
+      if (MEAS && live[i] && !pend[i]) msc_tally<ZZ>(tal, w[i], s[i]);
+    }
+#pragma unroll
+    for (int i = 0; i < WIF; ++i) {
+      const unsigned pmask = __ballot_sync(0xffffffffu, pend[i]);
+      if (pmask) {
+        if (pend[i]) {
+          uint32_t* e = s_q[warp][qn + __popc(pmask & ((1u << lane) - 1u))];
+          e[0] = j[i];
+          e[1] = s[i];
+          e[2] = w[i].und;
+          e[3] = w[i].acc;
+#pragma unroll
+          for (int q = 0; q < ND; ++q) e[4 + q] = w[i].m[q];
+          if (MEAS) {
+            e[7] = w[i].b0;
+            e[8] = w[i].b1;
+            e[9] = w[i].b2;
+            e[10] = w[i].s0;
+          }
+        }
+        qn += __popc(pmask);
+        if (qn >= 32) finish(32);
+      }
+    }
+  }
+  if (qn > 0) finish(qn);
+  if (MEAS) {  // lane l: replica l's sums over the warp's words
+#pragma unroll
+    for (int k = 0; k < 7; ++k) ca += (unsigned)__popc(warp_columns(tal.bond[k])) << k;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) cu += (unsigned)__popc(warp_columns(tal.up[k])) << k;
+  }
+}
+
+// MEAS (the last colour-1 pass of a round): also add the new state's
+// anti-aligned bonds (over class-1 sites, whose neighbours are all class 0)
+// and up spins per replica into obs[slot][replica][2].
+template <int C, int TPB, int WPT, int WIF, bool MEAS>
+__global__ void __launch_bounds__(TPB) msc_pass(const MscSeg* __restrict__ segs, const int2* __restrict__ blocks,
+                                                const uint32_t* __restrict__ tabs, const MscDev* __restrict__ dev,
+                                                uint32_t t_off, KeySchedule ks, int jsign, int total_rep,
+                                                unsigned long long* __restrict__ obs) {
+  static_assert(!MEAS || C == 1, "the measuring pass is the colour-1 pass");
+  __shared__ uint4 s_tab[33];  // plane k: the 4 categories' threshold words
+  __shared__ uint32_t s_q[TPB / 32][kQueue][queue_words<MEAS>()];
   __shared__ unsigned int s_cnt[2][32];
+  pdl_launch_dependents();
   const int2 bl = blocks[blockIdx.x];
-  const MscSeg& sg = segs[bl.x];
-  if (threadIdx.x < 32) {
+  const MscSeg sg = segs[bl.x];
+  if (MEAS && threadIdx.x < 32) {
     s_cnt[0][threadIdx.x] = 0;
     s_cnt[1][threadIdx.x] = 0;
   }
+  // Tables and counters change only in the exchange / advance kernels, which
+  // complete before any pass of the next round starts; spins are read after
+  // the wait for the previous pass.
+  for (int i = threadIdx.x; i < kTabWords; i += blockDim.x)  // category-major in memory, plane-major here
+    reinterpret_cast<uint32_t*>(s_tab)[(i % 33) * 4 + i / 33] = tabs[(size_t)bl.x * kTabWords + i];
+  const uint32_t sweep = dev->sweep0 + t_off;
   __syncthreads();
-  const int lane = threadIdx.x & 31;
-  unsigned int ca = 0, cu = 0;
-  for (int w = 0; w * 256 < words_per_block; ++w) {
-    const uint32_t j = (uint32_t)bl.y + (uint32_t)(w * 256) + threadIdx.x;
-    uint32_t b0 = 0, b1 = 0, b2 = 0, u0 = 0, u1 = 0;
-    if (j < sg.n_c && w * 256 + (int)threadIdx.x < words_per_block) {
-      const uint32_t s1 = sg.cls[1][j], s0 = sg.cls[0][j];
-      uint32_t a[6];
-      msc_anti(sg, 1, j, s1, sg.cls[0], a);
-      if (sg.dim3) count6(a[0], a[1], a[2], a[3], a[4], a[5], b0, b1, b2);
-      else count4(a[0], a[1], a[2], a[3], b0, b1, b2);
-      u0 = s0 ^ s1;
-      u1 = s0 & s1;
+  pdl_wait();
+  uint32_t* own = sg.cls[C];
+  const uint32_t* oth = sg.cls[C ^ 1];
+  unsigned ca = 0, cu = 0;
+  if (sg.dim3)
+    msc_pass_body<C, 6, TPB, WPT, WIF, MEAS>(sg, (uint32_t)bl.y, own, oth, s_tab, sweep, ks, jsign, s_q, ca, cu);
+  else
+    msc_pass_body<C, 4, TPB, WPT, WIF, MEAS>(sg, (uint32_t)bl.y, own, oth, s_tab, sweep, ks, jsign, s_q, ca, cu);
+  if (MEAS) {
+    const int lane = threadIdx.x & 31;
+    atomicAdd(&s_cnt[0][lane], ca);
+    atomicAdd(&s_cnt[1][lane], cu);
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      const uint32_t slot = dev->round - dev->round_base;
+      unsigned long long* o = obs + ((size_t)slot * total_rep + sg.rep0 + threadIdx.x) * 2;
+      atomicAdd(o, (unsigned long long)s_cnt[0][threadIdx.x]);
+      atomicAdd(o + 1, (unsigned long long)s_cnt[1][threadIdx.x]);
     }
-    // lane l counts replica l over the warp's 32 words: the columns of the
-    // 32 x 32 bit matrices (rows = the words' bit-sliced digits), then popc
-    ca += (unsigned)__popc(warp_columns(b0)) + 2u * (unsigned)__popc(warp_columns(b1)) +
-          4u * (unsigned)__popc(warp_columns(b2));
-    cu += (unsigned)__popc(warp_columns(u0)) + 2u * (unsigned)__popc(warp_columns(u1));
-  }
-  atomicAdd(&s_cnt[0][lane], ca);
-  atomicAdd(&s_cnt[1][lane], cu);
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    const uint32_t slot = dev->round - dev->round_base;
-    unsigned long long* o = obs + ((size_t)slot * total_rep + sg.rep0 + threadIdx.x) * 2;
-    atomicAdd(o, (unsigned long long)s_cnt[0][threadIdx.x]);
-    atomicAdd(o + 1, (unsigned long long)s_cnt[1][threadIdx.x]);
   }
 }
 
@@ -567,19 +633,20 @@ void bdestroy(vg_batch* b) {
   delete b;
 }
 
-using MscPassFn = void (*)(const MscSeg*, const int2*, const uint32_t*, const MscDev*, uint32_t, KeySchedule, int);
+using MscPassFn = void (*)(const MscSeg*, const int2*, const uint32_t*, const MscDev*, uint32_t, KeySchedule, int,
+                           int, unsigned long long*);
 
-template <int C, int TPB>
+template <int C, int TPB, bool MEAS>
 MscPassFn msc_pass_wpt(int wpt, int wif) {
-  if (wpt == 2) return wif == 2 ? msc_pass<C, TPB, 2, 2> : msc_pass<C, TPB, 2, 1>;
-  if (wpt == 4) return wif == 2 ? msc_pass<C, TPB, 4, 2> : msc_pass<C, TPB, 4, 1>;
-  return wif == 2 ? msc_pass<C, TPB, 8, 2> : msc_pass<C, TPB, 8, 1>;
+  if (wpt == 2) return wif == 2 ? msc_pass<C, TPB, 2, 2, MEAS> : msc_pass<C, TPB, 2, 1, MEAS>;
+  if (wpt == 4) return wif == 2 ? msc_pass<C, TPB, 4, 2, MEAS> : msc_pass<C, TPB, 4, 1, MEAS>;
+  return wif == 2 ? msc_pass<C, TPB, 8, 2, MEAS> : msc_pass<C, TPB, 8, 1, MEAS>;
 }
 
-template <int C>
+template <int C, bool MEAS = false>
 MscPassFn msc_pass_fn(const vg_batch_tuning& t) {
-  return t.threads_per_block == 128 ? msc_pass_wpt<C, 128>(t.words_per_thread, t.words_in_flight)
-                                    : msc_pass_wpt<C, 256>(t.words_per_thread, t.words_in_flight);
+  return t.threads_per_block == 128 ? msc_pass_wpt<C, 128, MEAS>(t.words_per_thread, t.words_in_flight)
+                                    : msc_pass_wpt<C, 256, MEAS>(t.words_per_thread, t.words_in_flight);
 }
 
 bool tuning_supported(const vg_batch_tuning& t) {
@@ -607,19 +674,18 @@ int build_blocks(vg_batch* b) {
 // One round on the stream: sweeps, measurement, exchange, advance.
 int enqueue_round(vg_batch* b) {
   const int nb = (int)b->blocks.size();
-  const MscPassFn p0 = msc_pass_fn<0>(b->tune), p1 = msc_pass_fn<1>(b->tune);
+  const MscPassFn p0 = msc_pass_fn<0>(b->tune), p1 = msc_pass_fn<1>(b->tune), p1m = msc_pass_fn<1, true>(b->tune);
   const dim3 tpb((unsigned)b->tune.threads_per_block);
   for (int t = 0; t < b->every; ++t) {
     const int jsign = b->J > 0.0 ? 1 : b->J < 0.0 ? -1 : 0;
     VG_BCUDA(b, launch_pdl_ex(p0, dim3(nb), tpb, 0, b->stream, (const MscSeg*)b->d_segs, (const int2*)b->d_blocks,
-                           (const uint32_t*)b->d_tabs, (const MscDev*)b->d_dev, (uint32_t)t, b->ks, jsign));
-    VG_BCUDA(b, launch_pdl_ex(p1, dim3(nb), tpb, 0, b->stream, (const MscSeg*)b->d_segs, (const int2*)b->d_blocks,
-                           (const uint32_t*)b->d_tabs, (const MscDev*)b->d_dev, (uint32_t)t, b->ks, jsign));
+                           (const uint32_t*)b->d_tabs, (const MscDev*)b->d_dev, (uint32_t)t, b->ks, jsign,
+                           b->total_rep, b->d_obs));
+    // the round's last sweep measures its final state
+    VG_BCUDA(b, launch_pdl_ex(t + 1 == b->every ? p1m : p1, dim3(nb), tpb, 0, b->stream, (const MscSeg*)b->d_segs,
+                           (const int2*)b->d_blocks, (const uint32_t*)b->d_tabs, (const MscDev*)b->d_dev,
+                           (uint32_t)t, b->ks, jsign, b->total_rep, b->d_obs));
   }
-  msc_measure<<<nb, 256, 0, b->stream>>>(b->d_segs, b->d_blocks,
-                                         b->tune.threads_per_block * b->tune.words_per_thread, b->d_dev,
-                                         b->total_rep, b->d_obs);
-  VG_BCUDA(b, cudaGetLastError());
   int maxrep = 0;
   for (auto& g : b->groups) maxrep = std::max(maxrep, g.n_rep);
   msc_exchange<<<(int)b->groups.size(), 256, sizeof(double) * maxrep, b->stream>>>(
