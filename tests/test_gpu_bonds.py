@@ -39,6 +39,24 @@ def test_ising_bonds_bit_exact(V, O, cell, ext, pbc, proposal):
         assert abs(E - (-2.0 * bond + mag * (-m))) < 1e-9
 
 
+@pytest.mark.parametrize("cell,ext,pbc", [("bcc", (9, 30, 30), (1, 1, 1)), ("fcc", (9, 40, 40), (1, 1, 0))])
+def test_ising_bonds_entry_batches_bit_exact(V, O, cell, ext, pbc):
+    """A grid narrower than the class (152 x 64 threads): two entries per
+    thread at a time, the last pair partly past the class's end."""
+    seed, T, mag, n = 43, 2.9, 0.25, 3
+    eng, g, jb = _setup(V, O, cell, ext, pbc, V.SPIN_ISING, seed, threads_per_block=64, blocks_per_sm=1)
+    with eng:
+        eng.set_exchange_bonds(jb)
+        eng.init_random()
+        s0 = eng.get_state()
+        eng.set_thermostat(T, (0, 0, 1), mag)
+        sums = eng.sweeps_sums(n)
+        ref, obs = g.ising_sweeps_bonds(s0, jb, mag, T, seed, 0, n)
+        assert np.array_equal(eng.get_state(), ref)
+        np.testing.assert_allclose(sums[:, 0], obs[:, 0], rtol=0, atol=1e-9)
+        np.testing.assert_array_equal(sums[:, 6], obs[:, 1])
+
+
 def test_uniform_bonds_equal_the_uniform_constant(V, O):
     lat = V.Lattice.bcc(4, 4, 4)
     H = V.hamiltonian(V.Exchange(1.0))

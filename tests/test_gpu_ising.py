@@ -347,3 +347,40 @@ def test_tiled_path_selection(V):
         with pytest.raises(V.VegasGpuError) as e:
             _engine(V, "sc", ext, pbc, H, 1, path=V.PATH_TILED)
         assert e.value.status == 5
+
+
+# Generic path with a grid narrower than the class (152 blocks of 64 threads
+# = 9,728 threads per pass): the kernel takes 4 entries per thread at a time
+# (2 with twelve neighbours), the last batch of each thread partly past the
+# class's end.
+BATCHED = [
+    ("sc", (33, 24, 30), (1, 1, 1)),   # odd x: greedy colouring, classes ~11.9 k (1.2 batches)
+    ("bcc", (9, 30, 30), (1, 0, 1)),   # classes 8.1 k, fewer than the threads: one entry each
+    ("bcc", (9, 60, 60), (1, 1, 1)),   # classes 32.4 k: 3.3 batches
+    ("fcc", (9, 40, 40), (1, 1, 0)),   # twelve neighbours, classes ~14.4 k
+]
+
+
+@pytest.mark.parametrize("cell,ext,pbc", BATCHED)
+@pytest.mark.parametrize("proposal", [0, 1])
+def test_generic_entry_batches_bit_exact(V, O, cell, ext, pbc, proposal):
+    seed, J, T, mag, n = 2024, 1.0, 3.7, 0.2, 4
+    H = V.hamiltonian(V.Exchange(J), V.Zeeman()) if proposal else V.hamiltonian(V.Exchange(J))
+    with _engine(V, cell, ext, pbc, H, seed, proposal=proposal, path=V.PATH_GENERIC, threads_per_block=64,
+                 blocks_per_sm=1) as eng:
+        assert eng.info().path == V.PATH_GENERIC
+        g = O.Graph(O.lattice(cell, *ext, pbc))
+        eng.init_random()
+        s0 = eng.get_state()
+        assert np.array_equal(s0, g.ising_init(seed))
+        if proposal:
+            eng.set_thermostat(T, (0, 0, 1), mag)
+            sums = eng.sweeps_sums(n)
+            ref, obs = g.ising_sweeps(s0, J, mag, T, seed, 0, n, proposal=1)
+        else:
+            eng.set_thermostat(T)
+            sums = eng.sweeps_sums(n)
+            ref, obs = g.ising_sweeps(s0, J, 0.0, T, seed, 0, n)
+        assert np.array_equal(eng.get_state(), ref)
+        np.testing.assert_array_equal(sums[:, 0], obs[:, 0])
+        np.testing.assert_array_equal(sums[:, 6], obs[:, 1])

@@ -565,8 +565,9 @@ __global__ void __launch_bounds__(256, kSc2MinBlocks) ising_sc2_kernel(const Isi
 }
 
 // ------------------------------------------------------------- generic
-// One class entry per thread (entry j of the class: site sites[j]), so that a
-// class of a few hundred thousand sites still fills the GPU.  Entry j draws
+// Class entries dealt out per thread of a grid stride (entry j of the class:
+// site sites[j]), so that a class of a few hundred thousand sites still fills
+// the GPU.  Entry j draws
 // byte (j & 15) of the blocks of group j >> 4, exactly as the 16-entry
 // kernels do: the sixteen lanes of a half warp compute their group's block
 // together (the same instructions, no extra issue).
@@ -610,9 +611,18 @@ __device__ __forceinline__ void draw1(const RngKey& key, uint32_t g, int k, int 
                   : 0u;
 }
 
-template <int ZT, bool MEASURE, bool UPDATE, int PROP>
+// NI class entries per thread at a time (j, j + stride, ...), every load of
+// the NI entries issued before any store: a pass writes only its own class
+// and reads only the others, so the loads of later entries never depend on
+// the stores of earlier ones, but the compiler cannot know that across loop
+// iterations.  One entry per iteration left the kernel waiting on two levels
+// of dependent loads (index, then spin) per entry (bcc 128^3: 28.3 -> 40.4
+// flips/ns, sc 255^3: 33.7 -> 53.0 with NI = 4).  Classes with no more
+// entries than the grid has threads run NI = 1 (the batch's extra loads made
+// sc 64^3 28 % slower).
+template <int ZT, int NI, bool MEASURE, bool UPDATE, int PROP>
 __global__ void __launch_bounds__(256, 4) ising_gen_kernel(const IsingGenArgs a, const IsingTable tab, const RngKey key,
-                                                        const int colour, long long* __restrict__ part) {
+                                                         const int colour, long long* __restrict__ part) {
   constexpr int W = 2 * ZT + 1;
   __shared__ unsigned long long s_thr[2 * W];
   const int z = a.z;
@@ -624,97 +634,134 @@ __global__ void __launch_bounds__(256, 4) ising_gen_kernel(const IsingGenArgs a,
 
   int bond = 0, ups = 0, nacc = 0;  // per thread: a few entries of at most +-z each
   const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < a.n_c; j += stride) {
-    const uint32_t g = (uint32_t)(j >> 4);
-    const int k = (int)(j & 15);
-    uint32_t ub0, up;
-    draw1<UPDATE, PROP>(key, g, k, colour, ub0, up);
-    const int i = __ldg(a.sites + j);
-    const int s = a.spin[i];
-    const uint32_t lm = __ldg(a.lowmask + j);
-    int nsum = 0, nlow = 0;
+  for (long long j0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; j0 < a.n_c; j0 += NI * stride) {
+    int site[NI], s[NI], nsum[NI], nlow[NI];
+    uint32_t lm[NI];
+    bool live[NI];
+#pragma unroll
+    for (int b = 0; b < NI; ++b) {
+      const long long j = j0 + b * stride;
+      live[b] = j < a.n_c;
+      // an entry past the class's end loads entry j0's data and is dropped:
+      // unconditional loads let the compiler issue all of them up front
+      const long long jj = live[b] ? j : j0;
+      site[b] = __ldg(a.sites + jj);
+      lm[b] = __ldg(a.lowmask + jj);
+      nsum[b] = 0;
+      nlow[b] = 0;
+    }
+#pragma unroll
+    for (int b = 0; b < NI; ++b) s[b] = a.spin[site[b]];
 #pragma unroll
     for (int q = 0; q < ZT; ++q) {
       if (q < z) {
-        const int t = __ldg(a.nbr + ((uint32_t)q * (uint32_t)a.n_c + (uint32_t)j));
-        if (t >= 0) {
-          const int v = 2 * (int)a.spin[t] - 1;
-          nsum += v;
-          if ((lm >> q) & 1u) nlow += v;
+#pragma unroll
+        for (int b = 0; b < NI; ++b) {
+          const long long jj = live[b] ? j0 + b * stride : j0;
+          const int t = __ldg(a.nbr + ((uint32_t)q * (uint32_t)a.n_c + (uint32_t)jj));
+          if (t >= 0) {
+            const int v = 2 * (int)a.spin[t] - 1;
+            nsum[b] += v;
+            if ((lm[b] >> q) & 1u) nlow[b] += v;
+          }
         }
       }
     }
-    bool acc = false;
-    if (UPDATE && (PROP == VG_PROPOSE_FLIP || up != (uint32_t)s))
-      acc = decide1(s_thr[s * Wz + nsum + z], ub0, key, g, k, colour);
-    const int sn = s ^ (int)acc;
-    if (acc) a.spin[i] = (uint8_t)sn;
-    if (MEASURE) {
-      ups += sn;
-      bond += sn ? nlow : -nlow;
-      nacc += acc;
+#pragma unroll
+    for (int b = 0; b < NI; ++b) {
+      if (!live[b]) continue;
+      const long long j = j0 + b * stride;
+      const uint32_t g = (uint32_t)(j >> 4);
+      const int k = (int)(j & 15);
+      uint32_t ub0, up;
+      draw1<UPDATE, PROP>(key, g, k, colour, ub0, up);
+      bool acc = false;
+      if (UPDATE && (PROP == VG_PROPOSE_FLIP || up != (uint32_t)s[b]))
+        acc = decide1(s_thr[s[b] * Wz + nsum[b] + z], ub0, key, g, k, colour);
+      const int sn = s[b] ^ (int)acc;
+      if (acc) a.spin[site[b]] = (uint8_t)sn;
+      if (MEASURE) {
+        ups += sn;
+        bond += sn ? nlow[b] : -nlow[b];
+        nacc += acc;
+      }
     }
   }
   if (MEASURE) block_sum3_store(bond, ups, nacc, part + (size_t)blockIdx.x * kNumSums);
 }
 
-// Per-bond exchange constants (Exchange's CSR with arbitrary J_ij,
-// src/energy.rs:169-206): the field of a site is hJ = sum_k J_k s_k (FP64,
-// k order) and its threshold is formed per site exactly as the host table
-// forms it for uniform J: dE = (-(-s) hJ + hz (-s)) - (-s hJ + hz s),
-// thr = ceil(exp(-dE / T) 2^32).  Same draws and tie digits as the table
-// kernel; partial rows are FP64 (the bond sum sum J_ij s_i s_j is not an
-// integer).
-template <int ZT, bool MEASURE, bool UPDATE, int PROP>
+template <int ZT, int NI, bool MEASURE, bool UPDATE, int PROP>
 __global__ void __launch_bounds__(256) ising_bond_kernel(const IsingGenArgs a, const RngKey key, const int colour,
                                                          double* __restrict__ part) {
+  // NI entries per thread at a time, loads before stores (as ising_gen_kernel)
   pdl_launch_dependents();
   pdl_wait();
   double bond = 0.0, ups = 0.0, nacc = 0.0;
   const int z = a.z;
   const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < a.n_c; j += stride) {
-    const uint32_t g = (uint32_t)(j >> 4);
-    const int k = (int)(j & 15);
-    uint32_t ub0, up;
-    draw1<UPDATE, PROP>(key, g, k, colour, ub0, up);
-    const int i = __ldg(a.sites + j);
-    const uint32_t s01 = a.spin[i];
-    const uint32_t lm = __ldg(a.lowmask + j);
-    double hj = 0.0, hlow = 0.0;
+  for (long long j0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; j0 < a.n_c; j0 += NI * stride) {
+    int site[NI];
+    uint32_t s01[NI], lm[NI];
+    double hj[NI], hlow[NI];
+    bool live[NI];
+#pragma unroll
+    for (int b = 0; b < NI; ++b) {
+      const long long j = j0 + b * stride;
+      live[b] = j < a.n_c;
+      const long long jj = live[b] ? j : j0;  // past the class's end: entry j0's data, dropped
+      site[b] = __ldg(a.sites + jj);
+      lm[b] = __ldg(a.lowmask + jj);
+      hj[b] = 0.0;
+      hlow[b] = 0.0;
+    }
+#pragma unroll
+    for (int b = 0; b < NI; ++b) s01[b] = a.spin[site[b]];
 #pragma unroll
     for (int q = 0; q < ZT; ++q) {
       if (q < z) {
-        const uint32_t e = (uint32_t)q * (uint32_t)a.n_c + (uint32_t)j;
-        const int nb = __ldg(a.nbr + e);
-        if (nb >= 0) {
-          const double v = __ldg(a.jb + e) * (double)(2 * (int)a.spin[nb] - 1);
-          hj += v;
-          if ((lm >> q) & 1u) hlow += v;
+#pragma unroll
+        for (int b = 0; b < NI; ++b) {
+          const long long jj = live[b] ? j0 + b * stride : j0;
+          const uint32_t e = (uint32_t)q * (uint32_t)a.n_c + (uint32_t)jj;
+          const int nb = __ldg(a.nbr + e);
+          if (nb >= 0) {
+            const double v = __ldg(a.jb + e) * (double)(2 * (int)a.spin[nb] - 1);
+            hj[b] += v;
+            if ((lm[b] >> q) & 1u) hlow[b] += v;
+          }
         }
       }
     }
-    bool acc = false;
-    if (UPDATE && (PROP == VG_PROPOSE_FLIP || up != s01)) {
-      const double sd = s01 ? 1.0 : -1.0;
-      const double e_old = -sd * hj + a.hz * sd;
-      const double e_new = -(-sd) * hj + a.hz * (-sd);
-      const double de = e_new - e_old;
-      unsigned long long th;
-      if (de <= 0.0) {
-        th = 1ull << 32;
-      } else {
-        const double x = ceil(exp(-de / a.T) * 4294967296.0);
-        th = x >= 4294967296.0 ? (1ull << 32) : x <= 0.0 ? 0ull : (unsigned long long)x;
+#pragma unroll
+    for (int b = 0; b < NI; ++b) {
+      if (!live[b]) continue;
+      const long long j = j0 + b * stride;
+      const uint32_t g = (uint32_t)(j >> 4);
+      const int k = (int)(j & 15);
+      uint32_t ub0, up;
+      draw1<UPDATE, PROP>(key, g, k, colour, ub0, up);
+      bool acc = false;
+      if (UPDATE && (PROP == VG_PROPOSE_FLIP || up != s01[b])) {
+        const double sd = s01[b] ? 1.0 : -1.0;
+        const double e_old = -sd * hj[b] + a.hz * sd;
+        const double e_new = -(-sd) * hj[b] + a.hz * (-sd);
+        const double de = e_new - e_old;
+        unsigned long long th;
+        if (de <= 0.0) {
+          th = 1ull << 32;
+        } else {
+          const double x = ceil(exp(-de / a.T) * 4294967296.0);
+          th = x >= 4294967296.0 ? (1ull << 32) : x <= 0.0 ? 0ull : (unsigned long long)x;
+        }
+        acc = decide1(th, ub0, key, g, k, colour);
       }
-      acc = decide1(th, ub0, key, g, k, colour);
-    }
-    const int sn = (int)s01 ^ (int)acc;
-    if (acc) a.spin[i] = (uint8_t)sn;
-    if (MEASURE) {
-      ups += (double)sn;
-      bond += sn ? hlow : -hlow;
-      nacc += acc ? 1.0 : 0.0;
+      const int sn = (int)s01[b] ^ (int)acc;
+      if (acc) a.spin[site[b]] = (uint8_t)sn;
+      if (MEASURE) {
+        ups += (double)sn;
+        bond += sn ? hlow[b] : -hlow[b];
+        nacc += acc ? 1.0 : 0.0;
+      }
     }
   }
   if (MEASURE) {
@@ -1075,18 +1122,44 @@ cudaError_t launch_ising_sc(const IsingScArgs& a, const IsingTable& tab, RngKey 
                  : sc_dispatch<1, false>(a, tab, key, proposal, update, part, grid, tpb, s);
 }
 
+template <int ZT, int NI>
+static cudaError_t gen_dispatch_ni(const IsingGenArgs& a, const IsingTable& tab, RngKey key, int colour,
+                                   int proposal, bool update, long long* part, int grid, int tpb, cudaStream_t s) {
+  const bool m = part != nullptr;
+  if (!update) {
+    launch_pdl(ising_gen_kernel<ZT, NI, true, false, VG_PROPOSE_FLIP>, grid, tpb, s, a, tab, key, colour, part);
+  } else if (proposal == VG_PROPOSE_FLIP) {
+    if (m) launch_pdl(ising_gen_kernel<ZT, NI, true, true, VG_PROPOSE_FLIP>, grid, tpb, s, a, tab, key, colour, part);
+    else launch_pdl(ising_gen_kernel<ZT, NI, false, true, VG_PROPOSE_FLIP>, grid, tpb, s, a, tab, key, colour, part);
+  } else {
+    if (m) launch_pdl(ising_gen_kernel<ZT, NI, true, true, VG_PROPOSE_RANDOM>, grid, tpb, s, a, tab, key, colour, part);
+    else launch_pdl(ising_gen_kernel<ZT, NI, false, true, VG_PROPOSE_RANDOM>, grid, tpb, s, a, tab, key, colour, part);
+  }
+  return cudaGetLastError();
+}
+
+// more class entries than threads: NI entries at a time (4 up to eight
+// neighbours, 2 for twelve: registers)
 template <int ZT>
 static cudaError_t gen_dispatch(const IsingGenArgs& a, const IsingTable& tab, RngKey key, int colour, int proposal,
                                 bool update, long long* part, int grid, int tpb, cudaStream_t s) {
+  if (a.n_c > (long long)grid * tpb)
+    return gen_dispatch_ni<ZT, ZT <= 8 ? 4 : 2>(a, tab, key, colour, proposal, update, part, grid, tpb, s);
+  return gen_dispatch_ni<ZT, 1>(a, tab, key, colour, proposal, update, part, grid, tpb, s);
+}
+
+template <int ZT, int NI>
+static cudaError_t bond_dispatch_ni(const IsingGenArgs& a, RngKey key, int colour, int proposal, bool update,
+                                    double* part, int grid, int tpb, cudaStream_t s) {
   const bool m = part != nullptr;
   if (!update) {
-    launch_pdl(ising_gen_kernel<ZT, true, false, VG_PROPOSE_FLIP>, grid, tpb, s, a, tab, key, colour, part);
+    launch_pdl(ising_bond_kernel<ZT, NI, true, false, VG_PROPOSE_FLIP>, grid, tpb, s, a, key, colour, part);
   } else if (proposal == VG_PROPOSE_FLIP) {
-    if (m) launch_pdl(ising_gen_kernel<ZT, true, true, VG_PROPOSE_FLIP>, grid, tpb, s, a, tab, key, colour, part);
-    else launch_pdl(ising_gen_kernel<ZT, false, true, VG_PROPOSE_FLIP>, grid, tpb, s, a, tab, key, colour, part);
+    if (m) launch_pdl(ising_bond_kernel<ZT, NI, true, true, VG_PROPOSE_FLIP>, grid, tpb, s, a, key, colour, part);
+    else launch_pdl(ising_bond_kernel<ZT, NI, false, true, VG_PROPOSE_FLIP>, grid, tpb, s, a, key, colour, part);
   } else {
-    if (m) launch_pdl(ising_gen_kernel<ZT, true, true, VG_PROPOSE_RANDOM>, grid, tpb, s, a, tab, key, colour, part);
-    else launch_pdl(ising_gen_kernel<ZT, false, true, VG_PROPOSE_RANDOM>, grid, tpb, s, a, tab, key, colour, part);
+    if (m) launch_pdl(ising_bond_kernel<ZT, NI, true, true, VG_PROPOSE_RANDOM>, grid, tpb, s, a, key, colour, part);
+    else launch_pdl(ising_bond_kernel<ZT, NI, false, true, VG_PROPOSE_RANDOM>, grid, tpb, s, a, key, colour, part);
   }
   return cudaGetLastError();
 }
@@ -1094,17 +1167,8 @@ static cudaError_t gen_dispatch(const IsingGenArgs& a, const IsingTable& tab, Rn
 template <int ZT>
 static cudaError_t bond_dispatch(const IsingGenArgs& a, RngKey key, int colour, int proposal, bool update,
                                  double* part, int grid, int tpb, cudaStream_t s) {
-  const bool m = part != nullptr;
-  if (!update) {
-    launch_pdl(ising_bond_kernel<ZT, true, false, VG_PROPOSE_FLIP>, grid, tpb, s, a, key, colour, part);
-  } else if (proposal == VG_PROPOSE_FLIP) {
-    if (m) launch_pdl(ising_bond_kernel<ZT, true, true, VG_PROPOSE_FLIP>, grid, tpb, s, a, key, colour, part);
-    else launch_pdl(ising_bond_kernel<ZT, false, true, VG_PROPOSE_FLIP>, grid, tpb, s, a, key, colour, part);
-  } else {
-    if (m) launch_pdl(ising_bond_kernel<ZT, true, true, VG_PROPOSE_RANDOM>, grid, tpb, s, a, key, colour, part);
-    else launch_pdl(ising_bond_kernel<ZT, false, true, VG_PROPOSE_RANDOM>, grid, tpb, s, a, key, colour, part);
-  }
-  return cudaGetLastError();
+  if (a.n_c > (long long)grid * tpb) return bond_dispatch_ni<ZT, 2>(a, key, colour, proposal, update, part, grid, tpb, s);
+  return bond_dispatch_ni<ZT, 1>(a, key, colour, proposal, update, part, grid, tpb, s);
 }
 
 cudaError_t launch_ising_gen(const IsingGenArgs& a, const IsingTable& tab, RngKey key, int colour, int proposal,
