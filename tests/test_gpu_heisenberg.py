@@ -78,6 +78,32 @@ def test_sublattice_runs_of_four_follow_oracle(V, O, cell, ext, pbc, precision):
         np.testing.assert_allclose(sums[-1, :7], obs[-1, :7], rtol=0, atol=1e-8)
 
 
+@pytest.mark.parametrize("cell,ext,pbc", [("sc", (33, 24, 30), (1, 1, 1)), ("fcc", (9, 40, 40), (1, 1, 0))])
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_generic_entry_batches_follow_oracle(V, O, cell, ext, pbc, precision):
+    """The neighbour-table kernel on a grid narrower than its classes (152 x 64
+    threads): two entries per thread at a time, the last pair partly past the
+    class's end."""
+    J, K, axis, mag, b, T, seed = 1.0, 0.1, (0.0, 0.0, 1.0), 0.05, (0.0, 0.6, 0.8), 0.9, 21
+    fp64 = precision == "fp64"
+    H = V.hamiltonian(V.Exchange(J), V.UniaxialAnisotropy(axis, K), V.Zeeman())
+    lat = getattr(V.Lattice, cell)(*ext, pbc=tuple(bool(p) for p in pbc))
+    with V.Engine(lat, H, spin=V.SPIN_HEISENBERG, seed=seed, precision=V.FP64 if fp64 else V.FP32, proposal=1,
+                  path=V.PATH_GENERIC, threads_per_block=64, blocks_per_sm=1) as eng:
+        assert eng.info().path == V.PATH_GENERIC
+        eng.init_random()
+        s0 = eng.get_state()
+        eng.set_thermostat(T, b, mag)
+        sums = eng.sweeps_sums(1)
+        s1 = eng.get_state()
+    g = O.Graph(O.lattice(cell, *ext, pbc))
+    ref1, obs = g.heis_sweeps(s0, _params(O, J, K, axis, mag, b, 0.0, T), seed, 0, 1, proposal=1)
+    same = np.all(np.abs(s1 - ref1) < (1e-12 if fp64 else 2e-6), axis=1)
+    assert same.mean() >= 0.999
+    if fp64 and same.all():
+        np.testing.assert_allclose(sums[-1, :7], obs[-1, :7], rtol=0, atol=1e-8)
+
+
 @pytest.mark.parametrize("cell,ext,pbc", LATTICES)
 def test_fp32_follows_oracle(V, O, cell, ext, pbc):
     s0, ref0, s1, ref1, sums, obs, _ = _run(V, O, cell, ext, pbc, V.FP32, 1, n=1)

@@ -201,7 +201,12 @@ __global__ void __launch_bounds__(256) heis_sc4_kernel(const HeisScArgs<R> a, co
 }
 
 // ------------------------------------------------------------- generic
-template <typename R, int ZT, bool MEASURE, bool UPDATE, int PROP>
+// NI class entries per thread at a time (j, j + stride, ...), the loads of
+// all NI issued before any store: a pass writes only its own class and reads
+// only the others, which the compiler cannot see across loop iterations.
+// Entries keep their order within a thread, so the per-thread sums are the
+// same.  Classes with no more entries than the grid has threads run NI = 1.
+template <typename R, int ZT, int NI, bool MEASURE, bool UPDATE, int PROP>
 __global__ void __launch_bounds__(256) heis_gen_kernel(const HeisGenArgs<R> a, const HeisParams<R> P, const RngKey key,
                                                        const int colour, double* __restrict__ part) {
   R acc[kNumSums];
@@ -210,42 +215,64 @@ __global__ void __launch_bounds__(256) heis_gen_kernel(const HeisGenArgs<R> a, c
   pdl_launch_dependents();
   pdl_wait();
   const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < a.n_c; j += stride) {
-    const int i = __ldg(a.sites + j);
-    const uint32_t lm = __ldg(a.lowmask + j);
-    V3<R> hs = {(R)0, (R)0, (R)0}, low = {(R)0, (R)0, (R)0};
+  for (long long j0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; j0 < a.n_c; j0 += NI * stride) {
+    int site[NI];
+    uint32_t lm[NI];
+    bool live[NI];
+    V3<R> hs[NI], low[NI], s[NI];
+#pragma unroll
+    for (int b = 0; b < NI; ++b) {
+      const long long j = j0 + b * stride;
+      live[b] = j < a.n_c;
+      const long long jj = live[b] ? j : j0;  // past the class's end: entry j0's data, dropped
+      site[b] = __ldg(a.sites + jj);
+      lm[b] = __ldg(a.lowmask + jj);
+      hs[b] = {(R)0, (R)0, (R)0};
+      low[b] = {(R)0, (R)0, (R)0};
+    }
 #pragma unroll
     for (int k = 0; k < ZT; ++k) {
       if (k < a.zc) {
-        const int t = __ldg(a.nbr + ((uint32_t)k * (uint32_t)a.n_c + (uint32_t)j));
-        if (t >= 0) {
-          const R wk = a.jb ? __ldg(a.jb + ((uint32_t)k * (uint32_t)a.n_c + (uint32_t)j)) : (R)1;
-          const R vx = wk * a.x[t], vy = wk * a.y[t], vz = wk * a.z[t];
-          hs.x += vx;
-          hs.y += vy;
-          hs.z += vz;
-          if ((lm >> k) & 1u) {
-            low.x += vx;
-            low.y += vy;
-            low.z += vz;
+#pragma unroll
+        for (int b = 0; b < NI; ++b) {
+          const long long jj = live[b] ? j0 + b * stride : j0;
+          const uint32_t e = (uint32_t)k * (uint32_t)a.n_c + (uint32_t)jj;
+          const int t = __ldg(a.nbr + e);
+          if (t >= 0) {
+            const R wk = a.jb ? __ldg(a.jb + e) : (R)1;
+            const R vx = wk * a.x[t], vy = wk * a.y[t], vz = wk * a.z[t];
+            hs[b].x += vx;
+            hs[b].y += vy;
+            hs[b].z += vz;
+            if ((lm[b] >> k) & 1u) {
+              low[b].x += vx;
+              low[b].y += vy;
+              low[b].z += vz;
+            }
           }
         }
       }
     }
-    V3<R> s = {a.x[i], a.y[i], a.z[i]};
-    if (UPDATE) {
-      const uint4 w =
-          philox_ks(make_uint4((uint32_t)j, key.sweep, (kTagHeis << 24) | ((uint32_t)colour << 8), key.replica), key.ks);
-      V3<R> sn;
-      if (heis_update<R, PROP>(s, hs, P, w, sn)) {
-        a.x[i] = sn.x;
-        a.y[i] = sn.y;
-        a.z[i] = sn.z;
-        s = sn;
-        acc[7] += (R)1;
+#pragma unroll
+    for (int b = 0; b < NI; ++b) s[b] = {a.x[site[b]], a.y[site[b]], a.z[site[b]]};
+#pragma unroll
+    for (int b = 0; b < NI; ++b) {
+      if (!live[b]) continue;
+      const long long j = j0 + b * stride;
+      if (UPDATE) {
+        const uint4 w = philox_ks(
+            make_uint4((uint32_t)j, key.sweep, (kTagHeis << 24) | ((uint32_t)colour << 8), key.replica), key.ks);
+        V3<R> sn;
+        if (heis_update<R, PROP>(s[b], hs[b], P, w, sn)) {
+          a.x[site[b]] = sn.x;
+          a.y[site[b]] = sn.y;
+          a.z[site[b]] = sn.z;
+          s[b] = sn;
+          acc[7] += (R)1;
+        }
       }
+      if (MEASURE) add_site_sums(acc, s[b], low[b], P);
     }
-    if (MEASURE) add_site_sums(acc, s, low, P);
   }
   if (MEASURE) flush_sums(acc, part);
 }
@@ -305,19 +332,26 @@ cudaError_t launch_heis_sc(const HeisScArgs<R>& a, const HeisParams<R>& p, RngKe
   return cudaGetLastError();
 }
 
+template <typename R, int ZT, int NI>
+static void gen_go_ni(const HeisGenArgs<R>& a, const HeisParams<R>& p, RngKey key, int colour, int proposal,
+                      bool update, double* part, int grid, int tpb, cudaStream_t s) {
+  const bool m = part != nullptr;
+  if (!update) {
+    launch_pdl(heis_gen_kernel<R, ZT, NI, true, false, VG_PROPOSE_FLIP>, grid, tpb, s, a, p, key, colour, part);
+  } else if (proposal == VG_PROPOSE_RANDOM) {
+    if (m) launch_pdl(heis_gen_kernel<R, ZT, NI, true, true, VG_PROPOSE_RANDOM>, grid, tpb, s, a, p, key, colour, part);
+    else launch_pdl(heis_gen_kernel<R, ZT, NI, false, true, VG_PROPOSE_RANDOM>, grid, tpb, s, a, p, key, colour, part);
+  } else {
+    if (m) launch_pdl(heis_gen_kernel<R, ZT, NI, true, true, VG_PROPOSE_FLIP>, grid, tpb, s, a, p, key, colour, part);
+    else launch_pdl(heis_gen_kernel<R, ZT, NI, false, true, VG_PROPOSE_FLIP>, grid, tpb, s, a, p, key, colour, part);
+  }
+}
+
 template <typename R, int ZT>
 static void gen_go(const HeisGenArgs<R>& a, const HeisParams<R>& p, RngKey key, int colour, int proposal, bool update,
                    double* part, int grid, int tpb, cudaStream_t s) {
-  const bool m = part != nullptr;
-  if (!update) {
-    launch_pdl(heis_gen_kernel<R, ZT, true, false, VG_PROPOSE_FLIP>, grid, tpb, s, a, p, key, colour, part);
-  } else if (proposal == VG_PROPOSE_RANDOM) {
-    if (m) launch_pdl(heis_gen_kernel<R, ZT, true, true, VG_PROPOSE_RANDOM>, grid, tpb, s, a, p, key, colour, part);
-    else launch_pdl(heis_gen_kernel<R, ZT, false, true, VG_PROPOSE_RANDOM>, grid, tpb, s, a, p, key, colour, part);
-  } else {
-    if (m) launch_pdl(heis_gen_kernel<R, ZT, true, true, VG_PROPOSE_FLIP>, grid, tpb, s, a, p, key, colour, part);
-    else launch_pdl(heis_gen_kernel<R, ZT, false, true, VG_PROPOSE_FLIP>, grid, tpb, s, a, p, key, colour, part);
-  }
+  if (a.n_c > (long long)grid * tpb) gen_go_ni<R, ZT, 2>(a, p, key, colour, proposal, update, part, grid, tpb, s);
+  else gen_go_ni<R, ZT, 1>(a, p, key, colour, proposal, update, part, grid, tpb, s);
 }
 
 template <typename R>
