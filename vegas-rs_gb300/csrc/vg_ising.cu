@@ -305,8 +305,10 @@ constexpr int kSc2MinBlocks = 3;  // 80 registers: the pair state stays in regis
 // that ignored ties ran 1,128 flips/ns against 790), and the work in the
 // pair loop, which runs in most rounds whatever the queue, dominates it:
 // a per-warp queue, this block queue, deferring whole groups to the end of
-// the block and a per-warp ring of tied groups drained 32 at a time all ran
-// between 756 and 802 flips/ns.  The kernel is latency-bound (43 % of issue
+// the block, a per-warp ring of tied groups drained 32 at a time, and
+// deciding a tied group's ties in line from its second-digit Philox block
+// (byte-parallel against the thresholds' second bytes) all ran between 739
+// and 802 flips/ns.  The kernel is latency-bound (43 % of issue
 // slots used), so serial work on a tie lengthens its warp's path.
 constexpr int kSc2BlockQueue = 512;
 
