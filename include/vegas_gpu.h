@@ -22,9 +22,11 @@
  *     the lattice's site order: site = ((cz*ny + cy)*nx + cx)*nbasis + b.
  *     Ising spins are int8 +1 (Up) / -1 (Down); Heisenberg spins are three
  *     doubles (x, y, z) per site.
- *   - Sweep t of a context draws its random numbers from Philox4x32-10 keyed by
- *     (seed, replica) with counters (site, t, stream tag); (seed, sweep index)
- *     is the whole RNG state, so vg_set_sweep_index resumes a run exactly.
+ *   - Sweep t of a context draws its random numbers from Philox4x32 keyed by
+ *     (seed, replica) with counters (site, t, stream tag): 10 rounds for
+ *     Ising draws and initial states, 7 for the Heisenberg update draws and
+ *     the batched threshold planes; (seed, sweep index) is the whole RNG
+ *     state, so vg_set_sweep_index resumes a run exactly.
  */
 #ifndef VEGAS_GPU_H
 #define VEGAS_GPU_H

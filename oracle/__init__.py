@@ -154,6 +154,7 @@ def philox(ctr, key, rounds=10):
 
 
 MSC_ROUNDS = 7  # Philox rounds of the batched threshold planes
+HEIS_ROUNDS = 7  # Philox rounds of the Heisenberg update draws
 
 
 def lattice(cell="sc", nx=4, ny=4, nz=4, pbc=(True, True, True)) -> Lattice:

@@ -463,7 +463,11 @@ static int heis_sweeps(int64_t n, int32_t zmax, const int32_t* nbr, const double
           }
         }
         uint32_t w[4];
-        draw(seed, (uint32_t)j, sweep, ((uint32_t)VO_TAG_HEIS << 24) | ((uint32_t)c << 8), replica, w);
+        {
+          const uint32_t ctr[4] = {(uint32_t)j, sweep, ((uint32_t)VO_TAG_HEIS << 24) | ((uint32_t)c << 8), replica};
+          const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+          vo_philox4x32_r(ctr, key, VO_HEIS_ROUNDS, w);
+        }
         double p[3];
         if (proposal == VO_PROPOSE_RANDOM) {
           vo_heis_proposal(w[0], w[1], p);

@@ -43,9 +43,12 @@ extern "C" {
 /* ---------------------------------------------------------------- Philox */
 void vo_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 /* Philox4x32 with the given number of rounds (1..10); the batched
- * multi-spin-coded threshold planes use VO_MSC_ROUNDS. */
+ * multi-spin-coded threshold planes use VO_MSC_ROUNDS, the Heisenberg
+ * update draws (proposal and acceptance) VO_HEIS_ROUNDS.  Salmon et al.
+ * (SC'11) report Philox4x32 passing TestU01's Crush batteries from 7
+ * rounds on; initial states, Ising draws and exchange decisions keep 10. */
 void vo_philox4x32_r(const uint32_t ctr[4], const uint32_t key[2], int rounds, uint32_t out[4]);
-enum { VO_MSC_ROUNDS = 7 };
+enum { VO_MSC_ROUNDS = 7, VO_HEIS_ROUNDS = 7 };
 
 /* Draw-stream tags (bits 24..31 of the third counter word). */
 enum {

@@ -168,7 +168,8 @@ __global__ void __launch_bounds__(kPassTpb, TRACK ? kTrackMinBlocks : kPassMinBl
       const V3<R> s = {S[0].v[k], S[1].v[k], S[2].v[k]};
       const V3<R> h = {hf[0].v[k], hf[1].v[k], hf[2].v[k]};
       const uint4 w =
-          philox_ks(make_uint4(j0 + (uint32_t)k, sweep, (kTagHeis << 24) | ((uint32_t)CLS << 8), rp.replica), rp.ks);
+          philox_ks<kHeisRounds>(make_uint4(j0 + (uint32_t)k, sweep, (kTagHeis << 24) | ((uint32_t)CLS << 8), rp.replica),
+                                 rp.ks);
       V3<R> sn;
       if (heis_update<R, PROP>(s, h, P, w, sn)) {
         S[0].v[k] = sn.x;

@@ -72,7 +72,8 @@ __global__ void __launch_bounds__(256) heis_sc_kernel(const HeisScArgs<R> a, con
     const int q = rb + h;
     V3<R> s = {ox[q], oy[q], oz[q]};
     if (UPDATE) {
-      const uint4 w = philox_ks(make_uint4(j, key.sweep, (kTagHeis << 24) | ((uint32_t)C << 8), key.replica), key.ks);
+      const uint4 w = philox_ks<kHeisRounds>(
+          make_uint4(j, key.sweep, (kTagHeis << 24) | ((uint32_t)C << 8), key.replica), key.ks);
       V3<R> sn;
       if (heis_update<R, PROP>(s, hs, P, w, sn)) {
         ox[q] = sn.x;
@@ -174,9 +175,8 @@ __global__ void __launch_bounds__(256) heis_sc4_kernel(const HeisScArgs<R> a, co
       V3<R> s = {S[0].v[k], S[1].v[k], S[2].v[k]};
       const V3<R> h = {hs[0].v[k], hs[1].v[k], hs[2].v[k]};
       if (UPDATE) {
-        const uint4 w = philox_ks(make_uint4(j0 + (uint32_t)k, key.sweep, (kTagHeis << 24) | ((uint32_t)C << 8),
-                                             key.replica),
-                                  key.ks);
+        const uint4 w = philox_ks<kHeisRounds>(
+            make_uint4(j0 + (uint32_t)k, key.sweep, (kTagHeis << 24) | ((uint32_t)C << 8), key.replica), key.ks);
         V3<R> sn;
         if (heis_update<R, PROP>(s, h, P, w, sn)) {
           S[0].v[k] = sn.x;
@@ -260,7 +260,7 @@ __global__ void __launch_bounds__(256) heis_gen_kernel(const HeisGenArgs<R> a, c
       if (!live[b]) continue;
       const long long j = j0 + b * stride;
       if (UPDATE) {
-        const uint4 w = philox_ks(
+        const uint4 w = philox_ks<kHeisRounds>(
             make_uint4((uint32_t)j, key.sweep, (kTagHeis << 24) | ((uint32_t)colour << 8), key.replica), key.ks);
         V3<R> sn;
         if (heis_update<R, PROP>(s[b], hs[b], P, w, sn)) {
@@ -409,9 +409,8 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 2) heis_sub_kernel(c
       V3<R> s = {S[0].v[k], S[1].v[k], S[2].v[k]};
       if (UPDATE) {
         const V3<R> h = {hf[0].v[k], hf[1].v[k], hf[2].v[k]};
-        const uint4 w = philox_ks(make_uint4(j0 + (uint32_t)k, key.sweep, (kTagHeis << 24) | ((uint32_t)CLS << 8),
-                                             key.replica),
-                                  key.ks);
+        const uint4 w = philox_ks<kHeisRounds>(
+            make_uint4(j0 + (uint32_t)k, key.sweep, (kTagHeis << 24) | ((uint32_t)CLS << 8), key.replica), key.ks);
         V3<R> sn;
         if (heis_update<R, PROP>(s, h, P, w, sn)) {
           S[0].v[k] = sn.x;

@@ -53,6 +53,14 @@ inline bool sweep_range_ok(unsigned long long first, unsigned long long n) {
   return first < kSweepLimit && n <= kSweepLimit - first;
 }
 
+// Philox rounds of the Heisenberg update draws (proposal and acceptance, one
+// block per site): Salmon et al., "Parallel random numbers: as easy as 1, 2,
+// 3" (SC'11), report Philox4x32 passing TestU01's Crush batteries from 7
+// rounds on and take 10 as the default for a safety margin of 3 rounds.  The
+// per-site block was about a fifth of the FP32 update's instructions.
+// Initial states and the Ising draws keep 10 rounds.
+constexpr int kHeisRounds = 7;
+
 // Draw-stream tags (bits 24..31 of Philox counter word 2).
 enum : uint32_t {
   kTagIsingAccept = 1,
