@@ -265,3 +265,19 @@ def test_philox_round_count(O):
     lib.vo_philox4x32_r(c, k, 10, o)
     assert list(o) == O.philox(ctr, key)
     assert O.philox(ctr, key, rounds=7) != O.philox(ctr, key)
+
+
+def test_heisenberg_draws_use_the_reduced_round_function(O):
+    """One oracle Heisenberg sweep at a temperature where every move accepts
+    sets each site to the proposal built from its Philox4x32-HEIS_ROUNDS block
+    (counter: class entry, sweep, tag 3 << 24 | colour << 8, replica)."""
+    seed = 5
+    g = O.Graph(O.lattice("sc", 4, 4, 4, (1, 1, 1)))
+    s0 = g.heis_init(seed)
+    P = O.HeisParams(J=1.0, K=0.0, hz=0.0, Kc=0.0, T=1e12)
+    s1, _ = g.heis_sweeps(s0, P, seed, 0, 1, proposal=O.PROPOSE_RANDOM)
+    assert O.HEIS_ROUNDS == 7
+    for c in range(g.ncolours):
+        for j, i in enumerate(np.nonzero(g.colour == c)[0]):
+            w = O.philox([int(j), 0, (3 << 24) | (c << 8), 0], [seed, 0], rounds=O.HEIS_ROUNDS)
+            np.testing.assert_array_equal(s1[i], O.heis_proposal(w[0], w[1]))
