@@ -9,7 +9,8 @@
  *
  *  (a) colour_cpu -- the GPU's own update order (colour-class passes over a
  *      greedy colouring of the neighbour list) with the same counter-based
- *      Philox4x32-10 draws, the same integer Delta-E index and the same
+ *      Philox4x32 draws (10 rounds; 7 for the Heisenberg update and the
+ *      batched threshold planes), the same integer Delta-E index and the same
  *      acceptance-threshold table.  Ising results are bit-exact against the
  *      CUDA kernels; Heisenberg runs in FP64 and is compared with tolerances.
  *
