@@ -550,7 +550,9 @@ __global__ void __launch_bounds__(256, kSc2MinBlocks) ising_sc2_kernel(const Isi
   // Larger classes run pairs: dealing the pairs left over after whole rounds
   // out as single groups, evenly over the SMs, was slower at 192^3 - 512^3
   // (256^3: 9.8 -> 10.4 us) than letting a quarter of the blocks run one
-  // more pair round on issue slots the others have freed.
+  // more pair round on issue slots the others have freed, and so were a
+  // few leftover pairs for every warp (256^3: 805 -> 707 flips/ns) and one
+  // contiguous range of pairs per block (805 -> 774; 512^3 1,085 -> 1,038).
   const uint32_t T = gridDim.x * blockDim.x;
   const uint32_t first = blockIdx.x * blockDim.x + (threadIdx.x & ~31u);
   if (a.groups <= T) {
