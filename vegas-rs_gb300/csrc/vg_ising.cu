@@ -297,7 +297,9 @@ __global__ void __launch_bounds__(256, UNIFORM ? 4 : 2) ising_sc_kernel(const Is
 // every group draws and decides exactly as in ising_sc_kernel (same Philox
 // blocks, same tie resolution), so results are identical.  ALLPER: all axes
 // periodic, no missing rows.
-constexpr int kSc2MinBlocks = 3;  // 80 registers: the pair state stays in registers
+// 80 registers: the pair state stays in registers (four blocks per SM at 64
+// registers spilled ~100 bytes a thread and ran 256^3 at 708 flips/ns, 804 so)
+constexpr int kSc2MinBlocks = 3;
 // Ties on the first digit (1/256 of the candidate sites, so that a warp
 // meets one in most rounds of pairs) are queued per block and decided after
 // the block's pairs; entries past the queue's end are decided in line.
