@@ -51,7 +51,11 @@ namespace {
 constexpr int kHbSums = VG_HB_NSUMS;
 constexpr int kTpb = 256;            // reduction and set-up kernels
 constexpr int kPassTpb = 256;        // colour passes and measurement
-constexpr int kPassMinBlocks = 4;    // 64 registers: 32 resident warps per SM (latency-bound loads)
+// 64 registers: 32 resident warps per SM (latency-bound loads).  One run
+// already has its 36 neighbour loads in flight: two runs per thread at a
+// time, loads before stores, ran the c5 sample at 62 flips/ns against 74.7
+// (spilling at 64 registers, or at 80 with three blocks per SM).
+constexpr int kPassMinBlocks = 4;
 constexpr int kTrackMinBlocks = 4;   // tracked passes too (partials in shared memory)
 
 template <typename R>
