@@ -1508,7 +1508,7 @@ int vg_current_sums(vg_ctx* c, vg_sums* out) {
 
 int vg_total_energy(vg_ctx* c, double* e) {
   if (!c || !e) return VG_ERR_INVALID_ARG;
-  vg_sums s;
+  vg_sums s{};
   int rc = vg_current_sums(c, &s);
   if (rc) return rc;
   energy_of(c, &s, e, nullptr);
@@ -1517,7 +1517,7 @@ int vg_total_energy(vg_ctx* c, double* e) {
 
 int vg_magnetization(vg_ctx* c, double m[3], double* mag) {
   if (!c) return VG_ERR_INVALID_ARG;
-  vg_sums s;
+  vg_sums s{};
   int rc = vg_current_sums(c, &s);
   if (rc) return rc;
   if (m) {
