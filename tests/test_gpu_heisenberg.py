@@ -104,6 +104,18 @@ def test_generic_entry_batches_follow_oracle(V, O, cell, ext, pbc, precision):
         np.testing.assert_allclose(sums[-1, :7], obs[-1, :7], rtol=0, atol=1e-8)
 
 
+@pytest.mark.parametrize("cell,ext,pbc", [("sc", (2, 2, 2), (1, 1, 1)), ("sc", (3, 2, 1), (1, 1, 0)),
+                                          ("bcc", (1, 1, 1), (1, 1, 1)), ("fcc", (1, 1, 1), (1, 1, 1)),
+                                          ("fcc", (1, 2, 1), (1, 0, 1))])
+def test_tiny_periodic_lattices_follow_oracle(V, O, cell, ext, pbc):
+    """Periodic axes of extent 1 or 2 (neighbour lists that repeat a site,
+    three- or four-class colourings): FP64 against the oracle."""
+    s0, ref0, s1, ref1, sums, obs, _ = _run(V, O, cell, ext, pbc, V.FP64, 1, n=4)
+    assert np.abs(s0 - ref0).max() < 1e-12
+    assert np.abs(s1 - ref1).max() < 1e-12
+    np.testing.assert_allclose(sums[-1, :7], obs[-1, :7], rtol=0, atol=1e-9)
+
+
 @pytest.mark.parametrize("cell,ext,pbc", LATTICES)
 def test_fp32_follows_oracle(V, O, cell, ext, pbc):
     s0, ref0, s1, ref1, sums, obs, _ = _run(V, O, cell, ext, pbc, V.FP32, 1, n=1)

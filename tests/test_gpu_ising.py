@@ -384,3 +384,40 @@ def test_generic_entry_batches_bit_exact(V, O, cell, ext, pbc, proposal):
         assert np.array_equal(eng.get_state(), ref)
         np.testing.assert_array_equal(sums[:, 0], obs[:, 0])
         np.testing.assert_array_equal(sums[:, 6], obs[:, 1])
+
+
+# Periodic axes of extent 1 (bcc / fcc) and 2: the neighbour lists repeat a
+# site (a bcc cell's eight neighbours are one site), odd rings and doubled
+# bonds give greedy colourings of three or four classes.
+TINY = [
+    ("sc", (2, 2, 2), (1, 1, 1)),
+    ("sc", (3, 2, 1), (1, 1, 0)),
+    ("sc", (2, 3, 4), (1, 1, 1)),
+    ("bcc", (1, 1, 1), (1, 1, 1)),
+    ("bcc", (2, 1, 3), (1, 1, 1)),
+    ("fcc", (1, 1, 1), (1, 1, 1)),
+    ("fcc", (1, 2, 1), (1, 0, 1)),
+]
+
+
+@pytest.mark.parametrize("cell,ext,pbc", TINY)
+@pytest.mark.parametrize("proposal", [0, 1])
+def test_tiny_periodic_lattices_bit_exact(V, O, cell, ext, pbc, proposal):
+    seed, J, T, mag, n = 314, 1.0, 2.5, 0.4, 8
+    H = V.hamiltonian(V.Exchange(J), V.Zeeman()) if proposal else V.hamiltonian(V.Exchange(J))
+    with _engine(V, cell, ext, pbc, H, seed, proposal=proposal) as eng:
+        g = O.Graph(O.lattice(cell, *ext, pbc))
+        eng.init_random()
+        s0 = eng.get_state()
+        assert np.array_equal(s0, g.ising_init(seed))
+        if proposal:
+            eng.set_thermostat(T, (0, 0, -1), mag)
+            sums = eng.sweeps_sums(n)
+            ref, obs = g.ising_sweeps(s0, J, -mag, T, seed, 0, n, proposal=1)
+        else:
+            eng.set_thermostat(T)
+            sums = eng.sweeps_sums(n)
+            ref, obs = g.ising_sweeps(s0, J, 0.0, T, seed, 0, n)
+        assert np.array_equal(eng.get_state(), ref)
+        np.testing.assert_array_equal(sums[:, 0], obs[:, 0])
+        np.testing.assert_array_equal(sums[:, 6], obs[:, 1])
