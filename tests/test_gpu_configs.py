@@ -88,6 +88,10 @@ def test_heisenberg_sc128_follows_oracle(V, O, precision):
 
 
 def test_msc_batch_256_replicas_bit_exact(V, O):
+    """The full c4 batch under three launch shapes (the default, the shape the
+    bench's autotuner picks on a GB300 and two words in flight at two words per
+    thread) against one oracle run: the round's last pass tallies the
+    per-replica observables, so every shape must reproduce them exactly."""
     every, rounds = 10, 2
     t2 = np.geomspace(2.0, 2.6, 64)
     t3 = np.geomspace(4.2, 4.8, 64)
@@ -97,26 +101,29 @@ def test_msc_batch_256_replicas_bit_exact(V, O):
     cpu = [(O.lattice("sc", *e, pb), t) for e, pb, t in shapes]
     ref = O.MscBatch(cpu)
     ref.init(SEED)
-    with V.Batch(gpu, J=1.0, seed=SEED, sweeps_per_round=every, exchange=True) as b:
-        assert b.info().total_replicas == 256
-        b.init_random()
-        b.run(rounds)
-        obs_ref, acc_ref = ref.run(1.0, SEED, 0, 0, every, rounds, True)
-        for rd in range(rounds):
-            counts, _ = b.observables(rd)
-            assert np.array_equal(counts, obs_ref[rd]), f"round {rd}: per-replica counts differ"
-        off = 0
-        for gi, g in enumerate(ref.groups):
-            assert np.array_equal(b.ladder(gi), g["tau"]), f"group {gi}: ladder differs"
-            acc, _ = b.swap_stats(gi)
-            n = g["temps"].size
-            assert np.array_equal(acc, acc_ref[off:off + n]), f"group {gi}: swap counts differ"
-            off += n
-            for w in range(n // 32):
-                for lane in (0, 17, 31):
-                    r = 32 * w + lane
-                    assert np.array_equal(b.get_replica(gi, r), g["spins"][r]), (gi, r)
-        assert acc_ref.sum() > 0
+    obs_ref, acc_ref = ref.run(1.0, SEED, 0, 0, every, rounds, True)
+    assert acc_ref.sum() > 0
+    for tuning in (None, (128, 8, 2), (256, 2, 2)):
+        with V.Batch(gpu, J=1.0, seed=SEED, sweeps_per_round=every, exchange=True) as b:
+            assert b.info().total_replicas == 256
+            if tuning:
+                b.set_tuning(*tuning)
+            b.init_random()
+            b.run(rounds)
+            for rd in range(rounds):
+                counts, _ = b.observables(rd)
+                assert np.array_equal(counts, obs_ref[rd]), f"{tuning}, round {rd}: per-replica counts differ"
+            off = 0
+            for gi, g in enumerate(ref.groups):
+                assert np.array_equal(b.ladder(gi), g["tau"]), f"{tuning}, group {gi}: ladder differs"
+                acc, _ = b.swap_stats(gi)
+                n = g["temps"].size
+                assert np.array_equal(acc, acc_ref[off:off + n]), f"{tuning}, group {gi}: swap counts differ"
+                off += n
+                for w in range(n // 32):
+                    for lane in (0, 17, 31):
+                        r = 32 * w + lane
+                        assert np.array_equal(b.get_replica(gi, r), g["spins"][r]), (tuning, gi, r)
 
 
 def test_hysteresis_fcc64_x64_fp64_follows_oracle(V, O):
