@@ -268,8 +268,9 @@ __device__ __forceinline__ uint32_t warp_columns(uint32_t x) {
 // Launch shape of a pass (chosen by the autotuner, vg_batch_autotune): a
 // block of TPB threads covers TPB x WPT consecutive words of one segment;
 // each thread takes its WPT words WIF at a time (WIF = 2 interleaves two
-// independent words' Philox chains and loads).  Every shape makes the same
-// decisions for every word.
+// independent words' Philox chains and loads; four at a time, 72 registers,
+// ran the c4 batch at 2,556 flips/ns against 2,586 with two).  Every shape
+// makes the same decisions for every word.
 //
 // Words still undecided after 8 planes are queued per warp and finished 32
 // at a time, so the rare long comparisons run with full warps.  MEAS: the
