@@ -421,3 +421,24 @@ def test_tiny_periodic_lattices_bit_exact(V, O, cell, ext, pbc, proposal):
         assert np.array_equal(eng.get_state(), ref)
         np.testing.assert_array_equal(sums[:, 0], obs[:, 0])
         np.testing.assert_array_equal(sums[:, 6], obs[:, 1])
+
+
+def test_largest_power_of_two_sc_lattice(V):
+    """sc 1024^3: 2^30 int8 spins, 2^29 bytes per checkerboard class (the
+    class offsets are 32-bit).  The sums the passes accumulate over two
+    measured sweeps equal a recount of the final state on the device."""
+    lat = V.Lattice.sc(1024, 1024, 1024)
+    with V.Engine(lat, V.hamiltonian(V.Exchange(1.0)), seed=3) as eng:
+        assert eng.info().path == V.PATH_STRUCTURED
+        eng.init_random()
+        eng.set_thermostat(4.5)
+        sums = eng.sweeps_sums(2)
+        cur = eng.current_sums()
+        assert sums[-1, 0] == cur[0] and sums[-1, 6] == cur[6]
+        assert abs(cur[6]) < 0.01 * lat.n_sites          # a random start stays unmagnetised
+        assert 0.3 * lat.n_sites < sums[-1, 7] < lat.n_sites  # accepted moves of the sweep
+
+
+def test_lattices_beyond_the_site_limit_are_rejected(V):
+    with pytest.raises(V.VegasGpuError, match="2\\^31-1 sites"):
+        V.Engine(V.Lattice.sc(2048, 1024, 1024), V.hamiltonian(V.Exchange(1.0)), seed=1)
