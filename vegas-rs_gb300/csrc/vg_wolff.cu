@@ -499,11 +499,13 @@ cudaError_t launch_ising_wolff(int8_t* spins, int n, int z, const int32_t* nbr, 
   const size_t smem = ising_wolff_smem(n);
   cudaError_t e = cudaFuncSetAttribute(ising_wolff_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  // about one thread per two sites, a power of two in [32, 1024]: small
-  // lattices spend their levels in barriers, not in bond draws (sc 10^3 near
-  // T_c: 83,000 cluster steps/s at 1024 threads, 98,000 at 512)
-  int tpb = 32;
-  while (tpb < 1024 && tpb < (n + 1) / 2) tpb *= 2;
+  // about one thread per four sites, a power of two in [128, 1024]: small
+  // lattices spend their levels in barriers, not in bond draws (ncu on sc
+  // 10^3 near T_c: 12 barrier stalls per issue at 512 threads; cluster
+  // steps/s at 1024 / 512 / 256 / 128 / 64 threads: 83,000 / 98,000 /
+  // 102,000 / 93,000 / 49,000; sc 6^3 best at 128-256, sc 16^3 at 1024)
+  int tpb = 128;
+  while (tpb < 1024 && tpb < (n + 3) / 4) tpb *= 2;
   ising_wolff_kernel<<<1, tpb, smem, s>>>(spins, n, z, nbr, occ, thr, key, n_steps, sums);
   return cudaGetLastError();
 }
